@@ -1,0 +1,192 @@
+"""ctypes bindings for the oracle libraries. TEST INFRASTRUCTURE ONLY.
+
+* :class:`Port` -- the C restatement (oracle/bc7_oracle.c), built by
+  ``make -C oracle port`` into ``oracle/_build/libbc7_oracle.so``.
+* :class:`Reference` -- FasTC's own encoder compiled in place by
+  ``make -C oracle ref`` into ``oracle/_ref/libfastc_ref.so`` (only where the
+  FasTC checkout is present).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libbc7_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libfastc_ref.so")
+DEFAULT_REFERENCE = "/root/reference"
+
+RNG_PER_FIT = 0
+RNG_SINGLE_STREAM = 1
+EXP_PORTABLE = 0
+EXP_LIBM = 1
+
+_u8p = C.POINTER(C.c_uint8)
+_u32p = C.POINTER(C.c_uint32)
+
+
+class Settings(C.Structure):
+    _fields_ = [("steps", C.c_uint32), ("block_modes", C.c_uint32), ("metric", C.c_uint32),
+                ("rng_mode", C.c_uint32), ("seed", C.c_uint32), ("exp_mode", C.c_uint32)]
+
+
+def _ptr(a: np.ndarray, t=_u8p):
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(t)
+
+
+def build_port() -> str:
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return PORT_SO
+
+
+def build_ref(reference: str = DEFAULT_REFERENCE) -> str | None:
+    if not os.path.isdir(os.path.join(reference, "BPTCEncoder")):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE={reference}"], check=True)
+    return REF_SO
+
+
+class Port:
+    def __init__(self, path: str = PORT_SO):
+        if not os.path.exists(path):
+            build_port()
+        lib = C.CDLL(path)
+        lib.bc7o_compress.argtypes = [_u8p, _u8p] + [C.c_uint32] * 6 + [C.POINTER(Settings), _u32p]
+        lib.bc7o_compress_mt.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32, C.POINTER(Settings),
+                                         C.c_uint32, C.c_int]
+        lib.bc7o_compress_block.argtypes = [_u32p, C.POINTER(Settings), C.c_uint32, C.c_uint32,
+                                            _u32p, _u32p, _u8p]
+        lib.bc7o_decompress.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32]
+        lib.bc7o_psnr.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32]
+        lib.bc7o_psnr.restype = C.c_double
+        lib.bc7o_block_sse.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double)]
+        lib.bc7o_box_selection.argtypes = [_u32p, C.c_uint32, _u32p]
+        lib.bc7o_tables.argtypes = [_u8p, _u8p]
+        lib.bc7o_partition.argtypes = [C.c_uint32, C.c_uint32, _u8p]
+        lib.bc7o_anchor.argtypes = [C.c_uint32] * 3
+        lib.bc7o_anchor.restype = C.c_uint32
+        lib.bc7o_fit_seed.argtypes = [C.c_uint32] * 4
+        lib.bc7o_fit_seed.restype = C.c_uint32
+        lib.bc7o_expf.argtypes = [C.c_float]
+        lib.bc7o_expf.restype = C.c_float
+        self.lib = lib
+
+    @staticmethod
+    def settings(steps=0, modes=0xFF, metric=0, rng_mode=RNG_PER_FIT, seed=0,
+                 exp_mode=EXP_PORTABLE) -> Settings:
+        return Settings(steps, modes, metric, rng_mode, seed, exp_mode)
+
+    def compress(self, img: np.ndarray, steps=0, modes=0xFF, metric=0, rng_mode=RNG_PER_FIT,
+                 seed=0, exp_mode=EXP_PORTABLE, rect=(0, 0, 0, 0), state=None) -> np.ndarray:
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape[:2]
+        out = np.zeros(w * h, dtype=np.uint8)
+        st = np.zeros(2, dtype=np.uint32) if state is None else state
+        s = self.settings(steps, modes, metric, rng_mode, seed, exp_mode)
+        rc = self.lib.bc7o_compress(_ptr(img), _ptr(out), w, h, *rect, C.byref(s), _ptr(st, _u32p))
+        if rc:
+            raise ValueError(f"bc7o_compress failed: {rc}")
+        return out
+
+    def compress_mt(self, img: np.ndarray, steps=0, modes=0xFF, metric=0, seed=0, wm_start=0,
+                    threads=None) -> np.ndarray:
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape[:2]
+        out = np.zeros(w * h, dtype=np.uint8)
+        s = self.settings(steps, modes, metric, RNG_PER_FIT, seed, EXP_PORTABLE)
+        rc = self.lib.bc7o_compress_mt(_ptr(img), _ptr(out), w, h, C.byref(s), wm_start,
+                                       threads or os.cpu_count() or 1)
+        if rc:
+            raise ValueError(f"bc7o_compress_mt failed: {rc}")
+        return out
+
+    def decompress(self, blocks: np.ndarray, w: int, h: int) -> np.ndarray:
+        blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+        out = np.zeros((h, w, 4), dtype=np.uint8)
+        self.lib.bc7o_decompress(_ptr(blocks), _ptr(out), w, h)
+        return out
+
+    def psnr(self, a: np.ndarray, b: np.ndarray) -> float:
+        a = np.ascontiguousarray(a, dtype=np.uint8)
+        b = np.ascontiguousarray(b, dtype=np.uint8)
+        return float(self.lib.bc7o_psnr(_ptr(a), _ptr(b), a.shape[1], a.shape[0]))
+
+    def block_sse(self, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+        a = np.ascontiguousarray(a, dtype=np.uint8)
+        b = np.ascontiguousarray(b, dtype=np.uint8)
+        h, w = a.shape[:2]
+        out = np.zeros((h // 4) * (w // 4), dtype=np.float64)
+        self.lib.bc7o_block_sse(_ptr(a), _ptr(b), w, h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
+    def box_selection(self, px: np.ndarray, metric=0):
+        px = np.ascontiguousarray(px, dtype=np.uint32)
+        out = np.zeros(4, dtype=np.uint32)
+        self.lib.bc7o_box_selection(_ptr(px, _u32p), metric, _ptr(out, _u32p))
+        return tuple(int(v) for v in out)
+
+    def tables(self):
+        o7 = np.zeros(512, dtype=np.uint8)
+        o6 = np.zeros(1536, dtype=np.uint8)
+        self.lib.bc7o_tables(_ptr(o7), _ptr(o6))
+        return o7, o6
+
+    def partition(self, shape: int, nsub: int) -> np.ndarray:
+        out = np.zeros(16, dtype=np.uint8)
+        self.lib.bc7o_partition(shape, nsub, _ptr(out))
+        return out
+
+
+class Reference:
+    """FasTC's encoder itself, compiled in place (x86-64 container only)."""
+
+    def __init__(self, path: str = REF_SO):
+        lib = C.CDLL(path)
+        lib.ref_set_seed.argtypes = [C.c_uint32]
+        lib.ref_get_seed.restype = C.c_uint32
+        lib.ref_set_wm.argtypes = [C.c_uint32]
+        lib.ref_get_wm.restype = C.c_uint32
+        lib.ref_compress.argtypes = [_u8p, _u8p] + [C.c_uint32] * 8 + [C.c_int]
+        lib.ref_compress_block.argtypes = [_u32p, _u8p, C.c_uint32, C.c_uint32, C.c_int]
+        lib.ref_decompress.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32]
+        lib.ref_box_selection.argtypes = [_u32p, C.c_int, _u32p]
+        lib.ref_tables.argtypes = [_u8p, _u8p]
+        self.lib = lib
+
+    def compress(self, img: np.ndarray, steps=0, modes=0xFF, metric=0, seed=None, wm=0,
+                 rect=None) -> np.ndarray:
+        """Fresh watermark counter (next single-colour block uses entry `wm`)."""
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape[:2]
+        out = np.zeros(w * h, dtype=np.uint8)
+        if seed is not None:
+            self.lib.ref_set_seed(seed)
+        self.lib.ref_set_wm((wm - 1) & 0xFFFFFFFF if wm else 0xFFFFFFFF)
+        x0, y0, x1, y1 = rect if rect else (0, 0, w, h)
+        self.lib.ref_compress(_ptr(img), _ptr(out), w, h, x0, y0, x1, y1, steps, modes, metric)
+        return out
+
+    def decompress(self, blocks: np.ndarray, w: int, h: int) -> np.ndarray:
+        blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+        out = np.zeros((h, w, 4), dtype=np.uint8)
+        self.lib.ref_decompress(_ptr(blocks), _ptr(out), w, h)
+        return out
+
+    def box_selection(self, px: np.ndarray, metric=0):
+        px = np.ascontiguousarray(px, dtype=np.uint32)
+        out = np.zeros(4, dtype=np.uint32)
+        self.lib.ref_box_selection(_ptr(px, _u32p), metric, _ptr(out, _u32p))
+        return tuple(int(v) for v in out)
+
+    def tables(self):
+        o7 = np.zeros(512, dtype=np.uint8)
+        o6 = np.zeros(1536, dtype=np.uint8)
+        self.lib.ref_tables(_ptr(o7), _ptr(o6))
+        return o7, o6
