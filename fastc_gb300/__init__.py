@@ -1,0 +1,16 @@
+"""GB300-native BC7 (BPTC) texture encoder with FasTC's compression API.
+
+The compute path is hand-written sm_103a CUDA in ``fastc_gb300/csrc`` behind
+the C ABI in ``include/fastc_bc7.h``; this package is the Python mirror of
+FasTC's BPTC interface (:mod:`fastc_gb300.bptc`), the batching/serving
+runtime, and the seeded synthetic workloads.
+"""
+from .bptc import (BC7Error, BlockMode, CompressionJob, CompressionJobList, CompressionSettings,
+                   ErrorMetric, Plan, compress, compress_atomic, compress_image_data, compress_jobs,
+                   decompress, get_launch_shape, set_launch_shape)
+
+__all__ = [
+    "BC7Error", "BlockMode", "CompressionJob", "CompressionJobList", "CompressionSettings",
+    "ErrorMetric", "Plan", "compress", "compress_atomic", "compress_image_data", "compress_jobs",
+    "decompress", "get_launch_shape", "set_launch_shape",
+]

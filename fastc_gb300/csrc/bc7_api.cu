@@ -1,0 +1,481 @@
+// C-ABI implementation of the GB300 BC7 encoder (include/fastc_bc7.h).
+//
+// Host-memory calls stage the job's texel rows into a grow-only device
+// buffer, launch the encoder on a private stream and copy the blocks back.
+// Device-memory calls are asynchronous and take their scratch from the
+// stream-ordered allocator of the caller's stream. Plans capture the whole
+// encode pipeline of a fixed job set into one CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bc7_kernels.cuh"
+#include "fastc_bc7.h"
+
+using fastc::EncodeScratch;
+using fastc::JobDev;
+using fastc::LaunchShape;
+
+namespace {
+
+thread_local std::string t_last_error;
+std::mutex g_mu;
+int g_warps = 4;
+int g_ctas_per_sm = 0;  // 0: as many as fit
+
+fastc_bc7_status fail_cuda(cudaError_t e) {
+  t_last_error = cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return FASTC_BC7_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return FASTC_BC7_ERR_NO_DEVICE;
+  return FASTC_BC7_ERR_CUDA;
+}
+
+#define CK(expr)                              \
+  do {                                        \
+    cudaError_t e_ = (expr);                  \
+    if (e_ != cudaSuccess) return fail_cuda(e_); \
+  } while (0)
+
+bool settings_ok(const fastc_bc7_settings &s, fastc_bc7_status *why) {
+  if (s.shape_selection_fn != nullptr) {
+    *why = FASTC_BC7_ERR_UNSUPPORTED;
+    return false;
+  }
+  if ((s.block_modes & 0xFFu) == 0 || s.error_metric > 1 || s.steps > 256) {
+    *why = FASTC_BC7_ERR_INVALID_ARGUMENT;
+    return false;
+  }
+  return true;
+}
+
+// Raster block range of a job (CP:1473-1520 semantics), or false.
+bool job_range(const fastc_bc7_job &j, uint32_t *first, uint32_t *count) {
+  if (j.width == 0 || j.height == 0 || (j.width | j.height) & 3) return false;
+  if ((j.x_start | j.y_start | j.x_end | j.y_end) & 3) return false;
+  if (j.x_start >= j.width || j.y_start >= j.height || j.x_end > j.width) return false;
+  const uint64_t bw = j.width / 4, bh = j.height / 4;
+  if (bw * bh > 0xFFFFFFFFull) return false;
+  const uint64_t start = (uint64_t)(j.y_start / 4) * bw + j.x_start / 4;
+  const uint64_t end = j.y_end > j.height - 4 ? bw * bh : (uint64_t)(j.y_end / 4) * bw + j.x_end / 4;
+  *first = (uint32_t)start;
+  *count = end > start ? (uint32_t)(end - start) : 0u;
+  return true;
+}
+
+int current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) return -1;
+  return d;
+}
+
+LaunchShape pick_shape(uint64_t total) {
+  const int dev = current_device();
+  const int sms = fastc::device_sm_count(dev);
+  int warps = g_warps;
+  int per_sm = g_ctas_per_sm > 0 ? g_ctas_per_sm : fastc::encode_ctas_per_sm(warps);
+  if (per_sm < 1) per_sm = 1;
+  uint64_t ctas = (uint64_t)sms * (uint64_t)per_sm;
+  const uint64_t need = (total + (uint64_t)warps - 1) / (uint64_t)warps;
+  if (ctas > need) ctas = need;
+  if (ctas < 1) ctas = 1;
+  return LaunchShape{warps, (int)ctas};
+}
+
+size_t scratch_bytes(uint64_t total) {
+  const uint64_t nchunks = (total + fastc::kRankChunk - 1) / fastc::kRankChunk;
+  return 256 + ((nchunks * 4 + 255) & ~255ull) + total * 2 + 256;
+}
+
+EncodeScratch carve_scratch(void *base, uint64_t total) {
+  uint8_t *p = static_cast<uint8_t *>(base);
+  const uint64_t nchunks = (total + fastc::kRankChunk - 1) / fastc::kRankChunk;
+  EncodeScratch s;
+  s.counter = reinterpret_cast<unsigned long long *>(p);
+  s.status = reinterpret_cast<uint32_t *>(p + 8);
+  s.chunk_prefix = reinterpret_cast<uint32_t *>(p + 256);
+  s.rank_local = reinterpret_cast<uint16_t *>(p + 256 + ((nchunks * 4 + 255) & ~255ull));
+  return s;
+}
+
+JobDev make_job(const fastc_bc7_job &j, const fastc_bc7_settings &s, uint32_t first,
+                uint32_t count, uint64_t begin) {
+  JobDev d;
+  d.in = j.in;
+  d.out = j.out;
+  d.width = j.width;
+  d.height = j.height;
+  d.row0 = 0;
+  d.out_first = 0;
+  d.first = first;
+  d.nblocks = count;
+  d.steps = s.steps;
+  d.modes = s.block_modes & 0xFFu;
+  d.metric = s.error_metric;
+  d.seed = s.seed;
+  d.wm_start = s.watermark_start;
+  d.flags = 0;
+  d.begin = begin;
+  return d;
+}
+
+uint32_t align_flags(const void *in, const void *out) {
+  uint32_t f = 0;
+  if ((reinterpret_cast<uintptr_t>(in) & 15) == 0) f |= fastc::kJobIn16;
+  if ((reinterpret_cast<uintptr_t>(out) & 15) == 0) f |= fastc::kJobOut16;
+  return f;
+}
+
+// Grow-only device buffer.
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) cap = n;
+    return e;
+  }
+};
+
+// State of the host-memory entry points (guarded by g_mu).
+struct HostCtx {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  DevBuf in, out, jobs, scratch;
+} g_host;
+
+fastc_bc7_status host_ctx_init() {
+  const int dev = current_device();
+  if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
+  if (g_host.device != dev) {
+    if (g_host.stream) cudaStreamDestroy(g_host.stream);
+    g_host = HostCtx();
+    CK(cudaStreamCreateWithFlags(&g_host.stream, cudaStreamNonBlocking));
+    g_host.device = dev;
+  }
+  fastc::upload_tables(dev);
+  return FASTC_BC7_OK;
+}
+
+const fastc_bc7_settings &settings_for(const fastc_bc7_settings *s, int per_job, uint32_t i,
+                                       const fastc_bc7_settings &dflt) {
+  if (!s) return dflt;
+  return per_job ? s[i] : s[0];
+}
+
+// Host-memory batch: stage rows, launch, copy back. Caller holds g_mu.
+fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7_settings *s,
+                          int per_job) {
+  fastc_bc7_settings dflt;
+  fastc_bc7_settings_default(&dflt);
+  std::vector<JobDev> dj(n);
+  std::vector<size_t> in_off(n), out_off(n), in_bytes(n);
+  size_t in_total = 0, out_total = 0;
+  uint64_t total = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    const fastc_bc7_settings &st = settings_for(s, per_job, i, dflt);
+    fastc_bc7_status why;
+    if (!settings_ok(st, &why)) return why;
+    uint32_t first, count;
+    if (!jobs[i].in || !jobs[i].out || !job_range(jobs[i], &first, &count))
+      return FASTC_BC7_ERR_INVALID_ARGUMENT;
+    dj[i] = make_job(jobs[i], st, first, count, total);
+    const uint32_t bw = jobs[i].width / 4;
+    const uint32_t r0 = count ? first / bw : 0, r1 = count ? (first + count - 1) / bw : 0;
+    in_bytes[i] = count ? (size_t)(r1 - r0 + 1) * 4 * jobs[i].width * 4 : 0;
+    dj[i].row0 = r0 * 4;
+    dj[i].out_first = first;
+    in_off[i] = in_total;
+    out_off[i] = out_total;
+    in_total += (in_bytes[i] + 255) & ~(size_t)255;
+    out_total += ((size_t)count * 16 + 255) & ~(size_t)255;
+    total += count;
+  }
+  if (total == 0) return FASTC_BC7_OK;
+  fastc_bc7_status st = host_ctx_init();
+  if (st != FASTC_BC7_OK) return st;
+  CK(g_host.in.ensure(in_total));
+  CK(g_host.out.ensure(out_total));
+  CK(g_host.jobs.ensure(n * sizeof(JobDev)));
+  CK(g_host.scratch.ensure(scratch_bytes(total)));
+  cudaStream_t cs = g_host.stream;
+  uint8_t *din = static_cast<uint8_t *>(g_host.in.p);
+  uint8_t *dout = static_cast<uint8_t *>(g_host.out.p);
+  for (uint32_t i = 0; i < n; i++) {
+    if (!dj[i].nblocks) continue;
+    const uint8_t *src = jobs[i].in + (size_t)dj[i].row0 * jobs[i].width * 4;
+    CK(cudaMemcpyAsync(din + in_off[i], src, in_bytes[i], cudaMemcpyHostToDevice, cs));
+    dj[i].in = din + in_off[i];
+    dj[i].out = dout + out_off[i];
+    dj[i].flags = fastc::kJobIn16 | fastc::kJobOut16;
+  }
+  CK(cudaMemcpyAsync(g_host.jobs.p, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs));
+  const EncodeScratch sc = carve_scratch(g_host.scratch.p, total);
+  const int le = fastc::launch_encode(static_cast<const JobDev *>(g_host.jobs.p), (int)n, total,
+                                      sc, pick_shape(total), cs);
+  if (le) return fail_cuda((cudaError_t)le);
+  for (uint32_t i = 0; i < n; i++) {
+    if (!dj[i].nblocks) continue;
+    CK(cudaMemcpyAsync(jobs[i].out + (size_t)dj[i].first * 16, dout + out_off[i],
+                       (size_t)dj[i].nblocks * 16, cudaMemcpyDeviceToHost, cs));
+  }
+  CK(cudaStreamSynchronize(cs));
+  return FASTC_BC7_OK;
+}
+
+}  // namespace
+
+struct fastc_bc7_plan_s {
+  int device = -1;
+  JobDev *d_jobs = nullptr;
+  void *d_scratch = nullptr;
+  uint64_t total = 0;
+  int njobs = 0;
+  EncodeScratch sc{};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+void fastc_bc7_settings_default(fastc_bc7_settings *s) {
+  if (!s) return;
+  std::memset(s, 0, sizeof(*s));
+  s->block_modes = FASTC_BC7_ALL_MODES;
+  s->error_metric = 0;
+  s->steps = 50;
+}
+
+const char *fastc_bc7_status_string(fastc_bc7_status st) {
+  switch (st) {
+    case FASTC_BC7_OK: return "ok";
+    case FASTC_BC7_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case FASTC_BC7_ERR_UNSUPPORTED: return "unsupported";
+    case FASTC_BC7_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case FASTC_BC7_ERR_CUDA: return "CUDA error";
+    case FASTC_BC7_ERR_BUDGET: return "over memory budget";
+    case FASTC_BC7_ERR_TIMEOUT: return "timed out";
+    case FASTC_BC7_ERR_NOT_FOUND: return "not found";
+    case FASTC_BC7_ERR_CANCELLED: return "cancelled";
+    case FASTC_BC7_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "internal error";
+  }
+}
+
+const char *fastc_bc7_last_error(void) { return t_last_error.c_str(); }
+uint32_t fastc_bc7_abi_version(void) { return FASTC_BC7_ABI_VERSION; }
+
+uint64_t fastc_bc7_job_blocks(const fastc_bc7_job *job) {
+  uint32_t first, count;
+  if (!job || !job_range(*job, &first, &count)) return 0;
+  return count;
+}
+
+fastc_bc7_status fastc_bc7_compress(const fastc_bc7_job *job, const fastc_bc7_settings *s) {
+  if (!job) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(g_mu);
+  return run_host(job, 1, s, 0);
+}
+
+fastc_bc7_status fastc_bc7_compress_batch(const fastc_bc7_job *jobs, uint32_t n,
+                                          const fastc_bc7_settings *settings,
+                                          int per_job_settings) {
+  if (!jobs && n) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  if (n == 0) return FASTC_BC7_OK;
+  std::lock_guard<std::mutex> lk(g_mu);
+  return run_host(jobs, n, settings, per_job_settings);
+}
+
+fastc_bc7_status fastc_bc7_compress_image(const uint8_t *rgba, uint32_t width, uint32_t height,
+                                          uint8_t *cmp, size_t cmp_size,
+                                          const fastc_bc7_settings *s) {
+  if (!rgba || !cmp || (size_t)width * height > cmp_size) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  fastc_bc7_job j{rgba, cmp, width, height, 0, 0, width, height};
+  return fastc_bc7_compress(&j, s);
+}
+
+fastc_bc7_status fastc_bc7_decompress(const uint8_t *blocks, uint8_t *rgba, uint32_t width,
+                                      uint32_t height, int spec) {
+  if (!blocks || !rgba || width == 0 || height == 0) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(g_mu);
+  fastc_bc7_status st = host_ctx_init();
+  if (st != FASTC_BC7_OK) return st;
+  const size_t nb = (size_t)((width + 3) / 4) * ((height + 3) / 4);
+  const size_t img = (size_t)width * height * 4;
+  CK(g_host.in.ensure(nb * 16));
+  CK(g_host.out.ensure(img));
+  cudaStream_t cs = g_host.stream;
+  CK(cudaMemcpyAsync(g_host.in.p, blocks, nb * 16, cudaMemcpyHostToDevice, cs));
+  const int le = fastc::launch_decode(static_cast<const uint8_t *>(g_host.in.p),
+                                      static_cast<uint8_t *>(g_host.out.p), width, height, spec, cs);
+  if (le) return fail_cuda((cudaError_t)le);
+  CK(cudaMemcpyAsync(rgba, g_host.out.p, img, cudaMemcpyDeviceToHost, cs));
+  CK(cudaStreamSynchronize(cs));
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_compress_device(const fastc_bc7_job *jobs, uint32_t n,
+                                           const fastc_bc7_settings *settings,
+                                           int per_job_settings, void *stream) {
+  if (!jobs && n) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  if (n == 0) return FASTC_BC7_OK;
+  fastc_bc7_settings dflt;
+  fastc_bc7_settings_default(&dflt);
+  std::vector<JobDev> dj(n);
+  uint64_t total = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    const fastc_bc7_settings &st = settings_for(settings, per_job_settings, i, dflt);
+    fastc_bc7_status why;
+    if (!settings_ok(st, &why)) return why;
+    uint32_t first, count;
+    if (!jobs[i].in || !jobs[i].out || !job_range(jobs[i], &first, &count) ||
+        (reinterpret_cast<uintptr_t>(jobs[i].in) & 3) || (reinterpret_cast<uintptr_t>(jobs[i].out) & 3))
+      return FASTC_BC7_ERR_INVALID_ARGUMENT;
+    dj[i] = make_job(jobs[i], st, first, count, total);
+    dj[i].flags = align_flags(jobs[i].in, jobs[i].out);
+    total += count;
+  }
+  if (total == 0) return FASTC_BC7_OK;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    const int dev = current_device();
+    if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
+    fastc::upload_tables(dev);
+  }
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  void *buf = nullptr;
+  const size_t jb = (n * sizeof(JobDev) + 255) & ~(size_t)255;
+  CK(cudaMallocAsync(&buf, jb + scratch_bytes(total), cs));
+  cudaError_t e = cudaMemcpyAsync(buf, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) {
+    const EncodeScratch sc = carve_scratch(static_cast<uint8_t *>(buf) + jb, total);
+    LaunchShape shape;
+    {
+      std::lock_guard<std::mutex> lk(g_mu);
+      shape = pick_shape(total);
+    }
+    e = (cudaError_t)fastc::launch_encode(static_cast<const JobDev *>(buf), (int)n, total, sc, shape,
+                                          cs);
+  }
+  cudaError_t ef = cudaFreeAsync(buf, cs);
+  if (e != cudaSuccess) return fail_cuda(e);
+  if (ef != cudaSuccess) return fail_cuda(ef);
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_decompress_device(const uint8_t *blocks, uint8_t *rgba, uint32_t width,
+                                             uint32_t height, int spec, void *stream) {
+  if (!blocks || !rgba || width == 0 || height == 0) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  if (reinterpret_cast<uintptr_t>(rgba) & 3) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  const int le = fastc::launch_decode(blocks, rgba, width, height, spec, stream);
+  if (le) return fail_cuda((cudaError_t)le);
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
+                                       const fastc_bc7_settings *settings, int per_job_settings,
+                                       fastc_bc7_plan *out) {
+  if (!out || (!jobs && n) || n == 0) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  fastc_bc7_settings dflt;
+  fastc_bc7_settings_default(&dflt);
+  std::vector<JobDev> dj(n);
+  uint64_t total = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    const fastc_bc7_settings &st = settings_for(settings, per_job_settings, i, dflt);
+    fastc_bc7_status why;
+    if (!settings_ok(st, &why)) return why;
+    uint32_t first, count;
+    if (!jobs[i].in || !jobs[i].out || !job_range(jobs[i], &first, &count) ||
+        (reinterpret_cast<uintptr_t>(jobs[i].in) & 3) || (reinterpret_cast<uintptr_t>(jobs[i].out) & 3))
+      return FASTC_BC7_ERR_INVALID_ARGUMENT;
+    dj[i] = make_job(jobs[i], st, first, count, total);
+    dj[i].flags = align_flags(jobs[i].in, jobs[i].out);
+    total += count;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  const int dev = current_device();
+  if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
+  fastc::upload_tables(dev);
+  fastc_bc7_plan p = new fastc_bc7_plan_s();
+  p->device = dev;
+  p->total = total;
+  p->njobs = (int)n;
+  cudaStream_t cs = nullptr;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p->d_jobs), n * sizeof(JobDev));
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_scratch, scratch_bytes(total > 0 ? total : 1));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p->d_jobs, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    p->sc = carve_scratch(p->d_scratch, total);
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      const int le = fastc::launch_encode(p->d_jobs, (int)n, total, p->sc, pick_shape(total), cs);
+      cudaError_t ee = cudaStreamEndCapture(cs, &p->graph);
+      e = le ? (cudaError_t)le : ee;
+    }
+  }
+  if (e == cudaSuccess && !p->graph) e = cudaErrorStreamCaptureInvalidated;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+  if (cs) cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    fastc_bc7_plan_destroy(p);
+    return fail_cuda(e);
+  }
+  *out = p;
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_plan_launch(fastc_bc7_plan p, void *stream) {
+  if (!p || !p->exec) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  CK(cudaGraphLaunch(p->exec, static_cast<cudaStream_t>(stream)));
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_plan_flags(fastc_bc7_plan p, uint32_t *flags) {
+  if (!p || !flags) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(flags, p->sc.status, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  return FASTC_BC7_OK;
+}
+
+uint64_t fastc_bc7_plan_blocks(fastc_bc7_plan p) { return p ? p->total : 0; }
+
+fastc_bc7_status fastc_bc7_plan_destroy(fastc_bc7_plan p) {
+  if (!p) return FASTC_BC7_OK;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->d_jobs) cudaFree(p->d_jobs);
+  if (p->d_scratch) cudaFree(p->d_scratch);
+  delete p;
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_set_launch_shape(int warps_per_cta, int ctas_per_sm) {
+  if (warps_per_cta != 0 && warps_per_cta != 1 && warps_per_cta != 2 && warps_per_cta != 4 &&
+      warps_per_cta != 8)
+    return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  if (ctas_per_sm < 0 || ctas_per_sm > 64) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (warps_per_cta) g_warps = warps_per_cta;
+  if (ctas_per_sm) g_ctas_per_sm = ctas_per_sm;
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_get_launch_shape(int *warps_per_cta, int *ctas_per_sm) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (warps_per_cta) *warps_per_cta = g_warps;
+  if (ctas_per_sm) *ctas_per_sm = g_ctas_per_sm;
+  return FASTC_BC7_OK;
+}
+
+}  // extern "C"

@@ -118,7 +118,12 @@ def tile_mix(seed: int = 2, width: int = 2048, height: int = 2048, x0: int = 0, 
     tx, ty = xs // tile, ys // tile
     lx = (xs - tx * tile) - (tile - 1) / 2.0
     ly = (ys - ty * tile) - (tile - 1) / 2.0
-    kind, c0, c1, ang, off = _tile_params(seed, tx, ty)
+    # per-tile parameters on the tile grid, then broadcast to the texels
+    tx0, ty0 = x0 // tile, y0 // tile
+    gtx, gty = np.mgrid[ty0:int(ty.max()) + 1, tx0:int(tx.max()) + 1][::-1]
+    params = _tile_params(seed, gtx.astype(np.int64), gty.astype(np.int64))
+    ix, iy = tx - tx0, ty - ty0
+    kind, c0, c1, ang, off = (p[iy, ix] for p in params)
     ca, sa = np.cos(ang), np.sin(ang)
     proj = lx * ca + ly * sa
     t = np.clip(proj / (tile * 0.7071) + 0.5, 0.0, 1.0)[..., None]

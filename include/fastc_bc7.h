@@ -1,0 +1,164 @@
+/*
+ * fastc_bc7.h -- C ABI of the GB300 BC7 (BPTC) encoder.
+ *
+ * Drop-in boundary for FasTC's BPTC encode path. Every entry point takes
+ * plain pointers and sizes and returns a status code; none throws, none
+ * keeps a pointer after it returns (plans excepted, see below).
+ *
+ * Reference interfaces replaced (paths within the FasTC project):
+ *   fastc_bc7_compress        BPTCC::Compress(const CompressionJob&,
+ *                             CompressionSettings)
+ *                             BPTCEncoder/include/FasTC/BPTCCompressor.h:166
+ *                             (and the Core plugin slot CompressionFunc,
+ *                             Core/src/CompressionFuncs.h:126, that
+ *                             Core/src/TexComp.cpp:55-57 fills with it)
+ *   fastc_bc7_compress_batch  BPTCC::CompressAtomic(CompressionJobList&)
+ *                             BPTCEncoder/include/FasTC/BPTCCompressor.h:189
+ *   fastc_bc7_compress_image  CompressImageData(...)
+ *                             Core/include/FasTC/TexComp.h:81-88
+ *   fastc_bc7_decompress      BPTCC::Decompress(const DecompressionJob&)
+ *                             BPTCEncoder/include/FasTC/BPTCCompressor.h:216
+ *
+ * Differences a caller can observe:
+ *   * steps > 0 draws annealing randomness from a per-fit stream seeded by
+ *     `seed` and the block position, so results repeat exactly and do not
+ *     depend on batching; FasTC seeds one global stream from time(NULL)
+ *     (BPTCEncoder/src/Compressor.cpp:358).
+ *   * A non-NULL shape_selection_fn (a host callback) is rejected with
+ *     FASTC_BC7_ERR_UNSUPPORTED: the search runs on the GPU.
+ *   * Where FasTC's selected mode set comes out empty (undefined behaviour
+ *     there), the encoder searches the caller's block_modes instead.
+ */
+#ifndef FASTC_BC7_H_
+#define FASTC_BC7_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FASTC_BC7_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define FASTC_BC7_API __attribute__((visibility("default")))
+#else
+#define FASTC_BC7_API
+#endif
+
+typedef enum {
+  FASTC_BC7_OK = 0,
+  FASTC_BC7_ERR_INVALID_ARGUMENT = 1, /* bad sizes, alignment or pointers */
+  FASTC_BC7_ERR_UNSUPPORTED = 2,      /* e.g. a host shape-selection callback */
+  FASTC_BC7_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed */
+  FASTC_BC7_ERR_CUDA = 4,             /* CUDA runtime error; see fastc_bc7_last_error */
+  FASTC_BC7_ERR_BUDGET = 5,           /* request larger than the server's memory budget */
+  FASTC_BC7_ERR_TIMEOUT = 6,          /* wait gave up */
+  FASTC_BC7_ERR_NOT_FOUND = 7,        /* unknown request id */
+  FASTC_BC7_ERR_CANCELLED = 8,        /* request cancelled */
+  FASTC_BC7_ERR_NO_DEVICE = 9,        /* no usable CUDA device */
+  FASTC_BC7_ERR_INTERNAL = 10
+} fastc_bc7_status;
+
+/* EBlockMode (BPTCCompressor.h:56-65): bit m enables BC7 mode m. */
+#define FASTC_BC7_ALL_MODES 0xFFu
+
+/* Mirrors BPTCC::CompressionSettings (BPTCCompressor.h:123-158) plus the
+ * GPU-side knobs. Use fastc_bc7_settings_default() to initialise. */
+typedef struct {
+  const void *shape_selection_fn;        /* m_ShapeSelectionFn: must be NULL */
+  const void *shape_selection_user_data; /* m_ShapeSelectionUserData: ignored */
+  uint32_t block_modes;                  /* m_BlockModes, default 0xFF */
+  uint32_t error_metric;                 /* m_ErrorMetric: 0 uniform, 1 nonuniform */
+  uint32_t steps;                        /* m_NumSimulatedAnnealingSteps (tc -q), default 50 */
+  uint32_t seed;                         /* annealing seed, default 0 */
+  uint32_t watermark_start;              /* watermark entry of the first single-colour
+                                            block (FasTC's gWMVal + 1), default 0 */
+  uint32_t reserved;
+} fastc_bc7_settings;
+
+/* One FasTC CompressionJob (Base/include/FasTC/CompressionJob.h:40-140):
+ * `in` holds width*height RGBA8 texels (R in the lowest byte), `out`
+ * receives width*height bytes of BC7 blocks in raster order. The job covers
+ * the raster range of blocks from (x_start, y_start) up to, on row y_end,
+ * x_end (exclusive); y_end > height - 4 means "to the end of the image".
+ * All four are pixel coordinates and multiples of 4; width and height are
+ * multiples of 4. Only the blocks of the range are written. */
+typedef struct {
+  const uint8_t *in;
+  uint8_t *out;
+  uint32_t width, height;
+  uint32_t x_start, y_start, x_end, y_end;
+} fastc_bc7_job;
+
+FASTC_BC7_API void fastc_bc7_settings_default(fastc_bc7_settings *s);
+FASTC_BC7_API const char *fastc_bc7_status_string(fastc_bc7_status st);
+/* Text of the last CUDA error seen by this thread's calls (or ""). */
+FASTC_BC7_API const char *fastc_bc7_last_error(void);
+FASTC_BC7_API uint32_t fastc_bc7_abi_version(void);
+
+/* Number of blocks a job covers (after validation), or 0 if invalid. */
+FASTC_BC7_API uint64_t fastc_bc7_job_blocks(const fastc_bc7_job *job);
+
+/* --- Host-memory entry points: copy in, encode, copy out, synchronise. --- */
+
+/* BPTCC::Compress: one job, host buffers. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_compress(const fastc_bc7_job *job, const fastc_bc7_settings *s);
+
+/* BPTCC::CompressAtomic: every job of a list compressed in one batched
+ * launch (FasTC's CompressAtomic always runs with default settings; pass
+ * NULL for the same behaviour). settings may be one entry for all jobs or,
+ * with per_job_settings != 0, an array of n. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_compress_batch(const fastc_bc7_job *jobs, uint32_t n,
+                                          const fastc_bc7_settings *settings,
+                                          int per_job_settings);
+
+/* CompressImageData for BC7: whole image, host buffers; cmp_size must be at
+ * least width*height bytes. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_compress_image(const uint8_t *rgba, uint32_t width,
+                                          uint32_t height, uint8_t *cmp, size_t cmp_size,
+                                          const fastc_bc7_settings *s);
+
+/* BPTCC::Decompress: host buffers; rgba receives width*height*4 bytes.
+ * spec_semantics = 0 decodes exactly as FasTC's decoder, 1 follows the
+ * BC7 specification for mode-4 blocks with index mode 1 (the only
+ * difference). */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_decompress(const uint8_t *blocks, uint8_t *rgba, uint32_t width,
+                                      uint32_t height, int spec_semantics);
+
+/* --- Device-memory entry points: asynchronous on `stream`. ---
+ * in/out of every job are device pointers to whole textures. Scratch is
+ * taken from the stream-ordered allocator on `stream`. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_compress_device(const fastc_bc7_job *jobs, uint32_t n,
+                                           const fastc_bc7_settings *settings,
+                                           int per_job_settings, void *stream);
+FASTC_BC7_API fastc_bc7_status fastc_bc7_decompress_device(const uint8_t *blocks, uint8_t *rgba,
+                                             uint32_t width, uint32_t height,
+                                             int spec_semantics, void *stream);
+
+/* --- Plans: a fixed set of device jobs captured once in a CUDA graph. ---
+ * The job table, scratch and the graph are built at creation; each launch
+ * replays the whole batch with one graph launch. The caller keeps the
+ * jobs' device buffers alive until the plan is destroyed. */
+typedef struct fastc_bc7_plan_s *fastc_bc7_plan;
+
+FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
+                                       const fastc_bc7_settings *settings,
+                                       int per_job_settings, fastc_bc7_plan *out);
+FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_launch(fastc_bc7_plan plan, void *stream);
+/* Device status bits of the plan's last completed launch (bit 0: a k-means
+ * loop reached its iteration bound). Synchronises with the plan's work. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_flags(fastc_bc7_plan plan, uint32_t *flags);
+FASTC_BC7_API uint64_t fastc_bc7_plan_blocks(fastc_bc7_plan plan);
+FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_destroy(fastc_bc7_plan plan);
+
+/* Launch geometry: warps per CTA (1, 2, 4 or 8) and CTAs per SM of the
+ * persistent encoder; 0 keeps the current value. Returns the values in use. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_set_launch_shape(int warps_per_cta, int ctas_per_sm);
+FASTC_BC7_API fastc_bc7_status fastc_bc7_get_launch_shape(int *warps_per_cta, int *ctas_per_sm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FASTC_BC7_H_ */

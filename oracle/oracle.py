@@ -173,6 +173,33 @@ class Reference:
         self.lib.ref_compress(_ptr(img), _ptr(out), w, h, x0, y0, x1, y1, steps, modes, metric)
         return out
 
+    def compress_threads(self, img: np.ndarray, steps=50, threads=1, seed=None) -> np.ndarray:
+        """`tc -t N`: N threads compress disjoint block ranges of one image,
+        split like Core/src/ThreadGroup.cpp:133-192 (they share FasTC's
+        global RNG state, racing on it exactly as the reference does)."""
+        import threading
+
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape[:2]
+        out = np.zeros(w * h, dtype=np.uint8)
+        if seed is not None:
+            self.lib.ref_set_seed(seed)
+        bw = w // 4
+        nb = bw * (h // 4)
+        per = nb // threads + (1 if nb % threads else 0)
+        ranges, done = [], 0
+        while done < nb:
+            e = min(done + per, nb)
+            ranges.append(((done % bw) * 4, (done // bw) * 4, (e % bw) * 4, (e // bw) * 4))
+            done = e
+        ts = [threading.Thread(target=self.lib.ref_compress,
+                               args=(_ptr(img), _ptr(out), w, h, *r, steps, 0xFF, 0)) for r in ranges]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        return out
+
     def decompress(self, blocks: np.ndarray, w: int, h: int) -> np.ndarray:
         blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
         out = np.zeros((h, w, 4), dtype=np.uint8)

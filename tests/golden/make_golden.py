@@ -1,0 +1,97 @@
+"""Regenerate the golden BC7 fixtures from FasTC's own encoder.
+
+Runs only where the FasTC checkout is available (it builds
+oracle/_ref/libfastc_ref.so from those sources in place):
+
+    python tests/golden/make_golden.py [--reference /path/to/FasTC]
+
+Every fixture is the reference's output on a seeded synthetic image from
+fastc_gb300.synth; manifest.json records the input hashes, settings and
+the reference's PSNR so the tests can check the generators too.
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from fastc_gb300 import synth  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+# name -> (generator call, steps, metric, pinned LCG seed or None)
+CASES = {
+    "c1_q0": ("gradient_noise_alpha_ramp(1, 256, 256)", 0, 0, None),
+    "tile_q0": ("tile_mix(2, 128, 128)", 0, 0, None),
+    "radial_q0": ("tile_mix_radial_alpha(5, 128, 128, 1000, 2000)", 0, 0, None),
+    "c1_q0_nonuniform": ("gradient_noise_alpha_ramp(1, 128, 128)", 0, 1, None),
+    "c1_q8_seed": ("gradient_noise_alpha_ramp(1, 128, 128)", 8, 0, 0x1234567),
+    "tile_q50_seed": ("tile_mix(2, 64, 64)", 50, 0, 0xBEEF),
+    "radial_q16_seed": ("tile_mix_radial_alpha(5, 64, 64, 3000, 3000)", 16, 0, 0xC0FFEE),
+}
+
+# PSNR reference points at q50: the reference with several pinned seeds
+QUALITY = {
+    "tile_q50_psnr": ("tile_mix(21, 512, 512)", 50, [11, 22, 33]),
+    "radial_q50_psnr": ("tile_mix_radial_alpha(5, 512, 512, 4096, 1024)", 50, [11, 22, 33]),
+}
+
+
+def make(expr: str) -> np.ndarray:
+    return eval("synth." + expr, {"synth": synth})
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=O.DEFAULT_REFERENCE)
+    args = ap.parse_args()
+    if not O.build_ref(args.reference):
+        sys.exit("FasTC checkout not found; cannot regenerate fixtures")
+    ref = O.Reference()
+    manifest = {"cases": {}, "quality": {}}
+    for name, (expr, steps, metric, seed) in CASES.items():
+        img = make(expr)
+        blocks = ref.compress(img, steps=steps, metric=metric, seed=seed)
+        blocks.tofile(os.path.join(HERE, name + ".bin"))
+        dec = ref.decompress(blocks, img.shape[1], img.shape[0])
+        manifest["cases"][name] = {
+            "image": expr, "steps": steps, "metric": metric, "lcg_seed": seed,
+            "input_sha256": sha(img), "blocks_sha256": sha(blocks), "decoded_sha256": sha(dec),
+        }
+        print(name, len(blocks) // 16, "blocks")
+    port = O.Port()
+    for name, (expr, steps, seeds) in QUALITY.items():
+        img = make(expr)
+        psnrs, sses = [], []
+        for s in seeds:
+            blocks = ref.compress(img, steps=steps, seed=s)
+            dec = ref.decompress(blocks, img.shape[1], img.shape[0])
+            psnrs.append(port.psnr(img, dec))
+            sses.append(port.block_sse(img, dec))
+        np.save(os.path.join(HERE, name + "_sse.npy"), np.stack(sses).astype(np.float32))
+        manifest["quality"][name] = {"image": expr, "steps": steps, "lcg_seeds": seeds,
+                                     "input_sha256": sha(img), "psnr": psnrs}
+        print(name, psnrs)
+    sel_img = make("tile_mix(11, 128, 128)")
+    sel = np.array([ref.box_selection(px) for px in synth.blocks_of(sel_img)], dtype=np.uint32)
+    np.save(os.path.join(HERE, "box_selection.npy"), sel)
+    manifest["box_selection"] = {"image": "tile_mix(11, 128, 128)", "input_sha256": sha(sel_img)}
+    o7, o6 = ref.tables()
+    np.savez(os.path.join(HERE, "endpoint_tables.npz"), opt7=o7, opt6=o6)
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()
