@@ -5,12 +5,14 @@ the C ABI in ``include/fastc_bc7.h``; this package is the Python mirror of
 FasTC's BPTC interface (:mod:`fastc_gb300.bptc`), the batching/serving
 runtime, and the seeded synthetic workloads.
 """
-from .bptc import (BC7Error, BlockMode, CompressionJob, CompressionJobList, CompressionSettings,
+from .bptc import (WATERMARK_CONTINUE, BC7Error, BlockMode, CompressionJob, CompressionJobList, CompressionSettings,
                    ErrorMetric, Plan, compress, compress_atomic, compress_image_data, compress_jobs,
-                   decompress, get_launch_shape, set_launch_shape)
+                   decompress, get_launch_shape, get_watermark_counter, set_launch_shape,
+                   set_watermark_counter)
 
 __all__ = [
     "BC7Error", "BlockMode", "CompressionJob", "CompressionJobList", "CompressionSettings",
     "ErrorMetric", "Plan", "compress", "compress_atomic", "compress_image_data", "compress_jobs",
-    "decompress", "get_launch_shape", "set_launch_shape",
+    "decompress", "get_launch_shape", "set_launch_shape", "WATERMARK_CONTINUE",
+    "get_watermark_counter", "set_watermark_counter",
 ]

@@ -52,6 +52,15 @@ class Job(C.Structure):
     ]
 
 
+class LogicalBlock(C.Structure):
+    _fields_ = [
+        ("mode", C.c_uint32), ("shape", C.c_uint32), ("subsets", C.c_uint32),
+        ("rotation", C.c_uint32), ("index_mode", C.c_uint32), ("depth", C.c_uint8 * 4),
+        ("endpoints", ((C.c_uint8 * 4) * 2) * 3), ("indices", C.c_uint8 * 16),
+        ("alpha_indices", C.c_uint8 * 16),
+    ]
+
+
 # Every function include/fastc_bc7.h declares, with its ctypes signature.
 SIGNATURES = {
     "fastc_bc7_settings_default": (None, [C.POINTER(Settings)]),
@@ -64,6 +73,7 @@ SIGNATURES = {
     "fastc_bc7_compress_image": (C.c_int, [u8p, C.c_uint32, C.c_uint32, u8p, C.c_size_t,
                                            C.POINTER(Settings)]),
     "fastc_bc7_decompress": (C.c_int, [u8p, u8p, C.c_uint32, C.c_uint32, C.c_int]),
+    "fastc_bc7_decode_logical": (C.c_int, [u8p, C.c_size_t, C.POINTER(LogicalBlock)]),
     "fastc_bc7_compress_device": (C.c_int, [C.POINTER(Job), C.c_uint32, C.POINTER(Settings), C.c_int,
                                             C.c_void_p]),
     "fastc_bc7_decompress_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int,
@@ -74,6 +84,8 @@ SIGNATURES = {
     "fastc_bc7_plan_flags": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
     "fastc_bc7_plan_blocks": (C.c_uint64, [C.c_void_p]),
     "fastc_bc7_plan_destroy": (C.c_int, [C.c_void_p]),
+    "fastc_bc7_set_watermark_counter": (None, [C.c_uint32]),
+    "fastc_bc7_get_watermark_counter": (C.c_uint32, []),
     "fastc_bc7_set_launch_shape": (C.c_int, [C.c_int, C.c_int]),
     "fastc_bc7_get_launch_shape": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
 }

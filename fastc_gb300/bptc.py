@@ -22,6 +22,8 @@ from . import _lib
 from ._lib import BC7Error, Job, Settings, check, load
 
 BLOCK_BYTES = 16
+#: watermark_start value continuing FasTC's process-wide watermark counter
+WATERMARK_CONTINUE = 0xFFFFFFFF
 
 
 class ErrorMetric(enum.IntEnum):
@@ -296,6 +298,14 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def set_watermark_counter(next_entry: int) -> None:
+    load().fastc_bc7_set_watermark_counter(next_entry)
+
+
+def get_watermark_counter() -> int:
+    return int(load().fastc_bc7_get_watermark_counter())
 
 
 def set_launch_shape(warps_per_cta: int = 0, ctas_per_sm: int = 0):

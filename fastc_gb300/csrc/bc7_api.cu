@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "bc7_format.cuh"
 #include "bc7_kernels.cuh"
 #include "fastc_bc7.h"
 
@@ -26,6 +27,7 @@ namespace {
 thread_local std::string t_last_error;
 std::mutex g_mu;
 int g_warps = 4;
+uint32_t g_wm_next = 0;  // FASTC_BC7_WATERMARK_CONTINUE counter (guarded by g_mu)
 int g_ctas_per_sm = 0;  // 0: as many as fit
 
 fastc_bc7_status fail_cuda(cudaError_t e) {
@@ -97,6 +99,7 @@ EncodeScratch carve_scratch(void *base, uint64_t total) {
   EncodeScratch s;
   s.counter = reinterpret_cast<unsigned long long *>(p);
   s.status = reinterpret_cast<uint32_t *>(p + 8);
+  s.singles = reinterpret_cast<uint32_t *>(p + 12);
   s.chunk_prefix = reinterpret_cast<uint32_t *>(p + 256);
   s.rank_local = reinterpret_cast<uint16_t *>(p + 256 + ((nchunks * 4 + 255) & ~255ull));
   return s;
@@ -180,6 +183,7 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
   std::vector<size_t> in_off(n), out_off(n), in_bytes(n);
   size_t in_total = 0, out_total = 0;
   uint64_t total = 0;
+  bool any_continue = false;
   for (uint32_t i = 0; i < n; i++) {
     const fastc_bc7_settings &st = settings_for(s, per_job, i, dflt);
     fastc_bc7_status why;
@@ -188,6 +192,11 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
     if (!jobs[i].in || !jobs[i].out || !job_range(jobs[i], &first, &count))
       return FASTC_BC7_ERR_INVALID_ARGUMENT;
     dj[i] = make_job(jobs[i], st, first, count, total);
+    if (st.watermark_start == FASTC_BC7_WATERMARK_CONTINUE) {
+      dj[i].wm_start = g_wm_next;
+      dj[i].flags |= fastc::kJobWmGlobal;
+      any_continue = true;
+    }
     const uint32_t bw = jobs[i].width / 4;
     const uint32_t r0 = count ? first / bw : 0, r1 = count ? (first + count - 1) / bw : 0;
     in_bytes[i] = count ? (size_t)(r1 - r0 + 1) * 4 * jobs[i].width * 4 : 0;
@@ -215,7 +224,7 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
     CK(cudaMemcpyAsync(din + in_off[i], src, in_bytes[i], cudaMemcpyHostToDevice, cs));
     dj[i].in = din + in_off[i];
     dj[i].out = dout + out_off[i];
-    dj[i].flags = fastc::kJobIn16 | fastc::kJobOut16;
+    dj[i].flags |= fastc::kJobIn16 | fastc::kJobOut16;
   }
   CK(cudaMemcpyAsync(g_host.jobs.p, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs));
   const EncodeScratch sc = carve_scratch(g_host.scratch.p, total);
@@ -227,7 +236,11 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
     CK(cudaMemcpyAsync(jobs[i].out + (size_t)dj[i].first * 16, dout + out_off[i],
                        (size_t)dj[i].nblocks * 16, cudaMemcpyDeviceToHost, cs));
   }
+  uint32_t singles = 0;
+  if (any_continue)
+    CK(cudaMemcpyAsync(&singles, sc.singles, sizeof(singles), cudaMemcpyDeviceToHost, cs));
   CK(cudaStreamSynchronize(cs));
+  if (any_continue) g_wm_next = (uint32_t)((g_wm_next + (uint64_t)singles) % 9u);
   return FASTC_BC7_OK;
 }
 
@@ -322,6 +335,72 @@ fastc_bc7_status fastc_bc7_decompress(const uint8_t *blocks, uint8_t *rgba, uint
   return FASTC_BC7_OK;
 }
 
+fastc_bc7_status fastc_bc7_decode_logical(const uint8_t *blocks, size_t n,
+                                          fastc_bc7_logical_block *out) {
+  if ((!blocks || !out) && n) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  static const uint32_t part2[64] = {FASTC_PART2_WORDS};
+  static const uint32_t part3[64] = {FASTC_PART3_WORDS};
+  static const uint8_t anc2[64] = {FASTC_ANCHOR2_BYTES};
+  static const uint8_t anc3[64] = {FASTC_ANCHOR3_BYTES};
+  for (size_t b = 0; b < n; b++) {
+    const uint8_t *blk = blocks + 16 * b;
+    fastc_bc7_logical_block &o = out[b];
+    std::memset(&o, 0, sizeof(o));
+    int pos = 0;
+    auto bits = [&](int k) {
+      uint32_t v = 0;
+      for (int i = 0; i < k; i++, pos++) v |= (uint32_t)((blk[pos >> 3] >> (pos & 7)) & 1) << i;
+      return v;
+    };
+    int mode = 0;
+    while (mode < 8 && !bits(1)) mode++;
+    o.mode = (uint32_t)mode;
+    if (mode >= 8) continue;
+    const fastc::ModeAttr a = fastc::mode_attr(mode);
+    o.subsets = (uint32_t)a.subsets;
+    if (a.subsets > 1) o.shape = bits(a.part_bits);
+    if (a.has_rotation) o.rotation = bits(2);
+    if (a.has_idx_mode) o.index_mode = bits(1);
+    for (int ch = 0; ch < 4; ch++) {
+      const int nb = ch == 3 ? a.alpha_bits : a.color_bits;
+      for (int s = 0; s < a.subsets; s++)
+        for (int e = 0; e < 2; e++) o.endpoints[s][e][ch] = nb ? (uint8_t)bits(nb) : 0xFF;
+      o.depth[ch] = (uint8_t)nb;
+    }
+    if (a.pbit != fastc::kPBitNone) {
+      for (int s = 0; s < a.subsets; s++) {
+        const uint32_t shared = a.pbit == fastc::kPBitShared ? bits(1) : 0;
+        for (int e = 0; e < 2; e++) {
+          const uint32_t pb = a.pbit == fastc::kPBitShared ? shared : bits(1);
+          for (int ch = 0; ch < 4; ch++)
+            if (o.depth[ch]) o.endpoints[s][e][ch] = (uint8_t)((o.endpoints[s][e][ch] << 1) | pb);
+        }
+      }
+      for (int ch = 0; ch < 4; ch++)
+        if (o.depth[ch]) o.depth[ch]++;
+    }
+    const uint32_t part = a.subsets == 2 ? part2[o.shape] : (a.subsets == 3 ? part3[o.shape] : 0u);
+    auto anchor = [&](int s) {
+      if (s == 0) return 0;
+      if (a.subsets == 2) return (int)anc2[o.shape];
+      return s == 1 ? (int)(anc3[o.shape] & 15) : (int)(anc3[o.shape] >> 4);
+    };
+    uint8_t first[16], second[16];
+    for (int i = 0; i < 16; i++) {
+      const int s = (int)((part >> (2 * i)) & 3);
+      first[i] = (uint8_t)bits(anchor(s) == i ? a.idx_bits - 1 : a.idx_bits);
+    }
+    for (int i = 0; i < 16; i++)
+      second[i] = a.alpha_idx_bits ? (uint8_t)bits(i == 0 ? a.alpha_idx_bits - 1 : a.alpha_idx_bits)
+                                   : first[i];
+    for (int i = 0; i < 16; i++) {
+      o.indices[i] = o.index_mode ? second[i] : first[i];
+      o.alpha_indices[i] = o.index_mode ? first[i] : second[i];
+    }
+  }
+  return FASTC_BC7_OK;
+}
+
 fastc_bc7_status fastc_bc7_compress_device(const fastc_bc7_job *jobs, uint32_t n,
                                            const fastc_bc7_settings *settings,
                                            int per_job_settings, void *stream) {
@@ -335,6 +414,7 @@ fastc_bc7_status fastc_bc7_compress_device(const fastc_bc7_job *jobs, uint32_t n
     const fastc_bc7_settings &st = settings_for(settings, per_job_settings, i, dflt);
     fastc_bc7_status why;
     if (!settings_ok(st, &why)) return why;
+    if (st.watermark_start == FASTC_BC7_WATERMARK_CONTINUE) return FASTC_BC7_ERR_INVALID_ARGUMENT;
     uint32_t first, count;
     if (!jobs[i].in || !jobs[i].out || !job_range(jobs[i], &first, &count) ||
         (reinterpret_cast<uintptr_t>(jobs[i].in) & 3) || (reinterpret_cast<uintptr_t>(jobs[i].out) & 3))
@@ -393,6 +473,7 @@ fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
     const fastc_bc7_settings &st = settings_for(settings, per_job_settings, i, dflt);
     fastc_bc7_status why;
     if (!settings_ok(st, &why)) return why;
+    if (st.watermark_start == FASTC_BC7_WATERMARK_CONTINUE) return FASTC_BC7_ERR_INVALID_ARGUMENT;
     uint32_t first, count;
     if (!jobs[i].in || !jobs[i].out || !job_range(jobs[i], &first, &count) ||
         (reinterpret_cast<uintptr_t>(jobs[i].in) & 3) || (reinterpret_cast<uintptr_t>(jobs[i].out) & 3))
@@ -458,6 +539,16 @@ fastc_bc7_status fastc_bc7_plan_destroy(fastc_bc7_plan p) {
   if (p->d_scratch) cudaFree(p->d_scratch);
   delete p;
   return FASTC_BC7_OK;
+}
+
+void fastc_bc7_set_watermark_counter(uint32_t next_entry) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_wm_next = next_entry % 9u;
+}
+
+uint32_t fastc_bc7_get_watermark_counter(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g_wm_next;
 }
 
 fastc_bc7_status fastc_bc7_set_launch_shape(int warps_per_cta, int ctas_per_sm) {

@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(kRankChunk) classify_kernel(const JobDev *jobs
 // Exclusive scan of the chunk counts, in place; also resets the counter.
 __global__ void __launch_bounds__(1024) scan_kernel(uint32_t *chunk, uint32_t nchunks,
                                                      unsigned long long *counter,
-                                                     uint32_t *status) {
+                                                     uint32_t *status, uint32_t *singles) {
   __shared__ uint32_t s_warp[32];
   __shared__ uint32_t s_carry;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -250,6 +250,7 @@ __global__ void __launch_bounds__(1024) scan_kernel(uint32_t *chunk, uint32_t nc
     if (threadIdx.x == 1023) s_carry = carry + s_warp[wid] + incl;
     __syncthreads();
   }
+  if (threadIdx.x == 0) *singles = s_carry;
 }
 
 // ---------------------------------------------------------------------------
@@ -575,7 +576,9 @@ __global__ void __launch_bounds__(kWarps * 32) encode_kernel(
       if (lane == 0) {
         const uint64_t gb = jb.begin;
         const uint32_t rg = chunk_prefix[g / kRankChunk] + rank_local[g];
-        const uint32_t rb = chunk_prefix[gb / kRankChunk] + rank_local[gb];
+        const uint32_t rb = (jb.flags & kJobWmGlobal)
+                                ? 0u
+                                : chunk_prefix[gb / kRankChunk] + rank_local[gb];
         single_color_block(px[0], jb.wm_start + (rg - rb), out);
         store_block(jb, lin, out);
       }
@@ -678,7 +681,8 @@ int launch_encode(const JobDev *jobs_dev, int njobs, uint64_t total, const Encod
   const uint32_t nchunks = (uint32_t)((total + kRankChunk - 1) / kRankChunk);
   classify_kernel<<<nchunks, kRankChunk, 0, st>>>(jobs_dev, njobs, total, sc.rank_local,
                                                   sc.chunk_prefix);
-  scan_kernel<<<1, 1024, 0, st>>>(sc.chunk_prefix, nchunks, sc.counter, sc.status);
+  scan_kernel<<<1, 1024, 0, st>>>(sc.chunk_prefix, nchunks, sc.counter, sc.status,
+                                  sc.singles);
   const int ctas = shape.ctas > 0 ? shape.ctas : 1;
   switch (shape.warps_per_cta) {
     case 1:

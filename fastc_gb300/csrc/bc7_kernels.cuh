@@ -24,6 +24,9 @@ struct JobDev {
 
 constexpr uint32_t kJobIn16 = 1u;   // 16-byte texel-row loads are legal
 constexpr uint32_t kJobOut16 = 2u;  // 16-byte block stores are legal
+// Watermark index = wm_start + the block's single-colour rank over every job
+// of the launch (FasTC's process-global counter), instead of within its job.
+constexpr uint32_t kJobWmGlobal = 4u;
 
 constexpr int kRankChunk = 1024;    // blocks per watermark-rank chunk
 
@@ -33,6 +36,7 @@ struct EncodeScratch {
   uint32_t *chunk_prefix;  // [nchunks] exclusive prefix of single-colour counts
   unsigned long long *counter;  // work counter of the persistent kernel
   uint32_t *status;        // device-side status bits
+  uint32_t *singles;       // single-colour blocks in the launch (written by the scan)
 };
 
 struct LaunchShape {

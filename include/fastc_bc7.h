@@ -61,6 +61,12 @@ typedef enum {
   FASTC_BC7_ERR_INTERNAL = 10
 } fastc_bc7_status;
 
+/* watermark_start value that continues the process-wide single-colour
+ * watermark counter, like FasTC's global gWMVal (Compressor.cpp:140): every
+ * single-colour block of the call, in job and raster order, takes the next
+ * entry. Host-memory entry points only. */
+#define FASTC_BC7_WATERMARK_CONTINUE 0xFFFFFFFFu
+
 /* EBlockMode (BPTCCompressor.h:56-65): bit m enables BC7 mode m. */
 #define FASTC_BC7_ALL_MODES 0xFFu
 
@@ -127,6 +133,26 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_compress_image(const uint8_t *rgba, uin
 FASTC_BC7_API fastc_bc7_status fastc_bc7_decompress(const uint8_t *blocks, uint8_t *rgba, uint32_t width,
                                       uint32_t height, int spec_semantics);
 
+/* BPTCC::LogicalBlock (BPTCCompressor.h:203-209): the stored fields of one
+ * block. Endpoints are at their stored precision (p-bit appended as the
+ * lowest bit), depth[] gives that precision per channel (0: channel absent,
+ * reads as 255), indices are per texel after the index-mode swap. */
+typedef struct {
+  uint32_t mode;  /* 0..7, 8 = reserved block */
+  uint32_t shape;
+  uint32_t subsets;
+  uint32_t rotation;
+  uint32_t index_mode;
+  uint8_t depth[4];
+  uint8_t endpoints[3][2][4];
+  uint8_t indices[16];
+  uint8_t alpha_indices[16];
+} fastc_bc7_logical_block;
+
+/* BPTCC::DecompressLogical: parse n blocks on the host. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_decode_logical(const uint8_t *blocks, size_t n,
+                                          fastc_bc7_logical_block *out);
+
 /* --- Device-memory entry points: asynchronous on `stream`. ---
  * in/out of every job are device pointers to whole textures. Scratch is
  * taken from the stream-ordered allocator on `stream`. */
@@ -136,6 +162,11 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_compress_device(const fastc_bc7_job *jo
 FASTC_BC7_API fastc_bc7_status fastc_bc7_decompress_device(const uint8_t *blocks, uint8_t *rgba,
                                              uint32_t width, uint32_t height,
                                              int spec_semantics, void *stream);
+
+/* The process-wide watermark counter used by FASTC_BC7_WATERMARK_CONTINUE
+ * (the entry the next single-colour block takes; FasTC starts at 0). */
+FASTC_BC7_API void fastc_bc7_set_watermark_counter(uint32_t next_entry);
+FASTC_BC7_API uint32_t fastc_bc7_get_watermark_counter(void);
 
 /* --- Plans: a fixed set of device jobs captured once in a CUDA graph. ---
  * The job table, scratch and the graph are built at creation; each launch

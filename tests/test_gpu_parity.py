@@ -137,19 +137,28 @@ def test_device_api_and_plan_match_host_api(gpu):
     plan.close()
 
 
-def test_sub_jobs_tile_the_image(gpu):
-    """FasTC's ThreadGroup splits (Core/src/ThreadGroup.cpp:133-192) produce
-    the same bytes as one whole-image job."""
-    from fastc_gb300 import CompressionJob, CompressionSettings, compress
+def test_sub_jobs_tile_the_image(gpu, port):
+    """FasTC's ThreadGroup splits (Core/src/ThreadGroup.cpp:133-192), run one
+    after another with the watermark counter continuing across calls like
+    FasTC's global gWMVal, give the same bytes as one whole-image job."""
+    from fastc_gb300 import WATERMARK_CONTINUE, CompressionJob, CompressionSettings, compress
+    from fastc_gb300._lib import load
 
+    lib = load()
     img = make_image("tile_mix(80, 64, 48)")
-    whole = gpu_compress(img, 4, seed=2)
-    out = np.zeros_like(whole)
     w, h = 64, 48
+    s = CompressionSettings(num_simulated_annealing_steps=4, seed=2, watermark_start=WATERMARK_CONTINUE)
+    lib.fastc_bc7_set_watermark_counter(0)
+    whole = np.zeros(w * h, np.uint8)
+    compress(CompressionJob(img, whole, w, h), s)
+    nsingle = sum(int((b == b[0]).all()) for b in __import__("fastc_gb300").synth.blocks_of(img))
+    assert lib.fastc_bc7_get_watermark_counter() == nsingle % 9
+    assert np.array_equal(whole, port.compress(img, steps=4, seed=2))
+    lib.fastc_bc7_set_watermark_counter(0)
+    out = np.zeros_like(whole)
     nblocks = (w // 4) * (h // 4)
     per = nblocks // 5 + 1
     done = 0
-    s = CompressionSettings(num_simulated_annealing_steps=4, seed=2)
     while done < nblocks:
         e = min(done + per, nblocks)
         compress(CompressionJob(img, out, w, h, (done % 16) * 4, (done // 16) * 4, (e % 16) * 4, (e // 16) * 4), s)
