@@ -86,6 +86,8 @@ SIGNATURES = {
     "fastc_bc7_plan_destroy": (C.c_int, [C.c_void_p]),
     "fastc_bc7_set_watermark_counter": (None, [C.c_uint32]),
     "fastc_bc7_get_watermark_counter": (C.c_uint32, []),
+    "fastc_bc7_set_engine": (C.c_int, [C.c_int]),
+    "fastc_bc7_get_engine": (C.c_int, []),
     "fastc_bc7_set_launch_shape": (C.c_int, [C.c_int, C.c_int]),
     "fastc_bc7_get_launch_shape": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
 }

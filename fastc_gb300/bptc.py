@@ -300,6 +300,19 @@ class Plan:
             pass
 
 
+ENGINE_PIPELINE = 0
+ENGINE_WARP_PER_BLOCK = 1
+
+
+def set_engine(engine: int) -> None:
+    """Select the encoder organisation for later calls and plans."""
+    check(load().fastc_bc7_set_engine(engine), "fastc_bc7_set_engine")
+
+
+def get_engine() -> int:
+    return int(load().fastc_bc7_get_engine())
+
+
 def set_watermark_counter(next_entry: int) -> None:
     load().fastc_bc7_set_watermark_counter(next_entry)
 

@@ -16,6 +16,7 @@
 
 #include "bc7_format.cuh"
 #include "bc7_kernels.cuh"
+#include "bc7_pipeline.cuh"
 #include "fastc_bc7.h"
 
 using fastc::EncodeScratch;
@@ -29,6 +30,7 @@ std::mutex g_mu;
 int g_warps = 4;
 uint32_t g_wm_next = 0;  // FASTC_BC7_WATERMARK_CONTINUE counter (guarded by g_mu)
 int g_ctas_per_sm = 0;  // 0: as many as fit
+int g_engine = FASTC_BC7_ENGINE_PIPELINE;
 
 fastc_bc7_status fail_cuda(cudaError_t e) {
   t_last_error = cudaGetErrorString(e);
@@ -88,9 +90,15 @@ LaunchShape pick_shape(uint64_t total) {
   return LaunchShape{warps, (int)ctas};
 }
 
-size_t scratch_bytes(uint64_t total) {
+size_t rank_scratch_bytes(uint64_t total) {
   const uint64_t nchunks = (total + fastc::kRankChunk - 1) / fastc::kRankChunk;
-  return 256 + ((nchunks * 4 + 255) & ~255ull) + total * 2 + 256;
+  return (256 + ((nchunks * 4 + 255) & ~255ull) + total * 2 + 256 + 255) & ~255ull;
+}
+
+size_t scratch_bytes(uint64_t total, int engine) {
+  size_t b = rank_scratch_bytes(total);
+  if (engine == FASTC_BC7_ENGINE_PIPELINE) b += fastc::pipeline_scratch_bytes(total);
+  return b;
 }
 
 EncodeScratch carve_scratch(void *base, uint64_t total) {
@@ -131,6 +139,19 @@ uint32_t align_flags(const void *in, const void *out) {
   if ((reinterpret_cast<uintptr_t>(in) & 15) == 0) f |= fastc::kJobIn16;
   if ((reinterpret_cast<uintptr_t>(out) & 15) == 0) f |= fastc::kJobOut16;
   return f;
+}
+
+// Encode `total` blocks of the device job table with the selected engine,
+// carving the rank and pipeline scratch out of `scratch`.
+int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
+                  LaunchShape shape, cudaStream_t st) {
+  const EncodeScratch rank = carve_scratch(scratch, total);
+  if (engine == FASTC_BC7_ENGINE_PIPELINE) {
+    void *pipe = static_cast<uint8_t *>(scratch) + rank_scratch_bytes(total);
+    return fastc::launch_pipeline(jobs, njobs, total, rank, pipe,
+                                  fastc::device_sm_count(current_device()), st);
+  }
+  return fastc::launch_encode(jobs, njobs, total, rank, shape, st);
 }
 
 // Grow-only device buffer.
@@ -214,7 +235,7 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
   CK(g_host.in.ensure(in_total));
   CK(g_host.out.ensure(out_total));
   CK(g_host.jobs.ensure(n * sizeof(JobDev)));
-  CK(g_host.scratch.ensure(scratch_bytes(total)));
+  CK(g_host.scratch.ensure(scratch_bytes(total, g_engine)));
   cudaStream_t cs = g_host.stream;
   uint8_t *din = static_cast<uint8_t *>(g_host.in.p);
   uint8_t *dout = static_cast<uint8_t *>(g_host.out.p);
@@ -228,8 +249,8 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
   }
   CK(cudaMemcpyAsync(g_host.jobs.p, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs));
   const EncodeScratch sc = carve_scratch(g_host.scratch.p, total);
-  const int le = fastc::launch_encode(static_cast<const JobDev *>(g_host.jobs.p), (int)n, total,
-                                      sc, pick_shape(total), cs);
+  const int le = launch_engine(static_cast<const JobDev *>(g_host.jobs.p), (int)n, total,
+                               g_host.scratch.p, g_engine, pick_shape(total), cs);
   if (le) return fail_cuda((cudaError_t)le);
   for (uint32_t i = 0; i < n; i++) {
     if (!dj[i].nblocks) continue;
@@ -253,6 +274,7 @@ struct fastc_bc7_plan_s {
   uint64_t total = 0;
   int njobs = 0;
   EncodeScratch sc{};
+  int engine = FASTC_BC7_ENGINE_PIPELINE;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -431,20 +453,20 @@ fastc_bc7_status fastc_bc7_compress_device(const fastc_bc7_job *jobs, uint32_t n
     fastc::upload_tables(dev);
   }
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  LaunchShape shape;
+  int engine;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    shape = pick_shape(total);
+    engine = g_engine;
+  }
   void *buf = nullptr;
   const size_t jb = (n * sizeof(JobDev) + 255) & ~(size_t)255;
-  CK(cudaMallocAsync(&buf, jb + scratch_bytes(total), cs));
+  CK(cudaMallocAsync(&buf, jb + scratch_bytes(total, engine), cs));
   cudaError_t e = cudaMemcpyAsync(buf, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs);
-  if (e == cudaSuccess) {
-    const EncodeScratch sc = carve_scratch(static_cast<uint8_t *>(buf) + jb, total);
-    LaunchShape shape;
-    {
-      std::lock_guard<std::mutex> lk(g_mu);
-      shape = pick_shape(total);
-    }
-    e = (cudaError_t)fastc::launch_encode(static_cast<const JobDev *>(buf), (int)n, total, sc, shape,
-                                          cs);
-  }
+  if (e == cudaSuccess)
+    e = (cudaError_t)launch_engine(static_cast<const JobDev *>(buf), (int)n, total,
+                                   static_cast<uint8_t *>(buf) + jb, engine, shape, cs);
   cudaError_t ef = cudaFreeAsync(buf, cs);
   if (e != cudaSuccess) return fail_cuda(e);
   if (ef != cudaSuccess) return fail_cuda(ef);
@@ -492,7 +514,8 @@ fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
   p->njobs = (int)n;
   cudaStream_t cs = nullptr;
   cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p->d_jobs), n * sizeof(JobDev));
-  if (e == cudaSuccess) e = cudaMalloc(&p->d_scratch, scratch_bytes(total > 0 ? total : 1));
+  p->engine = g_engine;
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_scratch, scratch_bytes(total > 0 ? total : 1, p->engine));
   if (e == cudaSuccess)
     e = cudaMemcpy(p->d_jobs, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
@@ -500,7 +523,8 @@ fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
     p->sc = carve_scratch(p->d_scratch, total);
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      const int le = fastc::launch_encode(p->d_jobs, (int)n, total, p->sc, pick_shape(total), cs);
+      const int le = launch_engine(p->d_jobs, (int)n, total, p->d_scratch, p->engine,
+                                   pick_shape(total), cs);
       cudaError_t ee = cudaStreamEndCapture(cs, &p->graph);
       e = le ? (cudaError_t)le : ee;
     }
@@ -560,6 +584,19 @@ fastc_bc7_status fastc_bc7_set_launch_shape(int warps_per_cta, int ctas_per_sm) 
   if (warps_per_cta) g_warps = warps_per_cta;
   if (ctas_per_sm) g_ctas_per_sm = ctas_per_sm;
   return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_set_engine(int engine) {
+  if (engine != FASTC_BC7_ENGINE_PIPELINE && engine != FASTC_BC7_ENGINE_WARP_PER_BLOCK)
+    return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_engine = engine;
+  return FASTC_BC7_OK;
+}
+
+int fastc_bc7_get_engine(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g_engine;
 }
 
 fastc_bc7_status fastc_bc7_get_launch_shape(int *warps_per_cta, int *ctas_per_sm) {

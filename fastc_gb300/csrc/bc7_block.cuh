@@ -45,7 +45,7 @@ constexpr int kMaxTasks = 32;
 constexpr uint32_t kStatusTaskOverflow = 2u;
 
 // EstimateTwoClusterError / EstimateThreeClusterError (CP:1626-1655)
-__device__ double estimate_shape(const uint32_t *px, uint32_t part, int nsub, int bits,
+__device__ inline double estimate_shape(const uint32_t *px, uint32_t part, int nsub, int bits,
                                  const float *w) {
   double err = 0.0;
   for (int ci = 0; ci < nsub; ci++) {
@@ -72,7 +72,7 @@ __device__ __forceinline__ void argmin_pair(double &e, int &i, double oe, int oi
 }
 
 // BoxSelection (CP:1670-1750), 64 shapes spread two per lane.
-__device__ Selection box_selection_warp(const uint32_t *px, const uint32_t *part2,
+__device__ inline Selection box_selection_warp(const uint32_t *px, const uint32_t *part2,
                                         const uint32_t *part3, int metric, int lane) {
   Selection r;
   r.nshapes = 1;
@@ -124,7 +124,7 @@ __device__ Selection box_selection_warp(const uint32_t *px, const uint32_t *part
 
 // The cluster fits CompressClusters (CP:1752-1817) runs, in its order.
 // Returns the number of tasks; fills `t` with task `want` if it exists.
-__device__ int enumerate_tasks(const Selection &sel, uint32_t modes, int want, Task &t) {
+__device__ inline int enumerate_tasks(const Selection &sel, uint32_t modes, int want, Task &t) {
   int n = 0;
   const uint32_t nshapes = sel.nshapes < 5 ? sel.nshapes : 5;
   for (int oi = 0; oi < 8; oi++) {
@@ -152,7 +152,7 @@ __device__ int enumerate_tasks(const Selection &sel, uint32_t modes, int want, T
   return n;
 }
 
-__device__ void run_task(const Task &t, const Selection &sel, const uint32_t *px,
+__device__ inline void run_task(const Task &t, const Selection &sel, const uint32_t *px,
                          const uint32_t *part2, const uint32_t *part3, const uint32_t *opt6,
                          const JobDev &jb, uint32_t bx, uint32_t by, uint32_t *status,
                          FitOut &o) {
@@ -194,7 +194,7 @@ struct BitWriter {
 };
 
 // CompressionMode::Pack (CP:1096-1298) from the winning fits.
-__device__ void pack_block(int mode, const Selection &sel, int slot, const FitOut *fits,
+__device__ inline void pack_block(int mode, const Selection &sel, int slot, const FitOut *fits,
                            const uint8_t *anc2, const uint8_t *anc3, const uint32_t *part2,
                            const uint32_t *part3, int rot, int im, uint32_t out[4]) {
   const ModeAttr a = mode_attr(mode);
@@ -277,7 +277,7 @@ __device__ void pack_block(int mode, const Selection &sel, int slot, const FitOu
   out[3] = bw.w[3];
 }
 
-__device__ void single_color_block(uint32_t pixel, uint32_t wm, const uint32_t *opt7,
+__device__ inline void single_color_block(uint32_t pixel, uint32_t wm, const uint32_t *opt7,
                                    const uint32_t *watermark, uint32_t out[4]) {
   BitWriter bw;
   bw.w[0] = bw.w[1] = bw.w[2] = bw.w[3] = 0;

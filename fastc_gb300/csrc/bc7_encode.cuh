@@ -249,7 +249,7 @@ __device__ __forceinline__ uint32_t get_nib(uint64_t v, int t) {
 
 // RGBACluster::QuantizedError<nBuckets> (RE:190-310). pb = -1 means the
 // caller passed no p-bits; otherwise bit0/bit1 are the endpoints' p-bits.
-__device__ float quantized_error(const Cluster &c, const float *p1, const float *p2,
+__device__ inline float quantized_error(const Cluster &c, const float *p1, const float *p2,
                                  int bits, uint32_t qmask, const float *w, int pb,
                                  uint64_t *idx) {
   const int nb = 1 << bits;
@@ -321,7 +321,7 @@ __device__ float quantized_error(const Cluster &c, const float *p1, const float 
 // Principal axis (RE:327-428) and power iteration (MatrixSquare.h:44-105)
 // --------------------------------------------------------------------------
 
-__device__ void power_method(const float m[4][4], float *out) {
+__device__ inline void power_method(const float m[4][4], float *out) {
   float b[4] = {0.5f, 0.5f, 0.5f, 0.5f};
   bool bad = false, fixed = false;
   int iters = 0;
@@ -351,7 +351,7 @@ __device__ void power_method(const float m[4][4], float *out) {
   for (int k = 0; k < 4; k++) out[k] = b[k];
 }
 
-__device__ void principal_axis(const Cluster &c, float *axis) {
+__device__ inline void principal_axis(const Cluster &c, float *axis) {
   // unique points, in order; slots past the unique count stay (-1,-1,-1,-1)
   float upts[16][4];
   int nu = 0;
@@ -489,7 +489,7 @@ __device__ __forceinline__ void clamp_endpoints(float *p1, float *p2) {  // RE:4
 }
 
 // ClampEndpointsToGrid (CP:212-250)
-__device__ void clamp_to_grid(const ModeCtx &m, float *p1, float *p2, uint32_t &best_pbit) {
+__device__ inline void clamp_to_grid(const ModeCtx &m, float *p1, float *p2, uint32_t &best_pbit) {
   const int nc = num_pbit_combos(m.a);
   const uint32_t qm = qmask_of(m.a);
   clamp_endpoints(p1, p2);
@@ -526,7 +526,7 @@ __device__ void clamp_to_grid(const ModeCtx &m, float *p1, float *p2, uint32_t &
 }
 
 // CompressSingleColor (CP:252-353)
-__device__ float single_color(const ModeCtx &m, const float *p, float *p1, float *p2,
+__device__ inline float single_color(const ModeCtx &m, const float *p, float *p1, float *p2,
                               uint32_t &best_pbit) {
   const uint32_t pixel = to_pixel(p, 0xFFFFFFFFu, -1);
   float best_err = FLT_MAX;
@@ -591,7 +591,7 @@ __device__ float single_color(const ModeCtx &m, const float *p, float *p1, float
 
 // PickBestNeighboringEndpoints (CP:426-498); the visited list only ever
 // holds the best state found so far.
-__device__ void pick_neighbor(ModeCtx &m, const float *p1, const float *p2, int cur_pbit,
+__device__ inline void pick_neighbor(ModeCtx &m, const float *p1, const float *p2, int cur_pbit,
                               float *np1, float *np2, int &npbit, const float *vis1,
                               const float *vis2, int vis_pbit) {
   float step[4];
@@ -629,25 +629,17 @@ __device__ void pick_neighbor(ModeCtx &m, const float *p1, const float *p2, int 
   }
 }
 
-// OptimizeEndpointsForCluster (CP:538-630)
-__device__ float optimize_endpoints(ModeCtx &m, const Cluster &c, float *p1, float *p2,
-                                    uint64_t &best_idx, uint32_t &best_pbit) {
+// OptimizeEndpointsForCluster (CP:538-630), from the point after its first
+// QuantizedError and the snap of p1/p2 onto the grid: p1/p2 hold grid
+// values, cur_err/best_idx/best_pbit the starting error, indices and p-bits.
+__device__ inline float anneal_from(ModeCtx &m, const Cluster &c, float *p1, float *p2,
+                             float cur_err, uint64_t &best_idx, uint32_t &best_pbit) {
   const int ib = bits_index(m, -1);
   const uint32_t qm = qmask_of(m.a);
   float w[4];
   metric_of(m, w);
-  float cur_err =
-      quantized_error(c, p1, p2, ib, qm, w, pbit_combo(m.a, (int)best_pbit), &best_idx);
   int cur_pbit = (int)best_pbit;
   float best_err = cur_err;
-  {
-    const int pc = pbit_combo(m.a, (int)best_pbit);
-    const bool hp = m.a.pbit != kPBitNone;
-    const uint32_t q1 = to_pixel(p1, qm, hp ? pb_first(pc) : -1);
-    const uint32_t q2 = to_pixel(p2, qm, hp ? pb_second(pc) : -1);
-    unpack4(q1, p1);
-    unpack4(q2, p2);
-  }
   float bp1[4], bp2[4], vis1[4], vis2[4];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
@@ -693,16 +685,32 @@ __device__ float optimize_endpoints(ModeCtx &m, const Cluster &c, float *p1, flo
   return best_err;
 }
 
-// CompressionMode::CompressCluster, colour version (CP:921-1094)
-__device__ double fit_rgb(ModeCtx &m, const Cluster &c, float *p1, float *p2,
-                          uint64_t &idx, uint32_t &pbit) {
+// A cluster fit up to the point where FasTC starts annealing.
+struct FitSetup {
+  double err;       // final error when !anneal (CompressCluster's return value)
+  float errf;       // starting error of the annealing
+  float p1[4], p2[4];
+  uint64_t idx;     // 4 bits per texel
+  uint32_t pbit;
+  bool anneal;      // the annealing loop has work (steps > 0, error > 0)
+};
+
+// CompressionMode::CompressCluster, colour version (CP:921-1094), up to the
+// annealing (the first QuantizedError and the grid snap of CP:546-566).
+__device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st) {
+  float *p1 = st.p1, *p2 = st.p2;
+  uint64_t &idx = st.idx;
+  uint32_t &pbit = st.pbit;
+  st.anneal = false;
+  st.errf = 0.0f;
   if (all_same_point(c)) {
     float p0[4];
     cl_point(c, __ffs(c.mask) - 1, p0);
     const double e = single_color(m, p0, p1, p2, pbit);
     for (int i = 0; i < 16; i++)
       if ((c.mask >> i) & 1) set_nib(idx, i, 1);
-    return (double)c.n * e;
+    st.err = (double)c.n * e;
+    return;
   }
   const int ib = bits_index(m, -1);
   const int nb = 1 << ib;
@@ -791,7 +799,8 @@ __device__ double fit_rgb(ModeCtx &m, const Cluster &c, float *p1, float *p2,
     const double e = single_color(m, pts[last], p1, p2, pbit);
     for (int i = 0; i < 16; i++)
       if ((c.mask >> i) & 1) set_nib(idx, i, 1);
-    return (double)c.n * e;
+    st.err = (double)c.n * e;
+    return;
   }
   float asq = 0.0f, bsq = 0.0f, ab = 0.0f;
   float ax[4] = {0.0f, 0.0f, 0.0f, 0.0f}, bx[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -815,13 +824,45 @@ __device__ double fit_rgb(ModeCtx &m, const Cluster &c, float *p1, float *p2,
     p2[k] = __fmul_rn(__fsub_rn(__fmul_rn(bx[k], asq), __fmul_rn(ax[k], ab)), f);
   }
   clamp_to_grid(m, p1, p2, pbit);
-  return (double)optimize_endpoints(m, c, p1, p2, idx, pbit);
+  const uint32_t qm = qmask_of(m.a);
+  float w[4];
+  metric_of(m, w);
+  const int pc = pbit_combo(m.a, (int)pbit);
+  st.errf = quantized_error(c, p1, p2, bits_index(m, -1), qm, w, pc, &idx);
+  const bool hp = m.a.pbit != kPBitNone;
+  const uint32_t q1 = to_pixel(p1, qm, hp ? pb_first(pc) : -1);
+  const uint32_t q2 = to_pixel(p2, qm, hp ? pb_second(pc) : -1);
+  unpack4(q1, p1);
+  unpack4(q2, p2);
+  st.err = (double)st.errf;
+  st.anneal = m.steps > 0 && st.errf > 0.0f;
 }
+
+__device__ inline double fit_rgb(ModeCtx &m, const Cluster &c, float *p1, float *p2,
+                          uint64_t &idx, uint32_t &pbit) {
+  FitSetup st;
+  st.idx = idx;
+  st.pbit = pbit;
+  fit_rgb_setup(m, c, st);
+  if (st.anneal) st.err = (double)anneal_from(m, c, st.p1, st.p2, st.errf, st.idx, st.pbit);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    p1[k] = st.p1[k];
+    p2[k] = st.p2[k];
+  }
+  idx = st.idx;
+  pbit = st.pbit;
+  return st.err;
+}
+
+__device__ inline void alpha_fit(const ModeCtx &m, const float *avals, float amin, float amax,
+                          const uint32_t *opt6, float &a1_out, float &a2_out, uint64_t &aidx,
+                          double &aerr_out);
 
 // CompressionMode::CompressCluster, separate-alpha version (CP:632-919).
 // `c` is the whole block; the colour fit runs on a rotated copy whose
 // statistics and error pixels stay those of the unrotated block.
-__device__ double fit_alpha(ModeCtx &m, const Cluster &c, const uint32_t *opt6,
+__device__ inline double fit_alpha(ModeCtx &m, const Cluster &c, const uint32_t *opt6,
                             float *p1, float *p2, uint64_t &idx, uint64_t &aidx) {
   Cluster rgb = c;
   rgb.rot = rotation_of(m);
@@ -839,6 +880,48 @@ __device__ double fit_alpha(ModeCtx &m, const Cluster &c, const uint32_t *opt6,
   uint32_t dummy = 0;
   float rp1[4], rp2[4];
   const double rgb_err = fit_rgb(m, rgb, rp1, rp2, idx, dummy);
+  double aerr;
+  float a1, a2;
+  alpha_fit(m, avals, amin, amax, opt6, a1, a2, aidx, aerr);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    p1[k] = rp1[k];
+    p2[k] = rp2[k];
+  }
+  p1[3] = a1;
+  p2[3] = a2;
+  return rgb_err + aerr;
+}
+
+// The separate-alpha fit up to the colour fit's annealing: the colour part
+// in `st` (rotated cluster, CP:664-701), the alpha part complete.
+__device__ inline void fit_alpha_setup(ModeCtx &m, const Cluster &c, const uint32_t *opt6,
+                                FitSetup &st, float &a1, float &a2, uint64_t &aidx,
+                                double &aerr) {
+  Cluster rgb = c;
+  rgb.rot = rotation_of(m);
+  rgb.a255 = true;
+  const int r = rgb.rot;
+  float avals[16];
+  float amin = FLT_MAX, amax = -FLT_MAX;
+  for (int i = 0; i < 16; i++) {
+    const uint32_t ch = r ? r - 1 : 3;
+    avals[i] = (float)((c.px[i] >> (8 * ch)) & 0xFF);
+    amin = min_std(avals[i], amin);
+    amax = max_std(avals[i], amax);
+  }
+  st.idx = 0;
+  st.pbit = 0;
+  fit_rgb_setup(m, rgb, st);
+  alpha_fit(m, avals, amin, amax, opt6, a1, a2, aidx, aerr);
+}
+
+// The alpha half of CompressCluster's separate-alpha version (CP:703-911):
+// 1-D k-means on the rotated channel, least squares, quantisation and the
+// per-texel bucket search. Independent of the colour fit's annealing.
+__device__ inline void alpha_fit(const ModeCtx &m, const float *avals, float amin, float amax,
+                          const uint32_t *opt6, float &a1_out, float &a2_out, uint64_t &aidx,
+                          double &aerr_out) {
 
   float a1 = amin, a2 = amax;
   double aerr;
@@ -956,14 +1039,9 @@ __device__ double fit_alpha(ModeCtx &m, const Cluster &c, const uint32_t *opt6,
       set_nib(aidx, i, bb);
     }
   }
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    p1[k] = rp1[k];
-    p2[k] = rp2[k];
-  }
-  p1[3] = a1;
-  p2[3] = a2;
-  return rgb_err + aerr;
+  a1_out = a1;
+  a2_out = a2;
+  aerr_out = aerr;
 }
 
 }  // namespace fastc

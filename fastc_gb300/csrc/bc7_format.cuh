@@ -23,7 +23,7 @@ struct ModeAttr {
   int has_rotation, has_idx_mode, pbit;
 };
 
-__host__ __device__ inline ModeAttr mode_attr(int mode) {
+__host__ __device__ constexpr ModeAttr mode_attr(int mode) {
   switch (mode) {
     case 0: return {4, 3, 3, 0, 4, 0, 0, 0, kPBitUnique};
     case 1: return {6, 2, 3, 0, 6, 0, 0, 0, kPBitShared};

@@ -25,6 +25,7 @@
 #include "bc7_format.cuh"
 #include "bc7_kernels.cuh"
 #include "bc7_block.cuh"
+#include "bc7_pipeline.cuh"
 
 namespace fastc {
 
@@ -116,6 +117,7 @@ void upload_tables(int device) {
   build_endpoint_tables(opt7, opt6);
   cudaMemcpyToSymbol(c_opt7, opt7, sizeof(opt7));
   cudaMemcpyToSymbol(c_opt6, opt6, sizeof(opt6));
+  upload_pipeline_tables(device, opt7, opt6);
   done[device] = true;
 }
 
@@ -398,8 +400,8 @@ int encode_ctas_per_sm(int warps) {
   return (e == cudaSuccess && n > 0) ? n : 1;
 }
 
-int launch_encode(const JobDev *jobs_dev, int njobs, uint64_t total, const EncodeScratch &sc,
-                  LaunchShape shape, void *stream) {
+int launch_rank_prepass(const JobDev *jobs_dev, int njobs, uint64_t total,
+                        const EncodeScratch &sc, void *stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (total == 0) return 0;
   const uint32_t nchunks = (uint32_t)((total + kRankChunk - 1) / kRankChunk);
@@ -407,6 +409,17 @@ int launch_encode(const JobDev *jobs_dev, int njobs, uint64_t total, const Encod
                                                   sc.chunk_prefix);
   scan_kernel<<<1, 1024, 0, st>>>(sc.chunk_prefix, nchunks, sc.counter, sc.status,
                                   sc.singles);
+  return (int)cudaPeekAtLastError();
+}
+
+int launch_encode(const JobDev *jobs_dev, int njobs, uint64_t total, const EncodeScratch &sc,
+                  LaunchShape shape, void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (total == 0) return 0;
+  {
+    const int e = launch_rank_prepass(jobs_dev, njobs, total, sc, stream);
+    if (e) return e;
+  }
   const int ctas = shape.ctas > 0 ? shape.ctas : 1;
   switch (shape.warps_per_cta) {
     case 1:

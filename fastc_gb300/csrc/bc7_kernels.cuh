@@ -51,6 +51,10 @@ int launch_encode(const JobDev *jobs_dev, int njobs, uint64_t total_blocks,
 int launch_decode(const uint8_t *blocks, uint8_t *rgba, uint32_t width, uint32_t height,
                   int spec_semantics, void *stream);
 int device_sm_count(int device);
+// The single-colour rank pre-pass (classify + scan); also resets the work
+// counter and status of `scratch`.
+int launch_rank_prepass(const JobDev *jobs_dev, int njobs, uint64_t total_blocks,
+                        const EncodeScratch &scratch, void *stream);
 // Resident CTAs per SM of the encoder with this many warps per CTA.
 int encode_ctas_per_sm(int warps_per_cta);
 

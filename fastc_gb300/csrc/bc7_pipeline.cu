@@ -1,0 +1,961 @@
+// Task-parallel BC7 encoder for sm_103a.
+//
+// The block search of FasTC's CompressBC7Block (BPTCEncoder/src/
+// Compressor.cpp:1819-1860) is split into stages so that every warp runs 32
+// pieces of identical work:
+//
+//   select_kernel   one warp per 4x4 block (texels staged in shared memory
+//                   from 128-bit loads): trivial blocks, the 64+64 shape
+//                   estimate of BoxSelection, and the number of cluster fits
+//                   each BC7 mode needs.
+//   count scan      exclusive scan of those counts, mode-major, so all fits
+//                   of one mode are contiguous in the task arrays.
+//   emit_kernel     one thread per block writes its task descriptors.
+//   setup_kernel    one thread per cluster fit: PCA, k-means, least squares,
+//                   grid clamp, first QuantizedError (CP:921-1094, 632-919).
+//   anneal_kernel   persistent; one thread per fit with refill from a queue:
+//                   the simulated annealing (CP:538-630) in exact integer
+//                   arithmetic, specialised per mode.
+//   pack_kernel     one thread per block: FasTC's arg-min over modes and the
+//                   128-bit packing (CP:1752-1817, 1096-1298).
+//
+// Blocks are processed in chunks so that the task arrays fit a fixed
+// scratch size; every stage is asynchronous and graph-capturable.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cstdint>
+
+#include "bc7_block.cuh"
+#include "bc7_encode.cuh"
+#include "bc7_format.cuh"
+#include "bc7_kernels.cuh"
+#include "bc7_pipeline.cuh"
+
+namespace fastc {
+
+__constant__ uint32_t q_part2[64] = {FASTC_PART2_WORDS};
+__constant__ uint32_t q_part3[64] = {FASTC_PART3_WORDS};
+__constant__ uint8_t q_anchor2[64] = {FASTC_ANCHOR2_BYTES};
+__constant__ uint8_t q_anchor3[64] = {FASTC_ANCHOR3_BYTES};
+__constant__ uint32_t q_watermark[9] = {FASTC_WATERMARK_WORDS};
+__constant__ uint32_t q_opt7[256];
+__constant__ uint32_t q_opt6[256];
+// QuantizeChannel (RGBAEndpoints.cpp:126-165) tabulated for masks of the top
+// `prec` bits, prec = 1..8, and p-bit -1/0/1: [prec-1][pbit+1][value].
+__constant__ uint8_t q_qlut[8][3][256];
+
+// ---------------------------------------------------------------------------
+// Host-side table construction
+// ---------------------------------------------------------------------------
+
+static uint8_t host_quantize(uint32_t val, uint32_t mask, int pbit) {
+  if (mask == 0xFF) return (uint8_t)val;
+  if (mask == 0) return 0xFF;
+  uint32_t prec = 0;
+  for (uint32_t m = mask; m; m &= m - 1) prec++;
+  const uint32_t step = 1u << (8 - prec);
+  uint32_t lval = val & mask, hval = lval + step;
+  if (pbit >= 0) {
+    prec++;
+    lval |= (uint32_t)(pbit != 0) << (8 - prec);
+    hval |= (uint32_t)(pbit != 0) << (8 - prec);
+  }
+  if (lval > val) {
+    lval -= step;
+    hval -= step;
+  }
+  lval |= lval >> prec;
+  hval |= hval >> prec;
+  const uint32_t l8 = lval & 0xFF, h8 = hval & 0xFF;
+  const uint32_t dl = val > l8 ? val - l8 : l8 - val, dh = val > h8 ? val - h8 : h8 - val;
+  return (uint8_t)(dl < dh ? l8 : h8);
+}
+
+void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t opt6[256]) {
+  static bool done[64] = {false};
+  if (device < 0 || device >= 64 || done[device]) return;
+  static uint8_t lut[8][3][256];
+  for (int p = 1; p <= 8; p++)
+    for (int b = -1; b <= 1; b++)
+      for (int v = 0; v < 256; v++)
+        lut[p - 1][b + 1][v] = host_quantize((uint32_t)v, (0xFFu << (8 - p)) & 0xFFu, b);
+  cudaMemcpyToSymbol(q_qlut, lut, sizeof(lut));
+  cudaMemcpyToSymbol(q_opt7, opt7, 256 * sizeof(uint32_t));
+  cudaMemcpyToSymbol(q_opt6, opt6, 256 * sizeof(uint32_t));
+  done[device] = true;
+}
+
+// ---------------------------------------------------------------------------
+// Shared helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int find_job_p(const JobDev *jobs, int njobs, uint64_t g) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].begin <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ uint4 load_row_p(const JobDev &jb, uint32_t lin, int r) {
+  const uint32_t bw = jb.width >> 2;
+  const uint32_t bx = lin % bw, by = lin / bw;
+  const size_t off = ((size_t)(by * 4 + r - jb.row0) * jb.width + (size_t)bx * 4) * 4;
+  const uint8_t *p = jb.in + off;
+  if (jb.flags & kJobIn16) return __ldg(reinterpret_cast<const uint4 *>(p));
+  const uint32_t *q = reinterpret_cast<const uint32_t *>(p);
+  return make_uint4(__ldg(q), __ldg(q + 1), __ldg(q + 2), __ldg(q + 3));
+}
+
+__device__ __forceinline__ void store_block_p(const JobDev &jb, uint32_t lin, const uint32_t w[4]) {
+  uint8_t *dst = jb.out + (size_t)(lin - jb.out_first) * 16;
+  if (jb.flags & kJobOut16) {
+    *reinterpret_cast<uint4 *>(dst) = make_uint4(w[0], w[1], w[2], w[3]);
+  } else {
+    uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+    d[0] = w[0];
+    d[1] = w[1];
+    d[2] = w[2];
+    d[3] = w[3];
+  }
+}
+
+__device__ __forceinline__ Selection sel_of(const BlockSel &b) {
+  Selection s;
+  s.nshapes = b.nshapes;
+  s.shape[0] = b.shape0;
+  s.shape[1] = b.shape1;
+  s.nparts[0] = 2;
+  s.nparts[1] = b.nshapes > 1 ? 3 : 0;
+  s.modes = b.modes;
+  return s;
+}
+
+// Number of cluster fits CompressClusters (CP:1752-1817) runs for `mode`.
+__device__ __forceinline__ int mode_task_count(const Selection &sel, uint32_t modes, int mode) {
+  if (!(modes & (1u << mode))) return 0;
+  const ModeAttr a = mode_attr(mode);
+  const uint32_t nshapes = sel.nshapes < 5 ? sel.nshapes : 5;
+  int n = 0;
+  for (uint32_t s = 0; s < nshapes; s++) {
+    if (a.subsets != 1 && (uint32_t)a.subsets != sel.nparts[s]) continue;
+    if (sel.shape[s] >= 16 && mode == 0) continue;
+    n += a.has_rotation ? (mode == 4 ? 8 : 4) : a.subsets;
+  }
+  return n;
+}
+
+// The i-th fit of `mode`, in CompressClusters' order.
+__device__ __forceinline__ Task mode_task(const Selection &sel, int mode, int i) {
+  const ModeAttr a = mode_attr(mode);
+  const uint32_t nshapes = sel.nshapes < 5 ? sel.nshapes : 5;
+  const int nim = mode == 4 ? 2 : 1;
+  Task t{mode, 0, 0, 0, 0};
+  for (uint32_t s = 0; s < nshapes; s++) {
+    if (a.subsets != 1 && (uint32_t)a.subsets != sel.nparts[s]) continue;
+    if (sel.shape[s] >= 16 && mode == 0) continue;
+    const int per = a.has_rotation ? 4 * nim : a.subsets;
+    if (i < per) {
+      t.slot = (int)s;
+      if (a.has_rotation) {
+        t.rot = i / nim;
+        t.im = i % nim;
+      } else {
+        t.subset = i;
+      }
+      return t;
+    }
+    i -= per;
+  }
+  return t;
+}
+
+__device__ __forceinline__ uint32_t part_word_of(const Selection &sel, int mode, int slot) {
+  const int ns = mode_attr(mode).subsets;
+  const uint32_t shape = sel.shape[slot];
+  return ns == 2 ? q_part2[shape] : (ns == 3 ? q_part3[shape] : 0u);
+}
+
+// offset of entry i of a chunk-scanned array
+__device__ __forceinline__ uint32_t scanned(const uint16_t *local, const uint32_t *chunk, uint64_t i) {
+  return chunk[i / kRankChunk] + local[i];
+}
+
+// ---------------------------------------------------------------------------
+// select
+// ---------------------------------------------------------------------------
+
+template <int kWarps>
+__global__ void __launch_bounds__(kWarps * 32) select_kernel(
+    const JobDev *__restrict__ jobs, int njobs, uint64_t c0, uint32_t nb,
+    const uint16_t *__restrict__ rank_local, const uint32_t *__restrict__ rank_chunk,
+    BlockSel *__restrict__ sel, uint8_t *__restrict__ counts, uint32_t *status) {
+  __shared__ uint32_t s_part2[64], s_part3[64];
+  __shared__ uint32_t s_px[kWarps][16];
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+    s_part2[i] = q_part2[i];
+    s_part3[i] = q_part3[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t *px = s_px[wid];
+  for (uint32_t gl = blockIdx.x * kWarps + wid; gl < nb; gl += gridDim.x * kWarps) {
+    const uint64_t g = c0 + gl;
+    const int j = find_job_p(jobs, njobs, g);
+    const JobDev &jb = jobs[j];
+    const uint32_t lin = jb.first + (uint32_t)(g - jb.begin);
+    if (lane < 4) {
+      const uint4 v = load_row_p(jb, lin, lane);
+      px[lane * 4 + 0] = v.x;
+      px[lane * 4 + 1] = v.y;
+      px[lane * 4 + 2] = v.z;
+      px[lane * 4 + 3] = v.w;
+    }
+    __syncwarp();
+    bool same = true, transparent = true;
+    for (int i = 0; i < 16; i++) {
+      same = same && px[i] == px[0];
+      transparent = transparent && (px[i] >> 24) == 0;
+    }
+    BlockSel bs;
+    bs.job = (uint32_t)j;
+    bs.lin = lin;
+    bs.shape0 = bs.shape1 = bs.nshapes = 0;
+    bs.modes = 0;
+    bs.done = 1;
+    bs.pad[0] = bs.pad[1] = bs.pad[2] = 0;
+    if (same || transparent) {
+      if (lane < 8) counts[(uint64_t)lane * nb + gl] = 0;
+      if (lane == 0) {
+        uint32_t out[4];
+        if (same) {
+          const uint64_t gb = jb.begin;
+          const uint32_t rg = rank_chunk[g / kRankChunk] + rank_local[g];
+          const uint32_t rb = (jb.flags & kJobWmGlobal)
+                                  ? 0u
+                                  : rank_chunk[gb / kRankChunk] + rank_local[gb];
+          single_color_block(px[0], jb.wm_start + (rg - rb), q_opt7, q_watermark, out);
+        } else {
+          out[0] = 1u << 6;
+          out[1] = out[2] = out[3] = 0;
+        }
+        store_block_p(jb, lin, out);
+        sel[gl] = bs;
+      }
+      __syncwarp();
+      continue;
+    }
+    const Selection s = box_selection_warp(px, s_part2, s_part3, (int)jb.metric, lane);
+    uint32_t modes = s.modes & jb.modes;
+    if (modes == 0) modes = jb.modes & 0xFF;  // FasTC: undefined behaviour
+    const int c = lane < 8 ? mode_task_count(s, modes, lane) : 0;
+    int total = c;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) total += __shfl_xor_sync(0xFFFFFFFFu, total, o);
+    const bool overflow = total > kMaxBlockTasks;  // not reachable with BC7's mode table
+    if (lane < 8) counts[(uint64_t)lane * nb + gl] = overflow ? 0 : (uint8_t)c;
+    if (lane == 0) {
+      bs.shape0 = (uint8_t)s.shape[0];
+      bs.shape1 = (uint8_t)s.shape[1];
+      bs.nshapes = (uint8_t)s.nshapes;
+      bs.modes = overflow ? 0 : (uint8_t)modes;
+      bs.done = 0;
+      if (overflow) atomicOr(status, 2u);
+      sel[gl] = bs;
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// counts -> offsets (two-level exclusive scan)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kRankChunk) scan_local_u8_kernel(const uint8_t *in, uint64_t n,
+                                                                   uint16_t *local,
+                                                                   uint32_t *chunk_total) {
+  __shared__ uint32_t s_warp[32];
+  const uint64_t i = (uint64_t)blockIdx.x * kRankChunk + threadIdx.x;
+  const uint32_t v = i < n ? in[i] : 0u;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) s_warp[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    const uint32_t w = s_warp[lane];
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    s_warp[lane] = wi - w;
+    if (lane == 31) chunk_total[blockIdx.x] = wi;
+  }
+  __syncthreads();
+  if (i < n) local[i] = (uint16_t)(s_warp[wid] + incl - v);
+}
+
+// In-place exclusive scan of the chunk totals; writes the grand total and
+// resets the annealing queue.
+__global__ void __launch_bounds__(1024) scan_chunks_kernel(uint32_t *chunk, uint32_t nchunks,
+                                                           PipelineCounters *ctr) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_carry;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < nchunks; base += 1024) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < nchunks ? chunk[i] : 0u;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_warp[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      const uint32_t w = s_warp[lane];
+      uint32_t wi = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+        if (lane >= o) wi += t;
+      }
+      s_warp[lane] = wi - w;
+    }
+    __syncthreads();
+    const uint32_t carry = s_carry;
+    if (i < nchunks) chunk[i] = carry + s_warp[wid] + incl - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) s_carry = carry + s_warp[wid] + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    ctr->tasks = s_carry;
+    ctr->anneal_next = 0ull;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// emit
+// ---------------------------------------------------------------------------
+
+__global__ void emit_kernel(uint32_t nb, const uint8_t *__restrict__ counts,
+                            const uint16_t *__restrict__ local, const uint32_t *__restrict__ chunk,
+                            uint2 *__restrict__ desc) {
+  const uint32_t gl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gl >= nb) return;
+  for (int m = 0; m < 8; m++) {
+    const uint64_t i = (uint64_t)m * nb + gl;
+    const uint32_t c = counts[i];
+    if (!c) continue;
+    const uint32_t base = scanned(local, chunk, i);
+    for (uint32_t k = 0; k < c; k++) desc[base + k] = make_uint2(gl, (uint32_t)m | (k << 8));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// setup: one thread per cluster fit
+// ---------------------------------------------------------------------------
+
+constexpr int kSetupThreads = 128;
+
+__global__ void __launch_bounds__(kSetupThreads) setup_kernel(
+    const JobDev *__restrict__ jobs, const BlockSel *__restrict__ sel,
+    const uint2 *__restrict__ desc, const PipelineCounters *__restrict__ ctr,
+    TaskState *__restrict__ state, uint32_t *status) {
+  __shared__ uint32_t s_px[kSetupThreads * 17];
+  uint32_t *px = s_px + threadIdx.x * 17;
+  const uint32_t ntasks = ctr->tasks;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntasks;
+       t += gridDim.x * blockDim.x) {
+    const uint2 d = desc[t];
+    const uint32_t gl = d.x;
+    const int mode = (int)(d.y & 0xFF), i = (int)(d.y >> 8);
+    const BlockSel bs = sel[gl];
+    const JobDev &jb = jobs[bs.job];
+    const Selection s = sel_of(bs);
+    const Task tk = mode_task(s, mode, i);
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const uint4 v = load_row_p(jb, bs.lin, r);
+      px[r * 4 + 0] = v.x;
+      px[r * 4 + 1] = v.y;
+      px[r * 4 + 2] = v.z;
+      px[r * 4 + 3] = v.w;
+    }
+    const uint32_t bw = jb.width >> 2;
+    const uint32_t bx = bs.lin % bw, by = bs.lin / bw;
+    ModeCtx m;
+    m.mode = mode;
+    m.a = mode_attr(mode);
+    m.steps = (int)jb.steps;
+    m.metric = (int)jb.metric;
+    m.rot = tk.rot;
+    m.idx_mode = tk.im;
+    m.status = status;
+    m.lcg = 0;
+    Cluster c;
+    make_cluster(px, part_word_of(s, mode, tk.slot), tk.subset, c);
+    FitSetup st;
+    st.idx = 0;
+    st.pbit = 0;
+    TaskState o;
+    o.aerr = 0.0;
+    o.aidx = 0;
+    o.a1 = o.a2 = 0.0f;
+    if (m.a.has_rotation) {
+      fit_alpha_setup(m, c, q_opt6, st, o.a1, o.a2, o.aidx, o.aerr);
+    } else {
+      fit_rgb_setup(m, c, st);
+    }
+    o.err = st.err;
+    o.idx = st.idx;
+    o.p1 = to_pixel(st.p1, 0xFFFFFFFFu, -1);
+    o.p2 = to_pixel(st.p2, 0xFFFFFFFFu, -1);
+    o.gl = gl;
+    o.mode = (uint8_t)mode;
+    o.slot = (uint8_t)tk.slot;
+    o.subset = (uint8_t)tk.subset;
+    o.rotim = (uint8_t)((tk.rot << 1) | tk.im);
+    o.lcg = fit_seed(jb.seed, bx, by,
+                     (uint32_t)((mode << 8) | (tk.slot << 7) | (tk.subset << 4) | (tk.rot << 1) | tk.im));
+    o.steps = (uint16_t)jb.steps;
+    o.pbit = (uint8_t)st.pbit;
+    o.flags = (uint8_t)((st.anneal ? kTaskAnneal : 0u) | (jb.metric ? kTaskNonuniform : 0u));
+    state[t] = o;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// anneal: persistent, one thread per fit, refilled from the task array
+// ---------------------------------------------------------------------------
+
+constexpr int kAnnealThreads = 128;
+
+struct AnnealLane {
+  uint32_t t;        // task
+  uint32_t p1, p2;   // current endpoints (bytes)
+  uint32_t b1, b2;   // best endpoints
+  uint32_t lcg;
+  float cur_err, best_err;
+  uint64_t idx;      // best indices (texel nibbles)
+  uint64_t tex;      // texel index of point k, 4 bits each
+  int cur_pbit, best_pbit;
+  int energy, steps, n, kind;
+  float w[4];        // rotated metric weights (nonuniform metric only)
+};
+
+// Weight of a `bits`-bit index, templated so the divisor is a constant.
+template <int kBits>
+__device__ __forceinline__ int wt(int j) {
+  return (int)((64u * (uint32_t)j + (uint32_t)(((1 << kBits) - 1) / 2)) / (uint32_t)((1 << kBits) - 1));
+}
+
+// QuantizedError (RGBAEndpoints.cpp:190-310) for integer endpoints and
+// points. The projection index floor(D k / L) is computed exactly with
+// integers; only when D k is a multiple of L does FasTC's float rounding
+// matter, and that case repeats FasTC's float division and product.
+template <int kBits, bool kRot, bool kUniform>
+__device__ __forceinline__ float qe_int(const uint32_t *pts, const uint32_t *proj, int stride, int n,
+                                        uint32_t q1, uint32_t q2, const float *w, bool want_idx,
+                                        uint64_t tex, uint64_t &idx) {
+  constexpr int nb = 1 << kBits;
+  constexpr int km = nb - 1;
+  int u1[4], u2[4], dir[4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    u1[c] = (int)((q1 >> (8 * c)) & 0xFF);
+    u2[c] = (int)((q2 >> (8 * c)) & 0xFF);
+    dir[c] = u2[c] - u1[c];
+  }
+  const int L = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2] + dir[3] * dir[3];
+  int itotal = 0;
+  float ftotal = 0.0f;
+  if (L == 0) {
+    for (int k = 0; k < n; k++) {
+      const uint32_t e = pts[k * stride];
+      if (kUniform) {
+        int s = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int d = (int)((e >> (8 * c)) & 0xFF) - u1[c];
+          s += d * d;
+        }
+        itotal += s;
+      } else {
+        float ev[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int d = (int)((e >> (8 * c)) & 0xFF) - u1[c];
+          ev[c] = __fmul_rn((float)(d < 0 ? -d : d), w[c]);
+        }
+        ftotal = __fadd_rn(ftotal, dot4(ev, ev));
+      }
+      if (want_idx) set_nib(idx, (int)((tex >> (4 * k)) & 15), 0);
+    }
+    return kUniform ? (float)itotal : ftotal;
+  }
+  const float rl = __frcp_rn((float)L);
+  for (int k = 0; k < n; k++) {
+    const uint32_t e = pts[k * stride];
+    const uint32_t p = kRot ? proj[k * stride] : e;
+    int D = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) D += ((int)((p >> (8 * c)) & 0xFF) - u1[c]) * dir[c];
+    const int num = D * km;
+    int j = __float2int_rd(__fmul_rn((float)num, rl));
+    int r = num - j * L;
+    if (r < 0) {
+      j--;
+      r += L;
+    } else if (r >= L) {
+      j++;
+      r -= L;
+    }
+    int j1 = j, j2 = j + 1;
+    if (r == 0) {
+      const float sc = __fmul_rn(__fdiv_rn((float)D, (float)L), (float)km);
+      j1 = __float2int_rz(floorf(sc));
+      j2 = __float2int_rz(ceilf(sc));
+    }
+    j1 = min(max(0, j1), nb - 1);
+    j2 = min(j2, nb - 1);
+    int ec[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) ec[c] = (int)((e >> (8 * c)) & 0xFF);
+    const int w1a = wt<kBits>(j1), w0a = 64 - w1a;
+    if (kUniform) {
+      int e1 = 0;
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const int d = ec[c] - ((u1[c] * w0a + u2[c] * w1a + 32) >> 6);
+        e1 += d * d;
+      }
+      int best = e1, bj = j1;
+      if (j2 > j1) {
+        const int w1b = wt<kBits>(j1 + 1), w0b = 64 - w1b;
+        int e2 = 0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int d = ec[c] - ((u1[c] * w0b + u2[c] * w1b + 32) >> 6);
+          e2 += d * d;
+        }
+        if (e2 < e1) {
+          best = e2;
+          bj = j1 + 1;
+        }
+      }
+      itotal += best;
+      if (want_idx) set_nib(idx, (int)((tex >> (4 * k)) & 15), (uint32_t)bj);
+    } else {
+      float ev[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const int d = ec[c] - ((u1[c] * w0a + u2[c] * w1a + 32) >> 6);
+        ev[c] = __fmul_rn((float)(d < 0 ? -d : d), w[c]);
+      }
+      const float e1 = dot4(ev, ev);
+      float best = e1;
+      int bj = j1;
+      if (j2 > j1) {
+        const int w1b = wt<kBits>(j1 + 1), w0b = 64 - w1b;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int d = ec[c] - ((u1[c] * w0b + u2[c] * w1b + 32) >> 6);
+          ev[c] = __fmul_rn((float)(d < 0 ? -d : d), w[c]);
+        }
+        const float e2 = dot4(ev, ev);
+        if (e2 < e1) {
+          best = e2;
+          bj = j1 + 1;
+        }
+      }
+      ftotal = __fadd_rn(ftotal, best);
+      if (want_idx) set_nib(idx, (int)((tex >> (4 * k)) & 15), (uint32_t)bj);
+    }
+  }
+  return kUniform ? (float)itotal : ftotal;
+}
+
+// ToPixel (RGBAEndpoints.cpp:167-177) of integer endpoints through the table.
+template <int kColorBits, int kAlphaBits>
+__device__ __forceinline__ uint32_t qpix(const uint8_t *lut, uint32_t v, int pbit) {
+  const uint8_t *lc = lut + ((kColorBits - 1) * 3 + (pbit + 1)) * 256;
+  uint32_t r = (uint32_t)lc[v & 0xFF] | ((uint32_t)lc[(v >> 8) & 0xFF] << 8) |
+               ((uint32_t)lc[(v >> 16) & 0xFF] << 16);
+  if (kAlphaBits == 0) return r | 0xFF000000u;
+  const uint8_t *la = lut + ((kAlphaBits - 1) * 3 + (pbit + 1)) * 256;
+  return r | ((uint32_t)la[v >> 24] << 24);
+}
+
+// One step of OptimizeEndpointsForCluster (CP:583-624) for mode kMode
+// with kBits-bit indices. Returns true when the fit is finished.
+template <int kMode, int kBits, bool kUniform>
+__device__ __forceinline__ bool anneal_step(AnnealLane &s, const uint32_t *pts, const uint32_t *proj,
+                                            int stride, const uint8_t *lut) {
+  constexpr ModeAttr a = mode_attr(kMode);
+  constexpr bool kRot = a.has_rotation != 0;
+  constexpr bool kHasPbits = a.pbit != kPBitNone;
+  if (!(s.best_err > 0.0f && s.energy < s.steps)) return true;
+  const float temp = __fdiv_rn((float)s.energy, (float)(s.steps - 1));
+  // PickBestNeighboringEndpoints (CP:426-498), integer endpoints
+  constexpr int sc = 1 << (8 - a.color_bits);
+  constexpr int sa = kMode < 4 ? 0 : (1 << (8 - a.alpha_bits));
+  int npbit = 0;
+  if (kHasPbits) npbit = a.pbit == kPBitShared ? (s.cur_pbit + 1) % 2 : 3 - s.cur_pbit;
+  const int cur_combo = pbit_combo(a, s.cur_pbit);
+  uint32_t np1 = s.p1, np2 = s.p2;
+  bool visited = true;
+  int guard = -1;
+  while (visited && ++guard < 16) {
+#pragma unroll
+    for (int pt = 0; pt < 2; pt++) {
+      const uint32_t p = pt ? s.p1 : s.p2;
+      const uint32_t dir = lcg_next(s.lcg) % 16;
+      const int old = pt ? pb_second(cur_combo) : pb_first(cur_combo);
+      uint32_t np = 0;
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        int v = (int)((p >> (8 * c)) & 0xFF);
+        const int st = c == 3 ? sa : sc;
+        const bool down = (dir >> c) & 1;
+        if (kHasPbits) {
+          if (down && old == 0) v -= st;
+          else if (!down && old == 1) v += st;
+        } else {
+          v = down ? v - st : v + st;
+        }
+        v = min(max(v, 0), 255);
+        np |= (uint32_t)v << (8 * c);
+      }
+      if (pt) np1 = np;
+      else np2 = np;
+    }
+    visited = np1 == s.b1 && np2 == s.b2 && npbit == s.best_pbit;
+  }
+  // QuantizedError with the new p-bit combo (kPBits[0] for modes without
+  // p-bits, as FasTC passes it)
+  const int pc = pbit_combo(a, npbit);
+  const uint32_t q1 = qpix<a.color_bits, a.alpha_bits>(lut, np1, pb_first(pc));
+  const uint32_t q2 = qpix<a.color_bits, a.alpha_bits>(lut, np2, pb_second(pc));
+  uint64_t dummy = 0;
+  const float err = qe_int<kBits, kRot, kUniform>(pts, proj, stride, s.n, q1, q2, s.w, false, s.tex, dummy);
+  // AcceptNewEndpointError (CP:524-536)
+  bool accept = err < s.cur_err;
+  if (!accept) {
+    const uint32_t r16 = lcg_next(s.lcg) & 0xFFFF;
+    const uint32_t mant = (r16 << 8) | (r16 >> 7);
+    const float r = __fsub_rn(__uint_as_float((127u << 23) | mant), 1.0f);
+    if (r < 1.0f) {
+      const float x = __fdiv_rn(__fmul_rn(0.1f, __fsub_rn(s.cur_err, err)), temp);
+      accept = mant == 0 ? (x > -745.0f) : (r < portable_expf(x));
+    }
+  }
+  if (accept) {
+    s.cur_err = err;
+    s.p1 = np1;
+    s.p2 = np2;
+    s.cur_pbit = npbit;
+  }
+  if (err < s.best_err) {
+    s.idx = 0;
+    qe_int<kBits, kRot, kUniform>(pts, proj, stride, s.n, q1, q2, s.w, true, s.tex, s.idx);
+    s.b1 = np1;
+    s.b2 = np2;
+    s.best_pbit = npbit;
+    s.best_err = err;
+    s.energy = 0;
+  }
+  s.energy++;
+  return false;
+}
+
+// Fit kinds: (mode, colour index bits) pairs; mode 4 anneals with 2-bit
+// indices in index mode 0 and 3-bit indices in index mode 1.
+__device__ __forceinline__ int kind_of(int mode, int im) {
+  return mode == 4 ? (im ? 8 : 4) : mode;
+}
+
+template <bool kUniform>
+__device__ __forceinline__ bool anneal_dispatch(AnnealLane &s, const uint32_t *pts,
+                                                const uint32_t *proj, int stride,
+                                                const uint8_t *lut) {
+  switch (s.kind) {
+    case 0: return anneal_step<0, 3, kUniform>(s, pts, proj, stride, lut);
+    case 1: return anneal_step<1, 3, kUniform>(s, pts, proj, stride, lut);
+    case 2: return anneal_step<2, 2, kUniform>(s, pts, proj, stride, lut);
+    case 3: return anneal_step<3, 2, kUniform>(s, pts, proj, stride, lut);
+    case 4: return anneal_step<4, 2, kUniform>(s, pts, proj, stride, lut);
+    case 5: return anneal_step<5, 2, kUniform>(s, pts, proj, stride, lut);
+    case 6: return anneal_step<6, 4, kUniform>(s, pts, proj, stride, lut);
+    case 7: return anneal_step<7, 2, kUniform>(s, pts, proj, stride, lut);
+    default: return anneal_step<4, 3, kUniform>(s, pts, proj, stride, lut);
+  }
+}
+
+__global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
+    const JobDev *__restrict__ jobs, const BlockSel *__restrict__ sel,
+    PipelineCounters *__restrict__ ctr, TaskState *__restrict__ state) {
+  __shared__ uint8_t s_lut[8 * 3 * 256];
+  __shared__ uint32_t s_pts[16 * kAnnealThreads];
+  __shared__ uint32_t s_proj[16 * kAnnealThreads];
+  for (int i = threadIdx.x; i < 8 * 3 * 256; i += blockDim.x)
+    s_lut[i] = (&q_qlut[0][0][0])[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  uint32_t *pts = s_pts + threadIdx.x;
+  uint32_t *proj = s_proj + threadIdx.x;
+  const uint32_t ntasks = ctr->tasks;
+  AnnealLane s;
+  bool active = false, exhausted = false, uniform = true;
+  for (;;) {
+    const bool need = !active && !exhausted;
+    const uint32_t nmask = __ballot_sync(0xFFFFFFFFu, need);
+    if (nmask) {
+      uint32_t base = 0;
+      const int leader = __ffs(nmask) - 1;
+      if (lane == leader) base = (uint32_t)atomicAdd(&ctr->anneal_next, (unsigned long long)__popc(nmask));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (need) {
+        const uint32_t t = base + __popc(nmask & ((1u << lane) - 1u));
+        if (t >= ntasks) {
+          exhausted = true;
+        } else {
+          const TaskState o = state[t];
+          if (o.flags & kTaskAnneal) {
+            const BlockSel bs = sel[o.gl];
+            const JobDev &jb = jobs[bs.job];
+            const Selection sl = sel_of(bs);
+            const uint32_t part = part_word_of(sl, o.mode, o.slot);
+            const int rot = o.rotim >> 1;
+            s.t = t;
+            s.p1 = s.b1 = o.p1;
+            s.p2 = s.b2 = o.p2;
+            s.cur_pbit = s.best_pbit = o.pbit;
+            s.cur_err = s.best_err = (float)o.err;
+            s.idx = o.idx;
+            s.lcg = o.lcg;
+            s.energy = 0;
+            s.steps = o.steps;
+            s.kind = kind_of(o.mode, o.rotim & 1);
+            uniform = !(o.flags & kTaskNonuniform);
+            ModeCtx m;
+            m.a = mode_attr(o.mode);
+            m.rot = rot;
+            m.metric = uniform ? 0 : 1;
+            metric_of(m, s.w);
+            int n = 0;
+            uint64_t tex = 0;
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+              const uint4 v = load_row_p(jb, bs.lin, r);
+              const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+              for (int c = 0; c < 4; c++) {
+                const int ti = r * 4 + c;
+                if ((int)((part >> (2 * ti)) & 3) != o.subset) continue;
+                const uint32_t e = vv[c];
+                uint32_t pr = e;
+                if (m.a.has_rotation) {
+                  // the colour fit sees the rotated texel with alpha 255
+                  if (rot) {
+                    const uint32_t sh = 8u * (uint32_t)(rot - 1);
+                    pr = (pr & ~(0xFFu << sh)) | ((e >> 24) << sh);
+                  }
+                  pr |= 0xFF000000u;
+                }
+                pts[n * kAnnealThreads] = e;
+                proj[n * kAnnealThreads] = pr;
+                tex |= (uint64_t)ti << (4 * n);
+                n++;
+              }
+            }
+            s.n = n;
+            s.tex = tex;
+            active = true;
+          }
+        }
+      }
+    }
+    if (__all_sync(0xFFFFFFFFu, exhausted && !active)) break;
+    if (active) {
+      const bool done = uniform ? anneal_dispatch<true>(s, pts, proj, kAnnealThreads, s_lut)
+                                : anneal_dispatch<false>(s, pts, proj, kAnnealThreads, s_lut);
+      if (done) {
+        TaskState &o = state[s.t];
+        o.p1 = s.b1;
+        o.p2 = s.b2;
+        o.pbit = (uint8_t)s.best_pbit;
+        o.err = (double)s.best_err;
+        o.idx = s.idx;
+        active = false;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pack: one thread per block
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void fit_out_of(const TaskState &o, FitOut &f) {
+  const bool rotation = mode_attr(o.mode).has_rotation != 0;
+  unpack4(o.p1, f.p1);
+  unpack4(o.p2, f.p2);
+  if (rotation) {
+    f.p1[3] = o.a1;
+    f.p2[3] = o.a2;
+  }
+  f.err = o.err;
+  f.idx = o.idx;
+  f.aidx = o.aidx;
+  f.pbit = o.pbit;
+}
+
+__global__ void pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
+                            const BlockSel *__restrict__ sel, const uint16_t *__restrict__ local,
+                            const uint32_t *__restrict__ chunk,
+                            const TaskState *__restrict__ state) {
+  __shared__ uint32_t s_part2[64], s_part3[64];
+  __shared__ uint8_t s_anc2[64], s_anc3[64];
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+    s_part2[i] = q_part2[i];
+    s_part3[i] = q_part3[i];
+    s_anc2[i] = q_anchor2[i];
+    s_anc3[i] = q_anchor3[i];
+  }
+  __syncthreads();
+  const uint32_t gl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gl >= nb) return;
+  const BlockSel bs = sel[gl];
+  if (bs.done) return;
+  const JobDev &jb = jobs[bs.job];
+  const Selection s = sel_of(bs);
+  const uint32_t modes = bs.modes;
+  double best = DBL_MAX;
+  int best_mode = 8, best_slot = 0, best_rot = 0, best_im = 0;
+  uint32_t best_first = 0;
+  const uint32_t nshapes = s.nshapes < 5 ? s.nshapes : 5;
+  for (int oi = 0; oi < 8; oi++) {
+    const int mode = mode_order(oi);
+    if (!(modes & (1u << mode))) continue;
+    const ModeAttr a = mode_attr(mode);
+    uint32_t t = scanned(local, chunk, (uint64_t)mode * nb + gl);
+    for (uint32_t sl = 0; sl < nshapes; sl++) {
+      if (a.subsets != 1 && (uint32_t)a.subsets != s.nparts[sl]) continue;
+      if (s.shape[sl] >= 16 && mode == 0) continue;
+      double total = 0.0;
+      uint32_t first = t;
+      int rot = 0, im = 0;
+      if (a.has_rotation) {
+        const int nim = mode == 4 ? 2 : 1;
+        double b = DBL_MAX;
+        for (int r = 0; r < 4; r++)
+          for (int k = 0; k < nim; k++, t++) {
+            const double e = state[t].err + state[t].aerr;
+            if (e < b) {
+              b = e;
+              first = t;
+              rot = r;
+              im = k;
+            }
+          }
+        total = total + b;
+      } else {
+        for (int ci = 0; ci < a.subsets; ci++, t++) total = total + state[t].err;
+      }
+      if (total < best) {
+        best = total;
+        best_mode = mode;
+        best_slot = (int)sl;
+        best_first = first;
+        best_rot = rot;
+        best_im = im;
+      }
+    }
+  }
+  uint32_t out[4];
+  if (best_mode == 8) {
+    out[0] = 1u << 6;
+    out[1] = out[2] = out[3] = 0;
+  } else {
+    FitOut f[3];
+    const int ns = mode_attr(best_mode).subsets;
+    for (int k = 0; k < ns; k++) fit_out_of(state[best_first + k], f[k]);
+    pack_block(best_mode, s, best_slot, f, s_anc2, s_anc3, s_part2, s_part3, best_rot, best_im, out);
+  }
+  store_block_p(jb, bs.lin, out);
+}
+
+// ---------------------------------------------------------------------------
+// launcher
+// ---------------------------------------------------------------------------
+
+size_t pipeline_scratch_bytes(uint64_t total_blocks) {
+  const uint64_t nb = total_blocks < kPipelineChunk ? total_blocks : kPipelineChunk;
+  const uint64_t n8 = 8 * nb;
+  const uint64_t tmax = (uint64_t)kMaxBlockTasks * nb;
+  size_t b = 256;
+  b += (nb * sizeof(BlockSel) + 255) & ~255ull;
+  b += (n8 + 255) & ~255ull;
+  b += (n8 * 2 + 255) & ~255ull;
+  b += (((n8 + kRankChunk - 1) / kRankChunk) * 4 + 255) & ~255ull;
+  b += (tmax * sizeof(uint2) + 255) & ~255ull;
+  b += (tmax * sizeof(TaskState) + 255) & ~255ull;
+  return b;
+}
+
+int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
+                    void *scratch, int sm_count, void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (total == 0) return 0;
+  int e = launch_rank_prepass(jobs, njobs, total, rank, stream);
+  if (e) return e;
+  const uint64_t cap = kPipelineChunk;
+  uint8_t *p = static_cast<uint8_t *>(scratch);
+  PipelineCounters *ctr = reinterpret_cast<PipelineCounters *>(p);
+  p += 256;
+  const uint64_t nbmax = total < cap ? total : cap;
+  BlockSel *sel = reinterpret_cast<BlockSel *>(p);
+  p += (nbmax * sizeof(BlockSel) + 255) & ~255ull;
+  uint8_t *counts = p;
+  p += (8 * nbmax + 255) & ~255ull;
+  uint16_t *local = reinterpret_cast<uint16_t *>(p);
+  p += (16 * nbmax + 255) & ~255ull;
+  uint32_t *chunk = reinterpret_cast<uint32_t *>(p);
+  p += (((8 * nbmax + kRankChunk - 1) / kRankChunk) * 4 + 255) & ~255ull;
+  uint2 *desc = reinterpret_cast<uint2 *>(p);
+  p += ((uint64_t)kMaxBlockTasks * nbmax * sizeof(uint2) + 255) & ~255ull;
+  TaskState *state = reinterpret_cast<TaskState *>(p);
+  for (uint64_t c0 = 0; c0 < total; c0 += cap) {
+    const uint32_t nb = (uint32_t)(total - c0 < cap ? total - c0 : cap);
+    const uint64_t n8 = 8ull * nb;
+    const uint32_t nchunks = (uint32_t)((n8 + kRankChunk - 1) / kRankChunk);
+    const int sel_ctas = (int)((nb + 3) / 4 < (uint64_t)sm_count * 16 ? (nb + 3) / 4 : (uint64_t)sm_count * 16);
+    select_kernel<4><<<sel_ctas, 128, 0, st>>>(jobs, njobs, c0, nb, rank.rank_local, rank.chunk_prefix,
+                                               sel, counts, rank.status);
+    scan_local_u8_kernel<<<nchunks, kRankChunk, 0, st>>>(counts, n8, local, chunk);
+    scan_chunks_kernel<<<1, 1024, 0, st>>>(chunk, nchunks, ctr);
+    emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, counts, local, chunk, desc);
+    setup_kernel<<<sm_count * 8, kSetupThreads, 0, st>>>(jobs, sel, desc, ctr, state, rank.status);
+    anneal_kernel<<<sm_count * 6, kAnnealThreads, 0, st>>>(jobs, sel, ctr, state);
+    pack_kernel<<<(nb + 127) / 128, 128, 0, st>>>(jobs, nb, sel, local, chunk, state);
+    e = (int)cudaPeekAtLastError();
+    if (e) return e;
+  }
+  return 0;
+}
+
+}  // namespace fastc

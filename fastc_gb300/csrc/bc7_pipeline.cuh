@@ -1,0 +1,56 @@
+// Data structures of the task-parallel BC7 encoder (bc7_pipeline.cu).
+#pragma once
+
+#include <cstdint>
+
+#include "bc7_kernels.cuh"
+
+namespace fastc {
+
+// Blocks per pipeline chunk; scratch grows with it.
+constexpr uint64_t kPipelineChunk = 256 * 1024;
+// Cluster fits one block can need. BC7's mode table caps it at 32 (opaque
+// block whose selection falls back to the caller's mask of modes 1,3-7).
+constexpr int kMaxBlockTasks = 32;
+
+// Per-block outcome of the select stage (16 bytes).
+struct BlockSel {
+  uint8_t shape0, shape1, nshapes;
+  uint8_t modes;  // modes to search (CompressClusters' selectedModes)
+  uint8_t done;   // 1: block already written (single colour / transparent)
+  uint8_t pad[3];
+  uint32_t job;   // index into the job table
+  uint32_t lin;   // raster block index within the job's texture
+};
+
+constexpr uint8_t kTaskAnneal = 1u;      // the annealing loop has work
+constexpr uint8_t kTaskNonuniform = 2u;  // nonuniform error metric
+
+// State of one cluster fit between the stages (64 bytes).
+struct __align__(16) TaskState {
+  double err;     // CompressCluster's return value (colour part for modes 4/5)
+  double aerr;    // alpha error (modes 4/5)
+  uint64_t idx;   // colour indices, 4 bits per texel
+  uint64_t aidx;  // alpha indices, 4 bits per texel (modes 4/5)
+  uint32_t p1, p2;  // endpoints as bytes (grid values)
+  float a1, a2;     // alpha endpoints (modes 4/5), as FasTC keeps them
+  uint32_t gl;      // block within the chunk
+  uint8_t mode, slot, subset, rotim;  // rotim = rotation << 1 | index mode
+  uint32_t lcg;     // annealing stream of this fit
+  uint16_t steps;
+  uint8_t pbit;
+  uint8_t flags;
+};
+
+struct PipelineCounters {
+  unsigned long long anneal_next;  // next task for the annealing refill
+  uint32_t tasks;                  // tasks in the current chunk
+  uint32_t pad;
+};
+
+void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t opt6[256]);
+size_t pipeline_scratch_bytes(uint64_t total_blocks);
+int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
+                    void *scratch, int sm_count, void *stream);
+
+}  // namespace fastc

@@ -184,8 +184,18 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_flags(fastc_bc7_plan plan, uint32_
 FASTC_BC7_API uint64_t fastc_bc7_plan_blocks(fastc_bc7_plan plan);
 FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_destroy(fastc_bc7_plan plan);
 
-/* Launch geometry: warps per CTA (1, 2, 4 or 8) and CTAs per SM of the
- * persistent encoder; 0 keeps the current value. Returns the values in use. */
+/* Encoder organisation. PIPELINE (default): a per-block select stage, one
+ * thread per cluster fit for the fit and the annealing (warps run 32 fits of
+ * one mode, refilled from a queue), a per-block pack stage. WARP_PER_BLOCK:
+ * one warp owns a block through the whole search, one lane per cluster fit.
+ * Both give the same blocks. Applies to calls and plans created afterwards. */
+#define FASTC_BC7_ENGINE_PIPELINE 0
+#define FASTC_BC7_ENGINE_WARP_PER_BLOCK 1
+FASTC_BC7_API fastc_bc7_status fastc_bc7_set_engine(int engine);
+FASTC_BC7_API int fastc_bc7_get_engine(void);
+
+/* Launch geometry of the warp-per-block engine: warps per CTA (1, 2, 4 or 8)
+ * and CTAs per SM of the persistent encoder; 0 keeps the current value. */
 FASTC_BC7_API fastc_bc7_status fastc_bc7_set_launch_shape(int warps_per_cta, int ctas_per_sm);
 FASTC_BC7_API fastc_bc7_status fastc_bc7_get_launch_shape(int *warps_per_cta, int *ctas_per_sm);
 

@@ -9,6 +9,16 @@ from conftest import golden_blocks, make_image
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=[0, 1], ids=["pipeline", "warp_per_block"], autouse=True)
+def engine(request, gpu):
+    """Every parity test runs on both encoder organisations."""
+    from fastc_gb300 import set_engine
+
+    set_engine(request.param)
+    yield request.param
+    set_engine(0)
+
+
 def gpu_compress(img, steps=0, metric=0, modes=0xFF, seed=0, wm=0):
     from fastc_gb300 import CompressionSettings, compress_image_data
 
