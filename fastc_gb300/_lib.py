@@ -61,6 +61,19 @@ class LogicalBlock(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("memory_budget", C.c_size_t), ("max_inflight", C.c_uint32),
+                ("max_batch_blocks", C.c_uint32), ("max_batch_jobs", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("cancelled", C.c_uint64), ("rejected", C.c_uint64), ("batches", C.c_uint64),
+                ("pixels_completed", C.c_uint64), ("bytes_in_use", C.c_size_t), ("peak_bytes", C.c_size_t),
+                ("p50_latency_ms", C.c_double), ("p99_latency_ms", C.c_double),
+                ("mean_latency_ms", C.c_double), ("max_latency_ms", C.c_double), ("mpix_per_s", C.c_double)]
+
+
 # Every function include/fastc_bc7.h declares, with its ctypes signature.
 SIGNATURES = {
     "fastc_bc7_settings_default": (None, [C.POINTER(Settings)]),
@@ -86,6 +99,16 @@ SIGNATURES = {
     "fastc_bc7_plan_destroy": (C.c_int, [C.c_void_p]),
     "fastc_bc7_set_watermark_counter": (None, [C.c_uint32]),
     "fastc_bc7_get_watermark_counter": (C.c_uint32, []),
+    "fastc_bc7_server_config_default": (None, [C.POINTER(ServerConfig)]),
+    "fastc_bc7_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "fastc_bc7_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Job), C.POINTER(Settings),
+                                          C.POINTER(C.c_uint64)]),
+    "fastc_bc7_server_poll": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "fastc_bc7_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int64]),
+    "fastc_bc7_server_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "fastc_bc7_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "fastc_bc7_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    "fastc_bc7_server_destroy": (C.c_int, [C.c_void_p]),
     "fastc_bc7_set_engine": (C.c_int, [C.c_int]),
     "fastc_bc7_get_engine": (C.c_int, []),
     "fastc_bc7_set_launch_shape": (C.c_int, [C.c_int, C.c_int]),

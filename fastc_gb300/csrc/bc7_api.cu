@@ -18,12 +18,14 @@
 #include "bc7_kernels.cuh"
 #include "bc7_pipeline.cuh"
 #include "fastc_bc7.h"
+#include "bc7_host.h"
 
 using fastc::EncodeScratch;
 using fastc::JobDev;
 using fastc::LaunchShape;
 
-namespace {
+namespace fastc {
+namespace host {
 
 thread_local std::string t_last_error;
 std::mutex g_mu;
@@ -39,11 +41,6 @@ fastc_bc7_status fail_cuda(cudaError_t e) {
   return FASTC_BC7_ERR_CUDA;
 }
 
-#define CK(expr)                              \
-  do {                                        \
-    cudaError_t e_ = (expr);                  \
-    if (e_ != cudaSuccess) return fail_cuda(e_); \
-  } while (0)
 
 bool settings_ok(const fastc_bc7_settings &s, fastc_bc7_status *why) {
   if (s.shape_selection_fn != nullptr) {
@@ -153,6 +150,13 @@ int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, 
   }
   return fastc::launch_encode(jobs, njobs, total, rank, shape, st);
 }
+
+}  // namespace host
+}  // namespace fastc
+
+using namespace fastc::host;
+
+namespace {
 
 // Grow-only device buffer.
 struct DevBuf {

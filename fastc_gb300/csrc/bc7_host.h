@@ -1,0 +1,48 @@
+// Host-side helpers shared by the C-ABI entry points (bc7_api.cu) and the
+// request server (bc7_server.cu). Internal to the library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+
+#include "bc7_kernels.cuh"
+#include "fastc_bc7.h"
+
+namespace fastc {
+namespace host {
+
+extern thread_local std::string t_last_error;
+extern std::mutex g_mu;  // guards the globals below and the host context
+extern int g_warps;
+extern uint32_t g_wm_next;
+extern int g_ctas_per_sm;
+extern int g_engine;
+
+// Records the CUDA error text and maps it to a status.
+fastc_bc7_status fail_cuda(cudaError_t e);
+
+#define CK(expr)                                               \
+  do {                                                         \
+    cudaError_t e_ = (expr);                                   \
+    if (e_ != cudaSuccess) return ::fastc::host::fail_cuda(e_); \
+  } while (0)
+
+bool settings_ok(const fastc_bc7_settings &s, fastc_bc7_status *why);
+// Raster block range of a job (FasTC's BPTCC::Compress walk), or false.
+bool job_range(const fastc_bc7_job &j, uint32_t *first, uint32_t *count);
+int current_device();
+LaunchShape pick_shape(uint64_t total);
+size_t rank_scratch_bytes(uint64_t total);
+size_t scratch_bytes(uint64_t total, int engine);
+EncodeScratch carve_scratch(void *base, uint64_t total);
+JobDev make_job(const fastc_bc7_job &j, const fastc_bc7_settings &s, uint32_t first,
+                uint32_t count, uint64_t begin);
+uint32_t align_flags(const void *in, const void *out);
+int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
+                  LaunchShape shape, cudaStream_t st);
+
+}  // namespace host
+}  // namespace fastc

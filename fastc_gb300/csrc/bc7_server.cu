@@ -1,0 +1,489 @@
+// Continuous-batching BC7 request server (fastc_bc7_server_* in
+// include/fastc_bc7.h).
+//
+// A worker thread owns the GPU side. Requests queue in FIFO order; whenever
+// one of `max_inflight` batch slots is free, the worker admits the pending
+// requests that fit the device-memory budget (texels, blocks, job table and
+// encoder scratch of the batch), uploads their texel rows, launches the
+// encoder on the slot's stream and queues the copy of the blocks into
+// pinned staging. A host callback on the stream wakes the worker when the
+// batch is done; it copies the blocks to the callers' buffers and returns
+// the memory to the budget. While one batch runs, the next is admitted,
+// uploaded and launched on another stream, so requests that arrive during a
+// batch overlap with it on the device. Each block's result depends only on
+// its texture, position and settings, so a request gives the same bytes
+// alone or in any mix.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "bc7_host.h"
+#include "bc7_kernels.cuh"
+#include "fastc_bc7.h"
+
+using fastc::JobDev;
+using namespace fastc::host;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+enum ReqState { kPending = 0, kRunning = 1, kDone = 2, kFailed = 3, kCancelled = 4 };
+
+struct Request {
+  uint64_t id = 0;
+  fastc_bc7_job job{};
+  fastc_bc7_settings settings{};
+  uint32_t first = 0, count = 0;  // raster block range
+  uint32_t row0 = 0;              // first texel row uploaded
+  size_t in_bytes = 0, out_bytes = 0;
+  ReqState state = kPending;
+  fastc_bc7_status status = FASTC_BC7_OK;
+  Clock::time_point t_submit, t_done;
+};
+
+struct Slot {
+  cudaStream_t stream = nullptr;
+  void *dev = nullptr;
+  uint8_t *pinned = nullptr;
+  size_t pinned_cap = 0;
+  size_t bytes = 0;  // budget held by the batch
+  std::vector<Request *> reqs;
+  std::vector<size_t> out_off;
+  bool busy = false;
+  bool finished = false;
+  cudaError_t error = cudaSuccess;
+};
+
+size_t round_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+struct fastc_bc7_server_s {
+  fastc_bc7_server_config cfg{};
+  int device = 0;
+  int engine = FASTC_BC7_ENGINE_PIPELINE;
+  std::mutex mu;
+  std::condition_variable cv_work;  // wakes the worker
+  std::condition_variable cv_done;  // wakes waiters
+  std::deque<Request *> pending;
+  std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
+  std::vector<Slot> slots;
+  uint64_t next_id = 1;
+  size_t in_use = 0, peak = 0;
+  bool stop = false;
+  std::thread worker;
+  // statistics
+  std::vector<double> latencies_ms;
+  uint64_t submitted = 0, completed = 0, failed = 0, cancelled = 0, rejected = 0, batches = 0;
+  uint64_t pixels = 0;
+  bool started = false;
+  Clock::time_point t_first;
+  Clock::time_point t_last;
+
+  // device bytes a batch needs, beyond the per-request texels and blocks
+  size_t batch_overhead(uint64_t blocks, size_t njobs) const {
+    return round_up(njobs * sizeof(JobDev)) + scratch_bytes(blocks, engine);
+  }
+
+  void loop();
+  void launch(Slot &s);
+  void retire(Slot &s);
+};
+
+namespace {
+
+void CUDART_CB on_batch_done(void *arg) {
+  auto *pair = static_cast<std::pair<fastc_bc7_server_s *, Slot *> *>(arg);
+  fastc_bc7_server_s *srv = pair->first;
+  Slot *s = pair->second;
+  delete pair;
+  std::lock_guard<std::mutex> lk(srv->mu);
+  s->finished = true;
+  srv->cv_work.notify_all();
+}
+
+}  // namespace
+
+void fastc_bc7_server_s::launch(Slot &s) {
+  // Called by the worker without the lock; s.reqs/out_off/bytes are set.
+  cudaError_t e = cudaSuccess;
+  uint64_t total = 0;
+  size_t in_total = 0, out_total = 0;
+  std::vector<size_t> in_off(s.reqs.size());
+  s.out_off.assign(s.reqs.size(), 0);
+  for (size_t i = 0; i < s.reqs.size(); i++) {
+    in_off[i] = in_total;
+    s.out_off[i] = out_total;
+    in_total += round_up(s.reqs[i]->in_bytes);
+    out_total += round_up(s.reqs[i]->out_bytes);
+    total += s.reqs[i]->count;
+  }
+  const size_t table = round_up(s.reqs.size() * sizeof(JobDev));
+  const size_t need = in_total + out_total + table + scratch_bytes(total, engine);
+  if (s.pinned_cap < out_total) {
+    if (s.pinned) cudaFreeHost(s.pinned);
+    s.pinned = nullptr;
+    s.pinned_cap = 0;
+    e = cudaMallocHost(reinterpret_cast<void **>(&s.pinned), out_total);
+    if (e == cudaSuccess) s.pinned_cap = out_total;
+  }
+  if (e == cudaSuccess) e = cudaMallocAsync(&s.dev, need, s.stream);
+  if (e == cudaSuccess) {
+    uint8_t *din = static_cast<uint8_t *>(s.dev);
+    uint8_t *dout = din + in_total;
+    JobDev *dtab = reinterpret_cast<JobDev *>(dout + out_total);
+    void *scratch = reinterpret_cast<uint8_t *>(dtab) + table;
+    std::vector<JobDev> dj(s.reqs.size());
+    uint64_t begin = 0;
+    for (size_t i = 0; i < s.reqs.size() && e == cudaSuccess; i++) {
+      Request &r = *s.reqs[i];
+      dj[i] = make_job(r.job, r.settings, r.first, r.count, begin);
+      dj[i].in = din + in_off[i];
+      dj[i].out = dout + s.out_off[i];
+      dj[i].row0 = r.row0;
+      dj[i].out_first = r.first;
+      dj[i].flags = fastc::kJobIn16 | fastc::kJobOut16;
+      begin += r.count;
+      const uint8_t *src = r.job.in + (size_t)r.row0 * r.job.width * 4;
+      e = cudaMemcpyAsync(din + in_off[i], src, r.in_bytes, cudaMemcpyHostToDevice, s.stream);
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dtab, dj.data(), dj.size() * sizeof(JobDev), cudaMemcpyHostToDevice,
+                          s.stream);
+    if (e == cudaSuccess) {
+      fastc::LaunchShape shape;
+      {
+        std::lock_guard<std::mutex> lk(g_mu);
+        shape = pick_shape(total);
+      }
+      e = (cudaError_t)launch_engine(dtab, (int)dj.size(), total, scratch, engine, shape, s.stream);
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s.pinned, dout, out_total, cudaMemcpyDeviceToHost, s.stream);
+    cudaFreeAsync(s.dev, s.stream);
+    s.dev = nullptr;
+  }
+  if (e == cudaSuccess) {
+    auto *arg = new std::pair<fastc_bc7_server_s *, Slot *>(this, &s);
+    e = cudaLaunchHostFunc(s.stream, on_batch_done, arg);
+    if (e != cudaSuccess) delete arg;
+  }
+  if (e != cudaSuccess) {
+    std::lock_guard<std::mutex> lk(mu);
+    s.error = e;
+    s.finished = true;
+  }
+}
+
+void fastc_bc7_server_s::retire(Slot &s) {
+  // Called by the worker without the lock, after the batch finished.
+  if (s.error == cudaSuccess) {
+    for (size_t i = 0; i < s.reqs.size(); i++) {
+      Request &r = *s.reqs[i];
+      std::memcpy(r.job.out + (size_t)r.first * 16, s.pinned + s.out_off[i], r.out_bytes);
+    }
+  }
+  const Clock::time_point now = Clock::now();
+  std::lock_guard<std::mutex> lk(mu);
+  for (Request *r : s.reqs) {
+    r->t_done = now;
+    if (s.error == cudaSuccess) {
+      r->state = kDone;
+      completed++;
+      pixels += (uint64_t)r->count * 16;
+      latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
+    } else {
+      r->state = kFailed;
+      r->status = fail_cuda(s.error);
+      failed++;
+    }
+  }
+  t_last = now;
+  in_use -= s.bytes;
+  s.bytes = 0;
+  s.reqs.clear();
+  s.busy = false;
+  s.finished = false;
+  s.error = cudaSuccess;
+  cv_done.notify_all();
+}
+
+void fastc_bc7_server_s::loop() {
+  cudaSetDevice(device);
+  std::unique_lock<std::mutex> lk(mu);
+  for (;;) {
+    // retire finished batches
+    for (Slot &s : slots) {
+      if (s.busy && s.finished) {
+        lk.unlock();
+        retire(s);
+        lk.lock();
+      }
+    }
+    // admit pending requests into a free slot
+    Slot *free_slot = nullptr;
+    for (Slot &s : slots)
+      if (!s.busy) {
+        free_slot = &s;
+        break;
+      }
+    if (free_slot && !pending.empty()) {
+      std::vector<Request *> batch;
+      uint64_t blocks = 0;
+      size_t data = 0;
+      while (!pending.empty() && batch.size() < cfg.max_batch_jobs) {
+        Request *r = pending.front();
+        const uint64_t nb = blocks + r->count;
+        const size_t nd = data + round_up(r->in_bytes) + round_up(r->out_bytes);
+        const size_t need = nd + batch_overhead(nb, batch.size() + 1);
+        if ((!batch.empty() && nb > cfg.max_batch_blocks) || in_use + need > cfg.memory_budget) break;
+        pending.pop_front();
+        r->state = kRunning;
+        batch.push_back(r);
+        blocks = nb;
+        data = nd;
+      }
+      if (!batch.empty()) {
+        free_slot->busy = true;
+        free_slot->finished = false;
+        free_slot->reqs = batch;
+        free_slot->bytes = data + batch_overhead(blocks, batch.size());
+        in_use += free_slot->bytes;
+        peak = std::max(peak, in_use);
+        batches++;
+        lk.unlock();
+        launch(*free_slot);
+        lk.lock();
+        continue;
+      }
+    }
+    bool busy = false;
+    for (Slot &s : slots) busy = busy || s.busy;
+    if (stop && pending.empty() && !busy) break;
+    cv_work.wait(lk);
+  }
+}
+
+extern "C" {
+
+void fastc_bc7_server_config_default(fastc_bc7_server_config *c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->memory_budget = (size_t)8 << 30;
+  c->max_inflight = 3;
+  c->max_batch_blocks = 1u << 22;
+  c->max_batch_jobs = 4096;
+}
+
+fastc_bc7_status fastc_bc7_server_create(const fastc_bc7_server_config *cfg,
+                                         fastc_bc7_server *out) {
+  if (!out) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  fastc_bc7_server_config c;
+  fastc_bc7_server_config_default(&c);
+  if (cfg) c = *cfg;
+  if (c.max_inflight == 0 || c.max_inflight > 16 || c.max_batch_jobs == 0 || c.memory_budget == 0)
+    return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  const int dev = current_device();
+  if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    fastc::upload_tables(dev);
+  }
+  auto *s = new fastc_bc7_server_s();
+  s->cfg = c;
+  s->device = dev;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    s->engine = g_engine;
+  }
+  s->slots.resize(c.max_inflight);
+  for (Slot &sl : s->slots) {
+    const cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      for (Slot &x : s->slots)
+        if (x.stream) cudaStreamDestroy(x.stream);
+      delete s;
+      return fail_cuda(e);
+    }
+  }
+  s->worker = std::thread([s] { s->loop(); });
+  *out = s;
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_server_submit(fastc_bc7_server s, const fastc_bc7_job *job,
+                                         const fastc_bc7_settings *settings, uint64_t *id) {
+  if (!s || !job || !id) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  fastc_bc7_settings st;
+  fastc_bc7_settings_default(&st);
+  if (settings) st = *settings;
+  fastc_bc7_status why;
+  if (!settings_ok(st, &why)) return why;
+  if (st.watermark_start == FASTC_BC7_WATERMARK_CONTINUE) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  uint32_t first, count;
+  if (!job->in || !job->out || !job_range(*job, &first, &count)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  auto r = std::make_unique<Request>();
+  r->job = *job;
+  r->settings = st;
+  r->first = first;
+  r->count = count;
+  const uint32_t bw = job->width / 4;
+  const uint32_t r0 = count ? first / bw : 0, r1 = count ? (first + count - 1) / bw : 0;
+  r->row0 = r0 * 4;
+  r->in_bytes = count ? (size_t)(r1 - r0 + 1) * 4 * job->width * 4 : 0;
+  r->out_bytes = (size_t)count * 16;
+  r->t_submit = Clock::now();
+  std::lock_guard<std::mutex> lk(s->mu);
+  const size_t alone = round_up(r->in_bytes) + round_up(r->out_bytes) + s->batch_overhead(count, 1);
+  s->submitted++;
+  if (!s->started) {
+    s->started = true;
+    s->t_first = r->t_submit;
+  }
+  r->id = s->next_id++;
+  *id = r->id;
+  if (alone > s->cfg.memory_budget) {
+    r->state = kFailed;
+    r->status = FASTC_BC7_ERR_BUDGET;
+    s->rejected++;
+    s->reqs.emplace(r->id, std::move(r));
+    return FASTC_BC7_ERR_BUDGET;
+  }
+  if (count == 0) {
+    r->state = kDone;
+    r->t_done = r->t_submit;
+    s->completed++;
+    s->reqs.emplace(r->id, std::move(r));
+    s->cv_done.notify_all();
+    return FASTC_BC7_OK;
+  }
+  s->pending.push_back(r.get());
+  s->reqs.emplace(r->id, std::move(r));
+  s->cv_work.notify_all();
+  return FASTC_BC7_OK;
+}
+
+static fastc_bc7_status state_status(const Request &r) {
+  switch (r.state) {
+    case kDone: return FASTC_BC7_OK;
+    case kFailed: return r.status;
+    case kCancelled: return FASTC_BC7_ERR_CANCELLED;
+    default: return FASTC_BC7_ERR_TIMEOUT;
+  }
+}
+
+fastc_bc7_status fastc_bc7_server_poll(fastc_bc7_server s, uint64_t id) {
+  if (!s) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return FASTC_BC7_ERR_NOT_FOUND;
+  return state_status(*it->second);
+}
+
+fastc_bc7_status fastc_bc7_server_wait(fastc_bc7_server s, uint64_t id, int64_t timeout_ms) {
+  if (!s) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return FASTC_BC7_ERR_NOT_FOUND;
+  Request *r = it->second.get();
+  auto finished = [r] { return r->state == kDone || r->state == kFailed || r->state == kCancelled; };
+  if (timeout_ms < 0) {
+    s->cv_done.wait(lk, finished);
+  } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), finished)) {
+    return FASTC_BC7_ERR_TIMEOUT;
+  }
+  return state_status(*r);
+}
+
+fastc_bc7_status fastc_bc7_server_cancel(fastc_bc7_server s, uint64_t id) {
+  if (!s) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return FASTC_BC7_ERR_NOT_FOUND;
+  Request *r = it->second.get();
+  if (r->state == kRunning) return FASTC_BC7_ERR_INVALID_ARGUMENT;  // already on the GPU
+  if (r->state != kPending) return state_status(*r);
+  s->pending.erase(std::find(s->pending.begin(), s->pending.end(), r));
+  r->state = kCancelled;
+  r->t_done = Clock::now();
+  s->cancelled++;
+  s->cv_done.notify_all();
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_server_release(fastc_bc7_server s, uint64_t id) {
+  if (!s) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return FASTC_BC7_ERR_NOT_FOUND;
+  const ReqState st = it->second->state;
+  if (st == kPending || st == kRunning) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  s->reqs.erase(it);
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_server_get_stats(fastc_bc7_server s, fastc_bc7_server_stats *out) {
+  if (!s || !out) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  std::memset(out, 0, sizeof(*out));
+  out->submitted = s->submitted;
+  out->completed = s->completed;
+  out->failed = s->failed;
+  out->cancelled = s->cancelled;
+  out->rejected = s->rejected;
+  out->batches = s->batches;
+  out->pixels_completed = s->pixels;
+  out->bytes_in_use = s->in_use;
+  out->peak_bytes = s->peak;
+  std::vector<double> l = s->latencies_ms;
+  if (!l.empty()) {
+    std::sort(l.begin(), l.end());
+    auto pct = [&l](double q) {
+      const size_t i = (size_t)std::min<double>((double)(l.size() - 1), q * (double)(l.size() - 1) + 0.5);
+      return l[i];
+    };
+    out->p50_latency_ms = pct(0.50);
+    out->p99_latency_ms = pct(0.99);
+    out->max_latency_ms = l.back();
+    double sum = 0;
+    for (double v : l) sum += v;
+    out->mean_latency_ms = sum / (double)l.size();
+  }
+  if (s->started && s->completed) {
+    const double secs = std::chrono::duration<double>(s->t_last - s->t_first).count();
+    out->mpix_per_s = secs > 0 ? (double)s->pixels / secs / 1e6 : 0.0;
+  }
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_server_destroy(fastc_bc7_server s) {
+  if (!s) return FASTC_BC7_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    s->cv_work.notify_all();
+  }
+  if (s->worker.joinable()) s->worker.join();
+  for (Slot &sl : s->slots) {
+    if (sl.stream) {
+      cudaStreamSynchronize(sl.stream);
+      cudaStreamDestroy(sl.stream);
+    }
+    if (sl.pinned) cudaFreeHost(sl.pinned);
+  }
+  delete s;
+  return FASTC_BC7_OK;
+}
+
+}  // extern "C"

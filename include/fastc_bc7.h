@@ -184,6 +184,51 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_flags(fastc_bc7_plan plan, uint32_
 FASTC_BC7_API uint64_t fastc_bc7_plan_blocks(fastc_bc7_plan plan);
 FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_destroy(fastc_bc7_plan plan);
 
+/* --- Request server: continuous batching under a device-memory budget. ---
+ * A worker thread admits queued requests (host buffers, kept alive by the
+ * caller until the request finishes) into up to max_inflight concurrent
+ * batches, as budget and slots free up; each batch is one encoder launch on
+ * its own stream. A request's blocks are the same alone or in any mix. */
+typedef struct fastc_bc7_server_s *fastc_bc7_server;
+
+typedef struct {
+  size_t memory_budget;      /* device bytes for texels, blocks and scratch (8 GiB) */
+  uint32_t max_inflight;     /* batches on the GPU at once (3) */
+  uint32_t max_batch_blocks; /* blocks per batch (4 Mi) */
+  uint32_t max_batch_jobs;   /* requests per batch (4096) */
+  uint32_t reserved;
+} fastc_bc7_server_config;
+
+typedef struct {
+  uint64_t submitted, completed, failed, cancelled, rejected, batches;
+  uint64_t pixels_completed;
+  size_t bytes_in_use, peak_bytes;
+  double p50_latency_ms, p99_latency_ms, mean_latency_ms, max_latency_ms;
+  double mpix_per_s; /* texels completed / time from first submit to last completion */
+} fastc_bc7_server_stats;
+
+FASTC_BC7_API void fastc_bc7_server_config_default(fastc_bc7_server_config *cfg);
+FASTC_BC7_API fastc_bc7_status fastc_bc7_server_create(const fastc_bc7_server_config *cfg,
+                                                       fastc_bc7_server *out);
+/* Queue one job (host buffers). FASTC_BC7_ERR_BUDGET when the request alone
+ * exceeds the budget. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_server_submit(fastc_bc7_server s, const fastc_bc7_job *job,
+                                                       const fastc_bc7_settings *settings,
+                                                       uint64_t *request_id);
+/* OK when finished, TIMEOUT while queued or running, else the failure. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_server_poll(fastc_bc7_server s, uint64_t request_id);
+/* Wait up to timeout_ms (negative: forever). */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_server_wait(fastc_bc7_server s, uint64_t request_id,
+                                                     int64_t timeout_ms);
+/* Cancel a request that is still queued. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_server_cancel(fastc_bc7_server s, uint64_t request_id);
+/* Forget a finished request. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_server_release(fastc_bc7_server s, uint64_t request_id);
+FASTC_BC7_API fastc_bc7_status fastc_bc7_server_get_stats(fastc_bc7_server s,
+                                                          fastc_bc7_server_stats *out);
+/* Finish queued and running work, then free the server. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_server_destroy(fastc_bc7_server s);
+
 /* Encoder organisation. PIPELINE (default): a per-block select stage, one
  * thread per cluster fit for the fit and the annealing (warps run 32 fits of
  * one mode, refilled from a queue), a per-block pack stage. WARP_PER_BLOCK:

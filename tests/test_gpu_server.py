@@ -1,0 +1,125 @@
+"""The continuous-batching request server on the GPU: results are the same
+alone and in a concurrent mix, the memory budget is enforced, queued
+requests can be cancelled, statistics add up."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from conftest import make_image
+
+pytestmark = pytest.mark.gpu
+
+
+def settings(q, seed=11):
+    from fastc_gb300 import CompressionSettings
+
+    return CompressionSettings(num_simulated_annealing_steps=q, seed=seed)
+
+
+def test_alone_equals_in_the_mix(gpu, port):
+    from fastc_gb300.serve import Server
+
+    rng = np.random.default_rng(3)
+    reqs = []
+    for i in range(24):
+        w, h = (int(x) for x in 4 * rng.integers(2, 40, 2))
+        q = int(rng.choice([0, 16, 50], p=[0.3, 0.4, 0.3]))
+        reqs.append((make_image(f"tile_mix({400 + i}, {w}, {h})"), q))
+    alone = []
+    with Server(max_inflight=1) as srv:
+        for img, q in reqs:
+            alone.append(srv.wait(srv.submit(img, settings(q))).copy())
+    with Server(max_inflight=3, max_batch_blocks=2048) as srv:
+        # submitted from several threads while earlier batches run
+        handles = [None] * len(reqs)
+
+        def worker(k):
+            for i in range(k, len(reqs), 4):
+                handles[i] = srv.submit(reqs[i][0], settings(reqs[i][1]))
+                time.sleep(0.001 * (i % 3))
+
+        ts = [threading.Thread(target=worker, args=(k,)) for k in range(4)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        mixed = [srv.wait(hd) for hd in handles]
+        st = srv.stats()
+    for (img, q), a, m in zip(reqs, alone, mixed):
+        assert np.array_equal(a, m)
+    # and the same bytes as the oracle
+    img, q = reqs[5]
+    assert np.array_equal(alone[5], port.compress(img, steps=q, seed=11))
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["batches"] >= 2
+    assert st["p99_latency_ms"] >= st["p50_latency_ms"] > 0
+    assert st["pixels_completed"] == sum(im.shape[0] * im.shape[1] for im, _ in reqs)
+
+
+def test_budget_rejects_oversized_and_queues_the_rest(gpu):
+    from fastc_gb300 import BC7Error
+    from fastc_gb300.serve import Server
+
+    small = make_image("tile_mix(7, 64, 64)")
+    big = make_image("tile_mix(8, 1024, 1024)")
+    with Server(memory_budget=96 << 20, max_inflight=2) as srv:
+        with pytest.raises(BC7Error) as e:
+            srv.submit(big, settings(0))
+        assert e.value.status == 5
+        hs = [srv.submit(small, settings(16)) for _ in range(8)]
+        outs = [srv.wait(h) for h in hs]
+        st = srv.stats()
+    assert all(np.array_equal(outs[0], o) for o in outs)
+    assert st["rejected"] == 1 and st["completed"] == 8
+    assert st["peak_bytes"] <= 96 << 20
+
+
+def test_cancel_queued_request(gpu):
+    from fastc_gb300 import BC7Error
+    from fastc_gb300.serve import Server
+
+    imgs = [make_image(f"tile_mix({20 + i}, 256, 256)") for i in range(6)]
+    with Server(max_inflight=1, max_batch_jobs=1) as srv:
+        hs = [srv.submit(im, settings(50)) for im in imgs]
+        cancelled = 0
+        for h in hs[2:]:
+            try:
+                srv.cancel(h)
+                cancelled += 1
+            except BC7Error:
+                pass
+        for h in hs[:2]:
+            srv.wait(h)
+        for h in hs[2:]:
+            try:
+                srv.wait(h, timeout_ms=60000)
+            except BC7Error as e:
+                assert e.status == 8
+        st = srv.stats()
+    assert cancelled >= 1
+    assert st["cancelled"] == cancelled
+    assert st["completed"] + st["cancelled"] == len(imgs)
+
+
+def test_wait_timeout_and_poll(gpu):
+    from fastc_gb300 import BC7Error
+    from fastc_gb300.serve import Server
+
+    img = make_image("tile_mix(31, 512, 512)")
+    with Server(max_inflight=1) as srv:
+        h = srv.submit(img, settings(50))
+        try:
+            srv.wait(h, timeout_ms=0)
+            finished_early = True
+        except BC7Error as e:
+            assert e.status == 6
+            finished_early = False
+        srv.wait(h)
+        assert srv.poll(h)
+        srv.release(h)
+        with pytest.raises(BC7Error) as e:
+            srv.poll(h)
+        assert e.value.status == 7
+    assert finished_early in (True, False)
