@@ -126,6 +126,7 @@ struct ModeCtx {
   int idx_mode;  // m_IndexMode
   uint32_t lcg;  // this fit's annealing stream
   uint32_t *status;
+  const uint32_t *sct;  // single_color_table() results, or nullptr to search
 };
 
 // kErrorMetrics (CP:205-208)
@@ -525,51 +526,72 @@ __device__ inline void clamp_to_grid(const ModeCtx &m, float *p1, float *p2, uin
   }
 }
 
+// The per-channel search of CompressSingleColor (CP:262-336): the first
+// (i, j) pair, in row-major order, whose interpolant at index 1 lands
+// closest to `val`, with FasTC's early exit on an exact hit. The result
+// depends only on (val, channel bits, p-bits of the two endpoints, index
+// bits): byte 0 = low endpoint, byte 1 = high endpoint, bits 16+ = distance.
+__host__ __device__ inline uint32_t single_channel_search(uint32_t val, int nbits, int havepbit,
+                                                          int pl, int ph, int ib) {
+  const int nposs = 1 << nbits;
+  const int eb = havepbit ? nbits + 1 : nbits;
+  const uint32_t w1 = weight1(ib, 1), w0 = 64u - w1;
+  uint32_t bestd = 0xFF, bi = 0xFFFFFFFFu, bj = 0xFFFFFFFFu;
+  for (int i = 0; bestd > 0 && i < nposs; i++) {
+    int vl = i;
+    if (havepbit) vl = (vl << 1) | pl;
+    uint32_t v1 = (uint32_t)(vl << (8 - eb));
+    v1 |= v1 >> eb;
+    for (int j = 0; bestd > 0 && j < nposs; j++) {
+      int vh = j;
+      if (havepbit) vh = (vh << 1) | ph;
+      uint32_t v2 = (uint32_t)(vh << (8 - eb));
+      v2 |= v2 >> eb;
+      const uint32_t cmb = (w0 * v1 + w1 * v2 + 32u) >> 6;
+      const uint32_t d = cmb > val ? cmb - val : val - cmb;
+      if (d < bestd) {
+        bestd = d;
+        bi = v1;
+        bj = v2;
+      }
+    }
+  }
+  return (bi & 0xFF) | ((bj & 0xFF) << 8) | (bestd << 16);
+}
+
+// Index of a single-colour table row: channel bits 1..8, p-bit variant
+// (0: none, 1 + pl + 2 ph), index bits 2..4.
+__host__ __device__ constexpr int sct_row(int nbits, int pvar, int ib) {
+  return ((nbits - 1) * 5 + pvar) * 3 + (ib - 2);
+}
+constexpr int kSctRows = 8 * 5 * 3;
+
 // CompressSingleColor (CP:252-353)
 __device__ inline float single_color(const ModeCtx &m, const float *p, float *p1, float *p2,
-                              uint32_t &best_pbit) {
+                                     uint32_t &best_pbit) {
   const uint32_t pixel = to_pixel(p, 0xFFFFFFFFu, -1);
   float best_err = FLT_MAX;
   const int nc = num_pbit_combos(m.a);
   const bool havepbit = m.a.pbit != kPBitNone;
   const int ib = bits_index(m, -1);
-  const uint32_t w1 = weight1(ib, 1), w0 = 64u - w1;
   for (int pbi = 0; pbi < nc; pbi++) {
     const int combo = pbit_combo(m.a, pbi);
     uint32_t dist[4] = {0, 0, 0, 0};
-    uint32_t bi[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
-    uint32_t bj[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    uint32_t bi[4], bj[4];
     for (int ci = 0; ci < 4; ci++) {
       const uint32_t val = (pixel >> (ci * 8)) & 0xFF;
-      int nbits = ci == 3 ? m.a.alpha_bits : m.a.color_bits;
+      const int nbits = ci == 3 ? m.a.alpha_bits : m.a.color_bits;
       if (nbits == 0) {
         bi[ci] = bj[ci] = 0xFF;
         dist[ci] = max(dist[ci], 0xFFu - val);
         continue;
       }
-      const int nposs = 1 << nbits;
-      if (havepbit) nbits++;
-      uint32_t bestd = 0xFF;
-      for (int i = 0; bestd > 0 && i < nposs; i++) {
-        int vl = i;
-        if (havepbit) vl = (vl << 1) | pb_first(combo);
-        uint32_t v1 = (uint32_t)(vl << (8 - nbits));
-        v1 |= v1 >> nbits;
-        for (int j = 0; bestd > 0 && j < nposs; j++) {
-          int vh = j;
-          if (havepbit) vh = (vh << 1) | pb_second(combo);
-          uint32_t v2 = (uint32_t)(vh << (8 - nbits));
-          v2 |= v2 >> nbits;
-          const uint32_t cmb = (w0 * v1 + w1 * v2 + 32u) >> 6;
-          const uint32_t e = cmb > val ? cmb - val : val - cmb;
-          if (e < bestd) {
-            bestd = e;
-            bi[ci] = v1;
-            bj[ci] = v2;
-          }
-        }
-      }
-      dist[ci] = max(bestd, dist[ci]);
+      const int pl = pb_first(combo), ph = pb_second(combo);
+      const uint32_t r = m.sct ? m.sct[sct_row(nbits, havepbit ? 1 + pl + 2 * ph : 0, ib) * 256 + val]
+                               : single_channel_search(val, nbits, havepbit, pl, ph, ib);
+      bi[ci] = r & 0xFF;
+      bj[ci] = (r >> 8) & 0xFF;
+      dist[ci] = max(r >> 16, dist[ci]);
     }
     float err = 0.0f;
     for (int i = 0; i < 4; i++) {

@@ -8,14 +8,18 @@
 //                   from 128-bit loads): trivial blocks, the 64+64 shape
 //                   estimate of BoxSelection, and the number of cluster fits
 //                   each BC7 mode needs.
-//   count scan      exclusive scan of those counts, mode-major, so all fits
-//                   of one mode are contiguous in the task arrays.
+//   count scan      exclusive scan of those counts, class-major (a class is
+//                   a mode and colour index width), so all fits of one class
+//                   are contiguous in the task arrays.
 //   emit_kernel     one thread per block writes its task descriptors.
 //   setup_kernel    one thread per cluster fit: PCA, k-means, least squares,
-//                   grid clamp, first QuantizedError (CP:921-1094, 632-919).
-//   anneal_kernel   persistent; one thread per fit with refill from a queue:
-//                   the simulated annealing (CP:538-630) in exact integer
-//                   arithmetic, specialised per mode.
+//                   grid clamp, first QuantizedError (CP:921-1094, 632-919);
+//                   fits with annealing work go to their class's list.
+//   anneal_kernel   one persistent launch per class; one thread per fit,
+//                   refilled from the class list: the simulated annealing
+//                   (CP:538-630) on integer endpoints, with the error loop
+//                   on packed bytes (dp2a projection, a per-step palette of
+//                   interpolated colours, vabsdiff4 + dp4a squared error).
 //   pack_kernel     one thread per block: FasTC's arg-min over modes and the
 //                   128-bit packing (CP:1752-1817, 1096-1298).
 //
@@ -44,6 +48,16 @@ __constant__ uint32_t q_opt6[256];
 // QuantizeChannel (RGBAEndpoints.cpp:126-165) tabulated for masks of the top
 // `prec` bits, prec = 1..8, and p-bit -1/0/1: [prec-1][pbit+1][value].
 __constant__ uint8_t q_qlut[8][3][256];
+// single_channel_search() for every row and value, built once per device.
+__device__ uint32_t g_sct[kSctRows * 256];
+
+__global__ void build_sct_kernel() {
+  const int row = blockIdx.x, val = threadIdx.x;
+  const int ib = row % 3 + 2, pvar = (row / 3) % 5, nbits = row / 15 + 1;
+  const int havepbit = pvar != 0;
+  const int pl = havepbit ? (pvar - 1) & 1 : 0, ph = havepbit ? (pvar - 1) >> 1 : 0;
+  g_sct[row * 256 + val] = single_channel_search((uint32_t)val, nbits, havepbit, pl, ph, ib);
+}
 
 // ---------------------------------------------------------------------------
 // Host-side table construction
@@ -83,6 +97,8 @@ void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t
   cudaMemcpyToSymbol(q_qlut, lut, sizeof(lut));
   cudaMemcpyToSymbol(q_opt7, opt7, 256 * sizeof(uint32_t));
   cudaMemcpyToSymbol(q_opt6, opt6, 256 * sizeof(uint32_t));
+  build_sct_kernel<<<kSctRows, 256>>>();
+  cudaDeviceSynchronize();
   done[device] = true;
 }
 
@@ -134,8 +150,9 @@ __device__ __forceinline__ Selection sel_of(const BlockSel &b) {
   return s;
 }
 
-// Number of cluster fits CompressClusters (CP:1752-1817) runs for `mode`.
-__device__ __forceinline__ int mode_task_count(const Selection &sel, uint32_t modes, int mode) {
+// Number of cluster fits CompressClusters (CP:1752-1817) runs for class c.
+__device__ __forceinline__ int class_task_count(const Selection &sel, uint32_t modes, int c) {
+  const int mode = class_mode(c);
   if (!(modes & (1u << mode))) return 0;
   const ModeAttr a = mode_attr(mode);
   const uint32_t nshapes = sel.nshapes < 5 ? sel.nshapes : 5;
@@ -143,29 +160,26 @@ __device__ __forceinline__ int mode_task_count(const Selection &sel, uint32_t mo
   for (uint32_t s = 0; s < nshapes; s++) {
     if (a.subsets != 1 && (uint32_t)a.subsets != sel.nparts[s]) continue;
     if (sel.shape[s] >= 16 && mode == 0) continue;
-    n += a.has_rotation ? (mode == 4 ? 8 : 4) : a.subsets;
+    n += a.has_rotation ? 4 : a.subsets;
   }
   return n;
 }
 
-// The i-th fit of `mode`, in CompressClusters' order.
-__device__ __forceinline__ Task mode_task(const Selection &sel, int mode, int i) {
+// The i-th fit of class c: shape slot, then subset (or rotation), in
+// CompressClusters' order.
+__device__ __forceinline__ Task class_task(const Selection &sel, int c, int i) {
+  const int mode = class_mode(c);
   const ModeAttr a = mode_attr(mode);
   const uint32_t nshapes = sel.nshapes < 5 ? sel.nshapes : 5;
-  const int nim = mode == 4 ? 2 : 1;
-  Task t{mode, 0, 0, 0, 0};
+  Task t{mode, 0, 0, 0, class_im(c)};
   for (uint32_t s = 0; s < nshapes; s++) {
     if (a.subsets != 1 && (uint32_t)a.subsets != sel.nparts[s]) continue;
     if (sel.shape[s] >= 16 && mode == 0) continue;
-    const int per = a.has_rotation ? 4 * nim : a.subsets;
+    const int per = a.has_rotation ? 4 : a.subsets;
     if (i < per) {
       t.slot = (int)s;
-      if (a.has_rotation) {
-        t.rot = i / nim;
-        t.im = i % nim;
-      } else {
-        t.subset = i;
-      }
+      if (a.has_rotation) t.rot = i;
+      else t.subset = i;
       return t;
     }
     i -= per;
@@ -228,7 +242,7 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
     bs.done = 1;
     bs.pad[0] = bs.pad[1] = bs.pad[2] = 0;
     if (same || transparent) {
-      if (lane < 8) counts[(uint64_t)lane * nb + gl] = 0;
+      if (lane < kClasses) counts[(uint64_t)lane * nb + gl] = 0;
       if (lane == 0) {
         uint32_t out[4];
         if (same) {
@@ -251,12 +265,12 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
     const Selection s = box_selection_warp(px, s_part2, s_part3, (int)jb.metric, lane);
     uint32_t modes = s.modes & jb.modes;
     if (modes == 0) modes = jb.modes & 0xFF;  // FasTC: undefined behaviour
-    const int c = lane < 8 ? mode_task_count(s, modes, lane) : 0;
+    const int c = lane < kClasses ? class_task_count(s, modes, lane) : 0;
     int total = c;
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) total += __shfl_xor_sync(0xFFFFFFFFu, total, o);
     const bool overflow = total > kMaxBlockTasks;  // not reachable with BC7's mode table
-    if (lane < 8) counts[(uint64_t)lane * nb + gl] = overflow ? 0 : (uint8_t)c;
+    if (lane < kClasses) counts[(uint64_t)lane * nb + gl] = overflow ? 0 : (uint8_t)c;
     if (lane == 0) {
       bs.shape0 = (uint8_t)s.shape[0];
       bs.shape1 = (uint8_t)s.shape[1];
@@ -341,10 +355,11 @@ __global__ void __launch_bounds__(1024) scan_chunks_kernel(uint32_t *chunk, uint
     if (threadIdx.x == 1023) s_carry = carry + s_warp[wid] + incl;
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    ctr->tasks = s_carry;
-    ctr->anneal_next = 0ull;
+  if (threadIdx.x < kClasses) {
+    ctr->anneal_next[threadIdx.x] = 0ull;
+    ctr->anneal_count[threadIdx.x] = 0u;
   }
+  if (threadIdx.x == 0) ctr->tasks = s_carry;
 }
 
 // ---------------------------------------------------------------------------
@@ -356,12 +371,12 @@ __global__ void emit_kernel(uint32_t nb, const uint8_t *__restrict__ counts,
                             uint2 *__restrict__ desc) {
   const uint32_t gl = blockIdx.x * blockDim.x + threadIdx.x;
   if (gl >= nb) return;
-  for (int m = 0; m < 8; m++) {
-    const uint64_t i = (uint64_t)m * nb + gl;
+  for (int cl = 0; cl < kClasses; cl++) {
+    const uint64_t i = (uint64_t)cl * nb + gl;
     const uint32_t c = counts[i];
     if (!c) continue;
     const uint32_t base = scanned(local, chunk, i);
-    for (uint32_t k = 0; k < c; k++) desc[base + k] = make_uint2(gl, (uint32_t)m | (k << 8));
+    for (uint32_t k = 0; k < c; k++) desc[base + k] = make_uint2(gl, (uint32_t)cl | (k << 8));
   }
 }
 
@@ -372,9 +387,10 @@ __global__ void emit_kernel(uint32_t nb, const uint8_t *__restrict__ counts,
 constexpr int kSetupThreads = 128;
 
 __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
-    const JobDev *__restrict__ jobs, const BlockSel *__restrict__ sel,
-    const uint2 *__restrict__ desc, const PipelineCounters *__restrict__ ctr,
-    TaskState *__restrict__ state, uint32_t *status) {
+    const JobDev *__restrict__ jobs, uint32_t nb, const BlockSel *__restrict__ sel,
+    const uint2 *__restrict__ desc, const uint16_t *__restrict__ local,
+    const uint32_t *__restrict__ chunk, PipelineCounters *__restrict__ ctr,
+    TaskState *__restrict__ state, uint32_t *__restrict__ alist, uint32_t *status) {
   __shared__ uint32_t s_px[kSetupThreads * 17];
   uint32_t *px = s_px + threadIdx.x * 17;
   const uint32_t ntasks = ctr->tasks;
@@ -382,11 +398,12 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
        t += gridDim.x * blockDim.x) {
     const uint2 d = desc[t];
     const uint32_t gl = d.x;
-    const int mode = (int)(d.y & 0xFF), i = (int)(d.y >> 8);
+    const int cls = (int)(d.y & 0xFF), i = (int)(d.y >> 8);
+    const int mode = class_mode(cls);
     const BlockSel bs = sel[gl];
     const JobDev &jb = jobs[bs.job];
     const Selection s = sel_of(bs);
-    const Task tk = mode_task(s, mode, i);
+    const Task tk = class_task(s, cls, i);
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       const uint4 v = load_row_p(jb, bs.lin, r);
@@ -406,6 +423,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     m.idx_mode = tk.im;
     m.status = status;
     m.lcg = 0;
+    m.sct = g_sct;
     Cluster c;
     make_cluster(px, part_word_of(s, mode, tk.slot), tk.subset, c);
     FitSetup st;
@@ -435,158 +453,43 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     o.pbit = (uint8_t)st.pbit;
     o.flags = (uint8_t)((st.anneal ? kTaskAnneal : 0u) | (jb.metric ? kTaskNonuniform : 0u));
     state[t] = o;
+    if (st.anneal) {
+      // append to the class's annealing list (warp-aggregated per class)
+      const uint32_t peers = __match_any_sync(__activemask(), cls);
+      const int leader = __ffs(peers) - 1;
+      const int lane = threadIdx.x & 31;
+      uint32_t pos = 0;
+      if (lane == leader) pos = atomicAdd(&ctr->anneal_count[cls], (uint32_t)__popc(peers));
+      pos = __shfl_sync(peers, pos, leader) + __popc(peers & ((1u << lane) - 1u));
+      alist[scanned(local, chunk, (uint64_t)cls * nb) + pos] = t;
+    }
   }
 }
 
 // ---------------------------------------------------------------------------
-// anneal: persistent, one thread per fit, refilled from the task array
+// anneal: one launch per class, persistent, one thread per fit, refilled
+// from the class's list
 // ---------------------------------------------------------------------------
 
 constexpr int kAnnealThreads = 128;
 
-struct AnnealLane {
-  uint32_t t;        // task
-  uint32_t p1, p2;   // current endpoints (bytes)
-  uint32_t b1, b2;   // best endpoints
-  uint32_t lcg;
-  float cur_err, best_err;
-  uint64_t idx;      // best indices (texel nibbles)
-  uint64_t tex;      // texel index of point k, 4 bits each
-  int cur_pbit, best_pbit;
-  int energy, steps, n, kind;
-  float w[4];        // rotated metric weights (nonuniform metric only)
-};
-
-// Weight of a `bits`-bit index, templated so the divisor is a constant.
+// Weight of a `kBits`-bit index (constant divisor).
 template <int kBits>
-__device__ __forceinline__ int wt(int j) {
-  return (int)((64u * (uint32_t)j + (uint32_t)(((1 << kBits) - 1) / 2)) / (uint32_t)((1 << kBits) - 1));
+__device__ __forceinline__ uint32_t wt(int j) {
+  return (64u * (uint32_t)j + (uint32_t)(((1 << kBits) - 1) / 2)) / (uint32_t)((1 << kBits) - 1);
 }
 
-// QuantizedError (RGBAEndpoints.cpp:190-310) for integer endpoints and
-// points. The projection index floor(D k / L) is computed exactly with
-// integers; only when D k is a multiple of L does FasTC's float rounding
-// matter, and that case repeats FasTC's float division and product.
-template <int kBits, bool kRot, bool kUniform>
-__device__ __forceinline__ float qe_int(const uint32_t *pts, const uint32_t *proj, int stride, int n,
-                                        uint32_t q1, uint32_t q2, const float *w, bool want_idx,
-                                        uint64_t tex, uint64_t &idx) {
-  constexpr int nb = 1 << kBits;
-  constexpr int km = nb - 1;
-  int u1[4], u2[4], dir[4];
-#pragma unroll
-  for (int c = 0; c < 4; c++) {
-    u1[c] = (int)((q1 >> (8 * c)) & 0xFF);
-    u2[c] = (int)((q2 >> (8 * c)) & 0xFF);
-    dir[c] = u2[c] - u1[c];
-  }
-  const int L = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2] + dir[3] * dir[3];
-  int itotal = 0;
-  float ftotal = 0.0f;
-  if (L == 0) {
-    for (int k = 0; k < n; k++) {
-      const uint32_t e = pts[k * stride];
-      if (kUniform) {
-        int s = 0;
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const int d = (int)((e >> (8 * c)) & 0xFF) - u1[c];
-          s += d * d;
-        }
-        itotal += s;
-      } else {
-        float ev[4];
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const int d = (int)((e >> (8 * c)) & 0xFF) - u1[c];
-          ev[c] = __fmul_rn((float)(d < 0 ? -d : d), w[c]);
-        }
-        ftotal = __fadd_rn(ftotal, dot4(ev, ev));
-      }
-      if (want_idx) set_nib(idx, (int)((tex >> (4 * k)) & 15), 0);
-    }
-    return kUniform ? (float)itotal : ftotal;
-  }
-  const float rl = __frcp_rn((float)L);
-  for (int k = 0; k < n; k++) {
-    const uint32_t e = pts[k * stride];
-    const uint32_t p = kRot ? proj[k * stride] : e;
-    int D = 0;
-#pragma unroll
-    for (int c = 0; c < 4; c++) D += ((int)((p >> (8 * c)) & 0xFF) - u1[c]) * dir[c];
-    const int num = D * km;
-    int j = __float2int_rd(__fmul_rn((float)num, rl));
-    int r = num - j * L;
-    if (r < 0) {
-      j--;
-      r += L;
-    } else if (r >= L) {
-      j++;
-      r -= L;
-    }
-    int j1 = j, j2 = j + 1;
-    if (r == 0) {
-      const float sc = __fmul_rn(__fdiv_rn((float)D, (float)L), (float)km);
-      j1 = __float2int_rz(floorf(sc));
-      j2 = __float2int_rz(ceilf(sc));
-    }
-    j1 = min(max(0, j1), nb - 1);
-    j2 = min(j2, nb - 1);
-    int ec[4];
-#pragma unroll
-    for (int c = 0; c < 4; c++) ec[c] = (int)((e >> (8 * c)) & 0xFF);
-    const int w1a = wt<kBits>(j1), w0a = 64 - w1a;
-    if (kUniform) {
-      int e1 = 0;
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const int d = ec[c] - ((u1[c] * w0a + u2[c] * w1a + 32) >> 6);
-        e1 += d * d;
-      }
-      int best = e1, bj = j1;
-      if (j2 > j1) {
-        const int w1b = wt<kBits>(j1 + 1), w0b = 64 - w1b;
-        int e2 = 0;
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const int d = ec[c] - ((u1[c] * w0b + u2[c] * w1b + 32) >> 6);
-          e2 += d * d;
-        }
-        if (e2 < e1) {
-          best = e2;
-          bj = j1 + 1;
-        }
-      }
-      itotal += best;
-      if (want_idx) set_nib(idx, (int)((tex >> (4 * k)) & 15), (uint32_t)bj);
-    } else {
-      float ev[4];
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const int d = ec[c] - ((u1[c] * w0a + u2[c] * w1a + 32) >> 6);
-        ev[c] = __fmul_rn((float)(d < 0 ? -d : d), w[c]);
-      }
-      const float e1 = dot4(ev, ev);
-      float best = e1;
-      int bj = j1;
-      if (j2 > j1) {
-        const int w1b = wt<kBits>(j1 + 1), w0b = 64 - w1b;
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const int d = ec[c] - ((u1[c] * w0b + u2[c] * w1b + 32) >> 6);
-          ev[c] = __fmul_rn((float)(d < 0 ? -d : d), w[c]);
-        }
-        const float e2 = dot4(ev, ev);
-        if (e2 < e1) {
-          best = e2;
-          bj = j1 + 1;
-        }
-      }
-      ftotal = __fadd_rn(ftotal, best);
-      if (want_idx) set_nib(idx, (int)((tex >> (4 * k)) & 15), (uint32_t)bj);
-    }
-  }
-  return kUniform ? (float)itotal : ftotal;
+// d = c + a.h0 * b.b0 + a.h1 * b.b1 (lo) / b.b2, b.b3 (hi); a signed 16-bit
+// pairs, b unsigned bytes.
+__device__ __forceinline__ int dp2a_lo(uint32_t a, uint32_t b, int c) {
+  int d;
+  asm("dp2a.lo.s32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ int dp2a_hi(uint32_t a, uint32_t b, int c) {
+  int d;
+  asm("dp2a.hi.s32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
 }
 
 // ToPixel (RGBAEndpoints.cpp:167-177) of integer endpoints through the table.
@@ -600,17 +503,131 @@ __device__ __forceinline__ uint32_t qpix(const uint8_t *lut, uint32_t v, int pbi
   return r | ((uint32_t)la[v >> 24] << 24);
 }
 
-// One step of OptimizeEndpointsForCluster (CP:583-624) for mode kMode
-// with kBits-bit indices. Returns true when the fit is finished.
-template <int kMode, int kBits, bool kUniform>
-__device__ __forceinline__ bool anneal_step(AnnealLane &s, const uint32_t *pts, const uint32_t *proj,
-                                            int stride, const uint8_t *lut) {
+// Squared error of a texel against a palette colour, per FasTC's metric.
+template <bool kUniform>
+__device__ __forceinline__ float texel_err(uint32_t e, uint32_t pal, const float *w) {
+  const uint32_t ad = __vabsdiffu4(e, pal);
+  if (kUniform) return (float)__dp4a(ad, ad, 0u);
+  float ev[4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) ev[c] = __fmul_rn((float)((ad >> (8 * c)) & 0xFF), w[c]);
+  return dot4(ev, ev);
+}
+
+// QuantizedError (RGBAEndpoints.cpp:190-310) for integer endpoints q1/q2 and
+// the fit's texels. The projection floor(D k / L) is exact integer
+// arithmetic; FasTC's float rounding only matters when D k is a multiple of
+// L, and that case repeats its float division and product.
+template <int kBits, bool kRot, bool kUniform, bool kIdx>
+__device__ __forceinline__ float qe_simd(const uint32_t *pts, const uint32_t *proj, uint32_t *pal,
+                                         int n, uint32_t q1, uint32_t q2, const float *w,
+                                         uint64_t tex, uint64_t &idx) {
+  constexpr int kNB = 1 << kBits;
+  constexpr uint32_t km = kNB - 1;
+  constexpr int T = kAnnealThreads;
+  int u1[4], dir[4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    u1[c] = (int)((q1 >> (8 * c)) & 0xFF);
+    dir[c] = (int)((q2 >> (8 * c)) & 0xFF) - u1[c];
+  }
+  const int L = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2] + dir[3] * dir[3];
+  uint32_t itotal = 0;
+  float ftotal = 0.0f;
+  if (L == 0) {
+    for (int k = 0; k < n; k++) {
+      const uint32_t e = pts[k * T];
+      if (kUniform) {
+        const uint32_t ad = __vabsdiffu4(e, q1);
+        itotal += __dp4a(ad, ad, 0u);
+      } else {
+        ftotal = __fadd_rn(ftotal, texel_err<false>(e, q1, w));
+      }
+      if (kIdx) set_nib(idx, (int)((tex >> (4 * k)) & 15), 0);
+    }
+    return kUniform ? (float)itotal : ftotal;
+  }
+  // palette of the interpolated colours, two 16-bit lanes at a time
+  {
+    const uint32_t rb1 = q1 & 0x00FF00FFu, ga1 = (q1 >> 8) & 0x00FF00FFu;
+    const uint32_t rb2 = q2 & 0x00FF00FFu, ga2 = (q2 >> 8) & 0x00FF00FFu;
+#pragma unroll
+    for (int j = 0; j < kNB; j++) {
+      const uint32_t w1 = wt<kBits>(j), w0 = 64u - w1;
+      const uint32_t vrb = rb1 * w0 + rb2 * w1 + 0x00200020u;
+      const uint32_t vga = ga1 * w0 + ga2 * w1 + 0x00200020u;
+      pal[j * T] = ((vrb >> 6) & 0x00FF00FFu) | (((vga >> 6) & 0x00FF00FFu) << 8);
+    }
+  }
+  const uint32_t dlo = ((uint32_t)dir[0] & 0xFFFFu) | ((uint32_t)dir[1] << 16);
+  const uint32_t dhi = ((uint32_t)dir[2] & 0xFFFFu) | ((uint32_t)dir[3] << 16);
+  const int negk = -(dir[0] * u1[0] + dir[1] * u1[1] + dir[2] * u1[2] + dir[3] * u1[3]);
+  const uint32_t R = L > 1 ? 0xFFFFFFFFu / (uint32_t)L + 1u : 0u;
+  for (int k = 0; k < n; k++) {
+    const uint32_t e = pts[k * T];
+    const uint32_t p = kRot ? proj[k * T] : e;
+    const int D = dp2a_hi(dhi, p, dp2a_lo(dlo, p, negk));
+    int j1, j2;
+    if (D <= 0) {
+      j1 = j2 = 0;
+    } else if (D >= L) {
+      j1 = j2 = (int)km;
+    } else {
+      const uint32_t num = (uint32_t)D * km;
+      uint32_t q = __umulhi(num, R);
+      int r = (int)(num - q * (uint32_t)L);
+      if (r < 0) {
+        q--;
+        r += L;
+      }
+      j1 = (int)q;
+      j2 = (int)q + 1;
+      if (r == 0) {
+        const float sc = __fmul_rn(__fdiv_rn((float)D, (float)L), (float)km);
+        j1 = min(max(0, __float2int_rz(floorf(sc))), (int)km);
+        j2 = min(__float2int_rz(ceilf(sc)), (int)km);
+      }
+    }
+    const float e1 = texel_err<kUniform>(e, pal[j1 * T], w);
+    float best = e1;
+    int bj = j1;
+    if (j2 > j1) {
+      const float e2 = texel_err<kUniform>(e, pal[(j1 + 1) * T], w);
+      if (e2 < e1) {
+        best = e2;
+        bj = j1 + 1;
+      }
+    }
+    if (kUniform) itotal += (uint32_t)best;
+    else ftotal = __fadd_rn(ftotal, best);
+    if (kIdx) set_nib(idx, (int)((tex >> (4 * k)) & 15), (uint32_t)bj);
+  }
+  return kUniform ? (float)itotal : ftotal;
+}
+
+struct Lane {
+  uint32_t t;
+  uint32_t p1, p2, b1, b2, lcg;
+  int cur_pbit, best_pbit, energy, steps, n;
+  float cur_err, best_err;
+  uint64_t tex;
+  float w[4];
+  bool uniform;
+};
+
+// One iteration of OptimizeEndpointsForCluster's loop (CP:583-624) for
+// class C; returns true when the fit is finished.
+template <int C, bool kUniform>
+__device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t *pts, const uint32_t *proj,
+                                            uint32_t *pal, const uint8_t *lut) {
+  constexpr int kMode = class_mode(C);
   constexpr ModeAttr a = mode_attr(kMode);
+  constexpr int kBits = class_im(C) ? a.alpha_idx_bits : a.idx_bits;
   constexpr bool kRot = a.has_rotation != 0;
   constexpr bool kHasPbits = a.pbit != kPBitNone;
   if (!(s.best_err > 0.0f && s.energy < s.steps)) return true;
   const float temp = __fdiv_rn((float)s.energy, (float)(s.steps - 1));
-  // PickBestNeighboringEndpoints (CP:426-498), integer endpoints
+  // PickBestNeighboringEndpoints (CP:426-498) on integer endpoints
   constexpr int sc = 1 << (8 - a.color_bits);
   constexpr int sa = kMode < 4 ? 0 : (1 << (8 - a.alpha_bits));
   int npbit = 0;
@@ -650,8 +667,8 @@ __device__ __forceinline__ bool anneal_step(AnnealLane &s, const uint32_t *pts, 
   const int pc = pbit_combo(a, npbit);
   const uint32_t q1 = qpix<a.color_bits, a.alpha_bits>(lut, np1, pb_first(pc));
   const uint32_t q2 = qpix<a.color_bits, a.alpha_bits>(lut, np2, pb_second(pc));
-  uint64_t dummy = 0;
-  const float err = qe_int<kBits, kRot, kUniform>(pts, proj, stride, s.n, q1, q2, s.w, false, s.tex, dummy);
+  uint64_t unused = 0;
+  const float err = qe_simd<kBits, kRot, kUniform, false>(pts, proj, pal, s.n, q1, q2, s.w, s.tex, unused);
   // AcceptNewEndpointError (CP:524-536)
   bool accept = err < s.cur_err;
   if (!accept) {
@@ -670,8 +687,6 @@ __device__ __forceinline__ bool anneal_step(AnnealLane &s, const uint32_t *pts, 
     s.cur_pbit = npbit;
   }
   if (err < s.best_err) {
-    s.idx = 0;
-    qe_int<kBits, kRot, kUniform>(pts, proj, stride, s.n, q1, q2, s.w, true, s.tex, s.idx);
     s.b1 = np1;
     s.b2 = np2;
     s.best_pbit = npbit;
@@ -682,124 +697,114 @@ __device__ __forceinline__ bool anneal_step(AnnealLane &s, const uint32_t *pts, 
   return false;
 }
 
-// Fit kinds: (mode, colour index bits) pairs; mode 4 anneals with 2-bit
-// indices in index mode 0 and 3-bit indices in index mode 1.
-__device__ __forceinline__ int kind_of(int mode, int im) {
-  return mode == 4 ? (im ? 8 : 4) : mode;
-}
-
-template <bool kUniform>
-__device__ __forceinline__ bool anneal_dispatch(AnnealLane &s, const uint32_t *pts,
-                                                const uint32_t *proj, int stride,
-                                                const uint8_t *lut) {
-  switch (s.kind) {
-    case 0: return anneal_step<0, 3, kUniform>(s, pts, proj, stride, lut);
-    case 1: return anneal_step<1, 3, kUniform>(s, pts, proj, stride, lut);
-    case 2: return anneal_step<2, 2, kUniform>(s, pts, proj, stride, lut);
-    case 3: return anneal_step<3, 2, kUniform>(s, pts, proj, stride, lut);
-    case 4: return anneal_step<4, 2, kUniform>(s, pts, proj, stride, lut);
-    case 5: return anneal_step<5, 2, kUniform>(s, pts, proj, stride, lut);
-    case 6: return anneal_step<6, 4, kUniform>(s, pts, proj, stride, lut);
-    case 7: return anneal_step<7, 2, kUniform>(s, pts, proj, stride, lut);
-    default: return anneal_step<4, 3, kUniform>(s, pts, proj, stride, lut);
-  }
-}
-
+template <int C>
 __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
-    const JobDev *__restrict__ jobs, const BlockSel *__restrict__ sel,
-    PipelineCounters *__restrict__ ctr, TaskState *__restrict__ state) {
+    const JobDev *__restrict__ jobs, uint32_t nb, const BlockSel *__restrict__ sel,
+    const uint16_t *__restrict__ local, const uint32_t *__restrict__ chunk,
+    PipelineCounters *__restrict__ ctr, const uint32_t *__restrict__ alist,
+    TaskState *__restrict__ state) {
+  constexpr int kMode = class_mode(C);
+  constexpr ModeAttr a = mode_attr(kMode);
+  constexpr int kBits = class_im(C) ? a.alpha_idx_bits : a.idx_bits;
+  constexpr bool kRot = a.has_rotation != 0;
+  constexpr int T = kAnnealThreads;
   __shared__ uint8_t s_lut[8 * 3 * 256];
-  __shared__ uint32_t s_pts[16 * kAnnealThreads];
-  __shared__ uint32_t s_proj[16 * kAnnealThreads];
-  for (int i = threadIdx.x; i < 8 * 3 * 256; i += blockDim.x)
-    s_lut[i] = (&q_qlut[0][0][0])[i];
+  __shared__ uint32_t s_pts[16 * T];
+  __shared__ uint32_t s_proj[kRot ? 16 * T : 1];
+  __shared__ uint32_t s_pal[(1 << kBits) * T];
+  for (int i = threadIdx.x; i < 8 * 3 * 256; i += blockDim.x) s_lut[i] = (&q_qlut[0][0][0])[i];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   uint32_t *pts = s_pts + threadIdx.x;
-  uint32_t *proj = s_proj + threadIdx.x;
-  const uint32_t ntasks = ctr->tasks;
-  AnnealLane s;
-  bool active = false, exhausted = false, uniform = true;
+  uint32_t *proj = kRot ? s_proj + threadIdx.x : pts;
+  uint32_t *pal = s_pal + threadIdx.x;
+  const uint32_t count = ctr->anneal_count[C];
+  const uint32_t base = scanned(local, chunk, (uint64_t)C * nb);
+  Lane s;
+  bool active = false, exhausted = false;
   for (;;) {
     const bool need = !active && !exhausted;
     const uint32_t nmask = __ballot_sync(0xFFFFFFFFu, need);
     if (nmask) {
-      uint32_t base = 0;
+      unsigned long long b0 = 0;
       const int leader = __ffs(nmask) - 1;
-      if (lane == leader) base = (uint32_t)atomicAdd(&ctr->anneal_next, (unsigned long long)__popc(nmask));
-      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (lane == leader) b0 = atomicAdd(&ctr->anneal_next[C], (unsigned long long)__popc(nmask));
+      b0 = __shfl_sync(0xFFFFFFFFu, b0, leader);
       if (need) {
-        const uint32_t t = base + __popc(nmask & ((1u << lane) - 1u));
-        if (t >= ntasks) {
+        const unsigned long long k = b0 + __popc(nmask & ((1u << lane) - 1u));
+        if (k >= count) {
           exhausted = true;
         } else {
+          const uint32_t t = alist[base + (uint32_t)k];
           const TaskState o = state[t];
-          if (o.flags & kTaskAnneal) {
-            const BlockSel bs = sel[o.gl];
-            const JobDev &jb = jobs[bs.job];
-            const Selection sl = sel_of(bs);
-            const uint32_t part = part_word_of(sl, o.mode, o.slot);
-            const int rot = o.rotim >> 1;
-            s.t = t;
-            s.p1 = s.b1 = o.p1;
-            s.p2 = s.b2 = o.p2;
-            s.cur_pbit = s.best_pbit = o.pbit;
-            s.cur_err = s.best_err = (float)o.err;
-            s.idx = o.idx;
-            s.lcg = o.lcg;
-            s.energy = 0;
-            s.steps = o.steps;
-            s.kind = kind_of(o.mode, o.rotim & 1);
-            uniform = !(o.flags & kTaskNonuniform);
-            ModeCtx m;
-            m.a = mode_attr(o.mode);
-            m.rot = rot;
-            m.metric = uniform ? 0 : 1;
-            metric_of(m, s.w);
-            int n = 0;
-            uint64_t tex = 0;
+          const BlockSel bs = sel[o.gl];
+          const JobDev &jb = jobs[bs.job];
+          const uint32_t part = part_word_of(sel_of(bs), kMode, o.slot);
+          const int rot = o.rotim >> 1;
+          s.t = t;
+          s.p1 = s.b1 = o.p1;
+          s.p2 = s.b2 = o.p2;
+          s.cur_pbit = s.best_pbit = o.pbit;
+          s.cur_err = s.best_err = (float)o.err;
+          s.lcg = o.lcg;
+          s.energy = 0;
+          s.steps = o.steps;
+          s.uniform = !(o.flags & kTaskNonuniform);
+          ModeCtx m;
+          m.a = a;
+          m.rot = rot;
+          m.metric = s.uniform ? 0 : 1;
+          metric_of(m, s.w);
+          int n = 0;
+          uint64_t tex = 0;
 #pragma unroll
-            for (int r = 0; r < 4; r++) {
-              const uint4 v = load_row_p(jb, bs.lin, r);
-              const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
+          for (int r = 0; r < 4; r++) {
+            const uint4 v = load_row_p(jb, bs.lin, r);
+            const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-              for (int c = 0; c < 4; c++) {
-                const int ti = r * 4 + c;
-                if ((int)((part >> (2 * ti)) & 3) != o.subset) continue;
-                const uint32_t e = vv[c];
+            for (int c = 0; c < 4; c++) {
+              const int ti = r * 4 + c;
+              if ((int)((part >> (2 * ti)) & 3) != o.subset) continue;
+              const uint32_t e = vv[c];
+              pts[n * T] = e;
+              if (kRot) {
+                // the colour fit projects the rotated texel with alpha 255
                 uint32_t pr = e;
-                if (m.a.has_rotation) {
-                  // the colour fit sees the rotated texel with alpha 255
-                  if (rot) {
-                    const uint32_t sh = 8u * (uint32_t)(rot - 1);
-                    pr = (pr & ~(0xFFu << sh)) | ((e >> 24) << sh);
-                  }
-                  pr |= 0xFF000000u;
+                if (rot) {
+                  const uint32_t sh = 8u * (uint32_t)(rot - 1);
+                  pr = (pr & ~(0xFFu << sh)) | ((e >> 24) << sh);
                 }
-                pts[n * kAnnealThreads] = e;
-                proj[n * kAnnealThreads] = pr;
-                tex |= (uint64_t)ti << (4 * n);
-                n++;
+                proj[n * T] = pr | 0xFF000000u;
               }
+              tex |= (uint64_t)ti << (4 * n);
+              n++;
             }
-            s.n = n;
-            s.tex = tex;
-            active = true;
           }
+          s.n = n;
+          s.tex = tex;
+          active = true;
         }
       }
     }
     if (__all_sync(0xFFFFFFFFu, exhausted && !active)) break;
     if (active) {
-      const bool done = uniform ? anneal_dispatch<true>(s, pts, proj, kAnnealThreads, s_lut)
-                                : anneal_dispatch<false>(s, pts, proj, kAnnealThreads, s_lut);
+      const bool done = s.uniform ? anneal_step<C, true>(s, pts, proj, pal, s_lut)
+                                  : anneal_step<C, false>(s, pts, proj, pal, s_lut);
       if (done) {
+        // indices of the best endpoints (the same QuantizedError call that
+        // found them)
+        const int pc = pbit_combo(a, s.best_pbit);
+        const uint32_t q1 = qpix<a.color_bits, a.alpha_bits>(s_lut, s.b1, pb_first(pc));
+        const uint32_t q2 = qpix<a.color_bits, a.alpha_bits>(s_lut, s.b2, pb_second(pc));
+        uint64_t idx = 0;
+        if (s.uniform) qe_simd<kBits, kRot, true, true>(pts, proj, pal, s.n, q1, q2, s.w, s.tex, idx);
+        else qe_simd<kBits, kRot, false, true>(pts, proj, pal, s.n, q1, q2, s.w, s.tex, idx);
         TaskState &o = state[s.t];
         o.p1 = s.b1;
         o.p2 = s.b2;
         o.pbit = (uint8_t)s.best_pbit;
         o.err = (double)s.best_err;
-        o.idx = s.idx;
+        o.idx = idx;
         active = false;
       }
     }
@@ -852,7 +857,12 @@ __global__ void pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
     const int mode = mode_order(oi);
     if (!(modes & (1u << mode))) continue;
     const ModeAttr a = mode_attr(mode);
-    uint32_t t = scanned(local, chunk, (uint64_t)mode * nb + gl);
+    const int nim = mode == 4 ? 2 : 1;
+    uint32_t cbase[2];
+    for (int k = 0; k < nim; k++)
+      cbase[k] = scanned(local, chunk, (uint64_t)class_of(mode, k) * nb + gl);
+    uint32_t t = cbase[0];
+    int slot_rank = 0;
     for (uint32_t sl = 0; sl < nshapes; sl++) {
       if (a.subsets != 1 && (uint32_t)a.subsets != s.nparts[sl]) continue;
       if (s.shape[sl] >= 16 && mode == 0) continue;
@@ -860,14 +870,15 @@ __global__ void pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
       uint32_t first = t;
       int rot = 0, im = 0;
       if (a.has_rotation) {
-        const int nim = mode == 4 ? 2 : 1;
+        // rotation-major, index-mode-minor, like CompressionMode::Compress
         double b = DBL_MAX;
         for (int r = 0; r < 4; r++)
-          for (int k = 0; k < nim; k++, t++) {
-            const double e = state[t].err + state[t].aerr;
+          for (int k = 0; k < nim; k++) {
+            const uint32_t tt = cbase[k] + (uint32_t)(slot_rank * 4 + r);
+            const double e = state[tt].err + state[tt].aerr;
             if (e < b) {
               b = e;
-              first = t;
+              first = tt;
               rot = r;
               im = k;
             }
@@ -876,6 +887,7 @@ __global__ void pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
       } else {
         for (int ci = 0; ci < a.subsets; ci++, t++) total = total + state[t].err;
       }
+      slot_rank++;
       if (total < best) {
         best = total;
         best_mode = mode;
@@ -905,7 +917,7 @@ __global__ void pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
 
 size_t pipeline_scratch_bytes(uint64_t total_blocks) {
   const uint64_t nb = total_blocks < kPipelineChunk ? total_blocks : kPipelineChunk;
-  const uint64_t n8 = 8 * nb;
+  const uint64_t n8 = (uint64_t)kClasses * nb;
   const uint64_t tmax = (uint64_t)kMaxBlockTasks * nb;
   size_t b = 256;
   b += (nb * sizeof(BlockSel) + 255) & ~255ull;
@@ -914,6 +926,7 @@ size_t pipeline_scratch_bytes(uint64_t total_blocks) {
   b += (((n8 + kRankChunk - 1) / kRankChunk) * 4 + 255) & ~255ull;
   b += (tmax * sizeof(uint2) + 255) & ~255ull;
   b += (tmax * sizeof(TaskState) + 255) & ~255ull;
+  b += (tmax * sizeof(uint32_t) + 255) & ~255ull;
   return b;
 }
 
@@ -931,17 +944,19 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
   BlockSel *sel = reinterpret_cast<BlockSel *>(p);
   p += (nbmax * sizeof(BlockSel) + 255) & ~255ull;
   uint8_t *counts = p;
-  p += (8 * nbmax + 255) & ~255ull;
+  p += ((uint64_t)kClasses * nbmax + 255) & ~255ull;
   uint16_t *local = reinterpret_cast<uint16_t *>(p);
-  p += (16 * nbmax + 255) & ~255ull;
+  p += ((uint64_t)kClasses * 2 * nbmax + 255) & ~255ull;
   uint32_t *chunk = reinterpret_cast<uint32_t *>(p);
-  p += (((8 * nbmax + kRankChunk - 1) / kRankChunk) * 4 + 255) & ~255ull;
+  p += ((((uint64_t)kClasses * nbmax + kRankChunk - 1) / kRankChunk) * 4 + 255) & ~255ull;
   uint2 *desc = reinterpret_cast<uint2 *>(p);
   p += ((uint64_t)kMaxBlockTasks * nbmax * sizeof(uint2) + 255) & ~255ull;
   TaskState *state = reinterpret_cast<TaskState *>(p);
+  p += ((uint64_t)kMaxBlockTasks * nbmax * sizeof(TaskState) + 255) & ~255ull;
+  uint32_t *alist = reinterpret_cast<uint32_t *>(p);
   for (uint64_t c0 = 0; c0 < total; c0 += cap) {
     const uint32_t nb = (uint32_t)(total - c0 < cap ? total - c0 : cap);
-    const uint64_t n8 = 8ull * nb;
+    const uint64_t n8 = (uint64_t)kClasses * nb;
     const uint32_t nchunks = (uint32_t)((n8 + kRankChunk - 1) / kRankChunk);
     const int sel_ctas = (int)((nb + 3) / 4 < (uint64_t)sm_count * 16 ? (nb + 3) / 4 : (uint64_t)sm_count * 16);
     select_kernel<4><<<sel_ctas, 128, 0, st>>>(jobs, njobs, c0, nb, rank.rank_local, rank.chunk_prefix,
@@ -949,8 +964,18 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     scan_local_u8_kernel<<<nchunks, kRankChunk, 0, st>>>(counts, n8, local, chunk);
     scan_chunks_kernel<<<1, 1024, 0, st>>>(chunk, nchunks, ctr);
     emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, counts, local, chunk, desc);
-    setup_kernel<<<sm_count * 8, kSetupThreads, 0, st>>>(jobs, sel, desc, ctr, state, rank.status);
-    anneal_kernel<<<sm_count * 6, kAnnealThreads, 0, st>>>(jobs, sel, ctr, state);
+    setup_kernel<<<sm_count * 8, kSetupThreads, 0, st>>>(jobs, nb, sel, desc, local, chunk, ctr,
+                                                         state, alist, rank.status);
+    const int ag = sm_count * 8;
+    anneal_kernel<0><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
+    anneal_kernel<1><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
+    anneal_kernel<2><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
+    anneal_kernel<3><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
+    anneal_kernel<4><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
+    anneal_kernel<5><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
+    anneal_kernel<6><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
+    anneal_kernel<7><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
+    anneal_kernel<8><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
     pack_kernel<<<(nb + 127) / 128, 128, 0, st>>>(jobs, nb, sel, local, chunk, state);
     e = (int)cudaPeekAtLastError();
     if (e) return e;

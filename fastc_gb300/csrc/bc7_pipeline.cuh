@@ -42,10 +42,20 @@ struct __align__(16) TaskState {
   uint8_t flags;
 };
 
+// Task classes: one per (BC7 mode, colour index width). Mode 4 anneals with
+// 2-bit indices in index mode 0 and 3-bit indices in index mode 1, so it
+// has two classes; every other mode has one.
+constexpr int kClasses = 9;
+__host__ __device__ constexpr int class_mode(int c) { return c < 4 ? c : (c <= 5 ? 4 : c - 1); }
+__host__ __device__ constexpr int class_im(int c) { return c == 5 ? 1 : 0; }
+__host__ __device__ constexpr int class_of(int mode, int im) {
+  return mode < 4 ? mode : (mode == 4 ? 4 + im : mode + 1);
+}
+
 struct PipelineCounters {
-  unsigned long long anneal_next;  // next task for the annealing refill
-  uint32_t tasks;                  // tasks in the current chunk
-  uint32_t pad;
+  unsigned long long anneal_next[kClasses];  // refill cursors of the annealing lists
+  uint32_t anneal_count[kClasses];           // fits of each class that anneal
+  uint32_t tasks;                            // tasks in the current chunk
 };
 
 void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t opt6[256]);
