@@ -50,7 +50,8 @@ __device__ inline double estimate_shape(const uint32_t *px, uint32_t part, int n
   double err = 0.0;
   for (int ci = 0; ci < nsub; ci++) {
     Cluster c;
-    make_cluster(px, part, ci, c);
+    uint32_t buf[16];
+    make_cluster(px, part, ci, buf, 1, c);
     float v[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) v[k] = __fsub_rn(c.mx[k], c.mn[k]);
@@ -170,7 +171,8 @@ __device__ inline void run_task(const Task &t, const Selection &sel, const uint3
   const uint32_t shape = sel.shape[t.slot];
   const uint32_t part = m.a.subsets == 2 ? part2[shape] : (m.a.subsets == 3 ? part3[shape] : 0u);
   Cluster c;
-  make_cluster(px, part, t.subset, c);
+  uint32_t buf[16];
+  make_cluster(px, part, t.subset, buf, 1, c);
   o.idx = 0;
   o.aidx = 0;
   o.pbit = 0;

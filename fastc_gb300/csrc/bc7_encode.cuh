@@ -187,32 +187,40 @@ __device__ __forceinline__ int pb_first(int combo) { return combo & 1; }
 __device__ __forceinline__ int pb_second(int combo) { return (combo >> 1) & 1; }
 
 // --------------------------------------------------------------------------
-// Clusters (RE:104-227). Points are iterated in texel order; arrays that
-// FasTC indexes by point are indexed by texel here (same order).
+// Clusters (RE:104-227). A cluster holds its member texels compacted in
+// texel order (FasTC's m_PointMap order): point k is px[k * stride], its
+// texel index is nibble k of `tex`.
 // --------------------------------------------------------------------------
 
 struct Cluster {
-  const uint32_t *px;  // the block's 16 texels
-  uint32_t mask;       // member texels
+  const uint32_t *px;  // member texels, compacted
+  int stride;
+  uint64_t tex;        // texel index of each point, 4 bits per point
   int n;
   int rot;    // alpha path: channel (1..3) swapped into alpha, 0 = none
   bool a255;  // alpha path: alpha of every point forced to 255
   float avg[4], mn[4], mx[4];
 };
 
-__device__ __forceinline__ void cl_point(const Cluster &c, int t, float *p) {
-  unpack4(c.px[t], p);
+__device__ __forceinline__ uint32_t cl_pixel(const Cluster &c, int k) { return c.px[k * c.stride]; }
+__device__ __forceinline__ int cl_texel(const Cluster &c, int k) { return (int)((c.tex >> (4 * k)) & 15); }
+
+__device__ __forceinline__ void cl_point(const Cluster &c, int k, float *p) {
+  unpack4(cl_pixel(c, k), p);
   if (c.a255) {
     if (c.rot) p[c.rot - 1] = p[3];
     p[3] = 255.0f;
   }
 }
 
-// RGBACluster ctor + SetPartition/Recalculate (RE:108-127, 205-226)
+// RGBACluster ctor + SetPartition/Recalculate (RE:108-127, 205-226). The
+// members of `subset` among the 16 texels `px` are written to `buf` (stride
+// `bstride`) in texel order.
 __device__ __forceinline__ void make_cluster(const uint32_t *px, uint32_t part_word,
-                                             int subset, Cluster &c) {
-  c.px = px;
-  c.mask = 0;
+                                             int subset, uint32_t *buf, int bstride, Cluster &c) {
+  c.px = buf;
+  c.stride = bstride;
+  c.tex = 0;
   c.n = 0;
   c.rot = 0;
   c.a255 = false;
@@ -226,7 +234,8 @@ __device__ __forceinline__ void make_cluster(const uint32_t *px, uint32_t part_w
     if ((int)((part_word >> (2 * i)) & 3) != subset) continue;
     float p[4];
     unpack4(px[i], p);
-    c.mask |= 1u << i;
+    buf[c.n * bstride] = px[i];
+    c.tex |= (uint64_t)i << (4 * c.n);
     c.n++;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -267,21 +276,21 @@ __device__ inline float quantized_error(const Cluster &c, const float *p1, const
   const float lsq = dot4(d, d);
   float total = 0.0f;
   if (lsq == 0.0f) {
-    for (int i = 0; i < 16; i++) {
-      if (!((c.mask >> i) & 1)) continue;
+    for (int i = 0; i < c.n; i++) {
+      const uint32_t e = cl_pixel(c, i);
       float ev[4];
 #pragma unroll
       for (int k = 0; k < 4; k++) {
         const uint32_t ip = (q1 >> (8 * k)) & 0xFF;
-        ev[k] = __fmul_rn((float)sad8(c.px[i] >> (8 * k), ip), w[k]);
+        ev[k] = __fmul_rn((float)sad8(e >> (8 * k), ip), w[k]);
       }
       total = __fadd_rn(total, dot4(ev, ev));
-      if (idx) set_nib(*idx, i, 0);
+      if (idx) set_nib(*idx, cl_texel(c, i), 0);
     }
     return total;
   }
-  for (int i = 0; i < 16; i++) {
-    if (!((c.mask >> i) & 1)) continue;
+  for (int i = 0; i < c.n; i++) {
+    const uint32_t epx = cl_pixel(c, i);
     float pt[4], t[4];
     cl_point(c, i, pt);
 #pragma unroll
@@ -302,7 +311,7 @@ __device__ inline float quantized_error(const Cluster &c, const float *p1, const
       for (int k = 0; k < 4; k++) {
         const uint32_t a = (q1 >> (8 * k)) & 0xFF, b = (q2 >> (8 * k)) & 0xFF;
         const uint32_t ip = ((a * w0 + b * w1 + 32u) >> 6) & 0xFF;
-        ev[k] = __fmul_rn((float)sad8(c.px[i] >> (8 * k), ip), w[k]);
+        ev[k] = __fmul_rn((float)sad8(epx >> (8 * k), ip), w[k]);
       }
       const float err = dot4(ev, ev);
       if (err < min_err) {
@@ -313,7 +322,7 @@ __device__ inline float quantized_error(const Cluster &c, const float *p1, const
       }
     } while (++j <= j2);
     total = __fadd_rn(total, min_err);
-    if (idx) set_nib(*idx, i, best);
+    if (idx) set_nib(*idx, cl_texel(c, i), best);
   }
   return total;
 }
@@ -356,8 +365,7 @@ __device__ inline void principal_axis(const Cluster &c, float *axis) {
   // unique points, in order; slots past the unique count stay (-1,-1,-1,-1)
   float upts[16][4];
   int nu = 0;
-  for (int i = 0; i < 16; i++) {
-    if (!((c.mask >> i) & 1)) continue;
+  for (int i = 0; i < c.n; i++) {
     float p[4];
     cl_point(c, i, p);
     bool has = false;
@@ -401,8 +409,7 @@ __device__ inline void principal_axis(const Cluster &c, float *axis) {
 #pragma unroll
     for (int j = 0; j <= i; j++) {
       float s = 0.0f;
-      for (int t = 0; t < 16; t++) {
-        if (!((c.mask >> t) & 1)) continue;
+      for (int t = 0; t < c.n; t++) {
         float p[4];
         cl_point(c, t, p);
         s = __fadd_rn(s, __fmul_rn(__fsub_rn(p[i], c.avg[i]), __fsub_rn(p[j], c.avg[j])));
@@ -727,10 +734,9 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
   st.errf = 0.0f;
   if (all_same_point(c)) {
     float p0[4];
-    cl_point(c, __ffs(c.mask) - 1, p0);
+    cl_point(c, 0, p0);
     const double e = single_color(m, p0, p1, p2, pbit);
-    for (int i = 0; i < 16; i++)
-      if ((c.mask >> i) & 1) set_nib(idx, i, 1);
+    for (int i = 0; i < c.n; i++) set_nib(idx, cl_texel(c, i), 1);
     st.err = (double)c.n * e;
     return;
   }
@@ -739,8 +745,7 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
   float axis[4];
   principal_axis(c, axis);
   float mindp = FLT_MAX, maxdp = -FLT_MAX;
-  for (int i = 0; i < 16; i++) {
-    if (!((c.mask >> i) & 1)) continue;
+  for (int i = 0; i < c.n; i++) {
     float p[4], t[4];
     cl_point(c, i, p);
 #pragma unroll
@@ -772,8 +777,7 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
       atomicOr(m.status, kStatusKMeansCap);
       break;
     }
-    for (int i = 0; i < 16; i++) {
-      if (!((c.mask >> i) & 1)) continue;
+    for (int i = 0; i < c.n; i++) {
       float p[4];
       cl_point(c, i, p);
       int minb = 0;
@@ -794,8 +798,8 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
     for (int j = 0; j < nb; j++) {
       float np[4] = {0.0f, 0.0f, 0.0f, 0.0f};
       uint32_t cnt = 0;
-      for (int i = 0; i < 16; i++) {
-        if (!((c.mask >> i) & 1) || get_nib(bidx, i) != (uint32_t)j) continue;
+      for (int i = 0; i < c.n; i++) {
+        if (get_nib(bidx, i) != (uint32_t)j) continue;
         float p[4];
         cl_point(c, i, p);
         cnt++;
@@ -819,8 +823,7 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
     }
   if (filled == 1) {
     const double e = single_color(m, pts[last], p1, p2, pbit);
-    for (int i = 0; i < 16; i++)
-      if ((c.mask >> i) & 1) set_nib(idx, i, 1);
+    for (int i = 0; i < c.n; i++) set_nib(idx, cl_texel(c, i), 1);
     st.err = (double)c.n * e;
     return;
   }
@@ -893,7 +896,7 @@ __device__ inline double fit_alpha(ModeCtx &m, const Cluster &c, const uint32_t 
   float avals[16];
   float amin = FLT_MAX, amax = -FLT_MAX;
   for (int i = 0; i < 16; i++) {
-    const uint32_t px = c.px[i];
+    const uint32_t px = cl_pixel(c, i);
     const uint32_t ch = r ? r - 1 : 3;
     avals[i] = (float)((px >> (8 * ch)) & 0xFF);
     amin = min_std(avals[i], amin);
@@ -928,7 +931,7 @@ __device__ inline void fit_alpha_setup(ModeCtx &m, const Cluster &c, const uint3
   float amin = FLT_MAX, amax = -FLT_MAX;
   for (int i = 0; i < 16; i++) {
     const uint32_t ch = r ? r - 1 : 3;
-    avals[i] = (float)((c.px[i] >> (8 * ch)) & 0xFF);
+    avals[i] = (float)((cl_pixel(c, i) >> (8 * ch)) & 0xFF);
     amin = min_std(avals[i], amin);
     amax = max_std(avals[i], amax);
   }

@@ -392,7 +392,9 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     const uint32_t *__restrict__ chunk, PipelineCounters *__restrict__ ctr,
     TaskState *__restrict__ state, uint32_t *__restrict__ alist, uint32_t *status) {
   __shared__ uint32_t s_px[kSetupThreads * 17];
+  __shared__ uint32_t s_pts[16 * kSetupThreads];
   uint32_t *px = s_px + threadIdx.x * 17;
+  uint32_t *pts = s_pts + threadIdx.x;
   const uint32_t ntasks = ctr->tasks;
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntasks;
        t += gridDim.x * blockDim.x) {
@@ -425,7 +427,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     m.lcg = 0;
     m.sct = g_sct;
     Cluster c;
-    make_cluster(px, part_word_of(s, mode, tk.slot), tk.subset, c);
+    make_cluster(px, part_word_of(s, mode, tk.slot), tk.subset, pts, kSetupThreads, c);
     FitSetup st;
     st.idx = 0;
     st.pbit = 0;
