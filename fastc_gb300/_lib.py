@@ -91,6 +91,8 @@ SIGNATURES = {
                                             C.c_void_p]),
     "fastc_bc7_decompress_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int,
                                               C.c_void_p]),
+    "fastc_bc7_compress_device_noalloc": (C.c_int, [C.POINTER(Job), C.c_uint32, C.POINTER(Settings),
+                                                  C.c_int, C.c_void_p]),
     "fastc_bc7_plan_create": (C.c_int, [C.POINTER(Job), C.c_uint32, C.POINTER(Settings), C.c_int,
                                         C.POINTER(C.c_void_p)]),
     "fastc_bc7_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
           "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
-SOURCES = ["bc7_kernels.cu", "bc7_pipeline.cu", "bc7_api.cu", "bc7_server.cu"]
+SOURCES = ["bc7_kernels.cu", "bc7_pipeline.cu", "bc7_api.cu", "bc7_server.cu", "bc7_static.cu"]
 
 
 def nvcc() -> str:

@@ -163,6 +163,30 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_decompress_device(const uint8_t *blocks
                                              uint32_t width, uint32_t height,
                                              int spec_semantics, void *stream);
 
+/* fastc_bc7_compress_device without any allocation inside the call: the job
+ * table and scratch live in a fixed array in the library's device image
+ * (about 2.1 MB). No counterpart in FasTC, whose encoder needs no device
+ * memory; it serves callers that cannot let a library allocate (memory
+ * budgeted up front, no allocator locks or device-wide synchronisation
+ * while encoding). Same arguments and the same output bytes as
+ * fastc_bc7_compress_device, with these differences:
+ *   - at most FASTC_BC7_NOALLOC_MAX_JOBS jobs and FASTC_BC7_NOALLOC_MAX_BLOCKS
+ *     4x4 blocks in total per call, else FASTC_BC7_ERR_INVALID_ARGUMENT with
+ *     the limit in fastc_bc7_last_error;
+ *   - the first call on each device does one-time set-up (looks the array
+ *     up and uploads the encoder's tables, synchronising the device); make
+ *     it before any stream capture;
+ *   - every call reuses the one array, so calls that overlap on the device
+ *     (different streams, or threads without ordering) race and corrupt
+ *     each other's output; calls in order on one stream are safe;
+ *   - it always runs the warp-per-block engine. */
+#define FASTC_BC7_NOALLOC_MAX_BLOCKS (1u << 20)
+#define FASTC_BC7_NOALLOC_MAX_JOBS 256u
+FASTC_BC7_API fastc_bc7_status fastc_bc7_compress_device_noalloc(const fastc_bc7_job *jobs,
+                                                   uint32_t n,
+                                                   const fastc_bc7_settings *settings,
+                                                   int per_job_settings, void *stream);
+
 /* The process-wide watermark counter used by FASTC_BC7_WATERMARK_CONTINUE
  * (the entry the next single-colour block takes; FasTC starts at 0). */
 FASTC_BC7_API void fastc_bc7_set_watermark_counter(uint32_t next_entry);
