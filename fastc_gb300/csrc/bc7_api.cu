@@ -20,6 +20,7 @@
 #include "fastc_bc7.h"
 #include "bc7_host.h"
 
+using fastc::ClassStreams;
 using fastc::EncodeScratch;
 using fastc::JobDev;
 using fastc::LaunchShape;
@@ -141,14 +142,44 @@ uint32_t align_flags(const void *in, const void *out) {
 // Encode `total` blocks of the device job table with the selected engine,
 // carving the rank and pipeline scratch out of `scratch`.
 int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
-                  LaunchShape shape, cudaStream_t st) {
+                  LaunchShape shape, const ClassStreams *cls, cudaStream_t st) {
   const EncodeScratch rank = carve_scratch(scratch, total);
   if (engine == FASTC_BC7_ENGINE_PIPELINE) {
     void *pipe = static_cast<uint8_t *>(scratch) + rank_scratch_bytes(total);
     return fastc::launch_pipeline(jobs, njobs, total, rank, pipe,
-                                  fastc::device_sm_count(current_device()), st);
+                                  fastc::device_sm_count(current_device()), cls, st);
   }
   return fastc::launch_encode(jobs, njobs, total, rank, shape, st);
+}
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_cls_mu;
+std::vector<ClassStreams *> g_cls_free[kMaxDevices];
+}  // namespace
+
+ClassStreams *acquire_class_streams(int device) {
+  if (device < 0 || device >= kMaxDevices) return nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_cls_mu);
+    if (!g_cls_free[device].empty()) {
+      ClassStreams *c = g_cls_free[device].back();
+      g_cls_free[device].pop_back();
+      return c;
+    }
+  }
+  ClassStreams *c = new ClassStreams();
+  if (fastc::class_streams_create(c) != cudaSuccess) {
+    delete c;
+    return nullptr;  // the pipeline then runs on the caller's stream alone
+  }
+  return c;
+}
+
+void release_class_streams(int device, ClassStreams *cls) {
+  if (!cls) return;
+  std::lock_guard<std::mutex> lk(g_cls_mu);
+  g_cls_free[device].push_back(cls);
 }
 
 }  // namespace host
@@ -178,6 +209,7 @@ struct HostCtx {
   int device = -1;
   cudaStream_t stream = nullptr;
   DevBuf in, out, jobs, scratch;
+  ClassStreams *cls = nullptr;
 } g_host;
 
 fastc_bc7_status host_ctx_init() {
@@ -185,9 +217,11 @@ fastc_bc7_status host_ctx_init() {
   if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
   if (g_host.device != dev) {
     if (g_host.stream) cudaStreamDestroy(g_host.stream);
+    if (g_host.cls) release_class_streams(g_host.device, g_host.cls);
     g_host = HostCtx();
     CK(cudaStreamCreateWithFlags(&g_host.stream, cudaStreamNonBlocking));
     g_host.device = dev;
+    g_host.cls = acquire_class_streams(dev);
   }
   fastc::upload_tables(dev);
   return FASTC_BC7_OK;
@@ -254,7 +288,7 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
   CK(cudaMemcpyAsync(g_host.jobs.p, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs));
   const EncodeScratch sc = carve_scratch(g_host.scratch.p, total);
   const int le = launch_engine(static_cast<const JobDev *>(g_host.jobs.p), (int)n, total,
-                               g_host.scratch.p, g_engine, pick_shape(total), cs);
+                               g_host.scratch.p, g_engine, pick_shape(total), g_host.cls, cs);
   if (le) return fail_cuda((cudaError_t)le);
   for (uint32_t i = 0; i < n; i++) {
     if (!dj[i].nblocks) continue;
@@ -468,9 +502,12 @@ fastc_bc7_status fastc_bc7_compress_device(const fastc_bc7_job *jobs, uint32_t n
   const size_t jb = (n * sizeof(JobDev) + 255) & ~(size_t)255;
   CK(cudaMallocAsync(&buf, jb + scratch_bytes(total, engine), cs));
   cudaError_t e = cudaMemcpyAsync(buf, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs);
+  const int dev = current_device();
+  ClassStreams *cls = engine == FASTC_BC7_ENGINE_PIPELINE ? acquire_class_streams(dev) : nullptr;
   if (e == cudaSuccess)
     e = (cudaError_t)launch_engine(static_cast<const JobDev *>(buf), (int)n, total,
-                                   static_cast<uint8_t *>(buf) + jb, engine, shape, cs);
+                                   static_cast<uint8_t *>(buf) + jb, engine, shape, cls, cs);
+  release_class_streams(dev, cls);
   cudaError_t ef = cudaFreeAsync(buf, cs);
   if (e != cudaSuccess) return fail_cuda(e);
   if (ef != cudaSuccess) return fail_cuda(ef);
@@ -523,18 +560,23 @@ fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
   if (e == cudaSuccess)
     e = cudaMemcpy(p->d_jobs, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  // private side streams: they belong to the capture until it ends
+  ClassStreams cls{};
+  const bool use_cls = p->engine == FASTC_BC7_ENGINE_PIPELINE;
+  if (e == cudaSuccess && use_cls) e = fastc::class_streams_create(&cls);
   if (e == cudaSuccess) {
     p->sc = carve_scratch(p->d_scratch, total);
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
       const int le = launch_engine(p->d_jobs, (int)n, total, p->d_scratch, p->engine,
-                                   pick_shape(total), cs);
+                                   pick_shape(total), use_cls ? &cls : nullptr, cs);
       cudaError_t ee = cudaStreamEndCapture(cs, &p->graph);
       e = le ? (cudaError_t)le : ee;
     }
   }
   if (e == cudaSuccess && !p->graph) e = cudaErrorStreamCaptureInvalidated;
   if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+  fastc::class_streams_destroy(&cls);
   if (cs) cudaStreamDestroy(cs);
   if (e != cudaSuccess) {
     fastc_bc7_plan_destroy(p);

@@ -9,6 +9,7 @@
 #include <string>
 
 #include "bc7_kernels.cuh"
+#include "bc7_pipeline.cuh"
 #include "fastc_bc7.h"
 
 namespace fastc {
@@ -41,8 +42,13 @@ EncodeScratch carve_scratch(void *base, uint64_t total);
 JobDev make_job(const fastc_bc7_job &j, const fastc_bc7_settings &s, uint32_t first,
                 uint32_t count, uint64_t begin);
 uint32_t align_flags(const void *in, const void *out);
+// `cls`: side streams for the pipeline engine's classes (null: one stream).
 int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
-                  LaunchShape shape, cudaStream_t st);
+                  LaunchShape shape, const ClassStreams *cls, cudaStream_t st);
+// Side-stream sets for callers without their own: taken for one enqueue
+// and given back (per device; created on first need).
+ClassStreams *acquire_class_streams(int device);
+void release_class_streams(int device, ClassStreams *cls);
 
 }  // namespace host
 }  // namespace fastc

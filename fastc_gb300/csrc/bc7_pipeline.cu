@@ -386,26 +386,38 @@ __global__ void emit_kernel(uint32_t nb, const uint8_t *__restrict__ counts,
 
 constexpr int kSetupThreads = 128;
 
+// First task of class C in the chunk's class-major task arrays.
+__device__ __forceinline__ uint32_t class_begin(const uint16_t *local, const uint32_t *chunk,
+                                                const PipelineCounters *ctr, uint32_t nb, int c) {
+  return c < kClasses ? scanned(local, chunk, (uint64_t)c * nb) : ctr->tasks;
+}
+
+// One launch per class (the mode is a compile-time constant, so each
+// kernel holds only its own mode's path).
+template <int C>
 __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     const JobDev *__restrict__ jobs, uint32_t nb, const BlockSel *__restrict__ sel,
     const uint2 *__restrict__ desc, const uint16_t *__restrict__ local,
     const uint32_t *__restrict__ chunk, PipelineCounters *__restrict__ ctr,
-    TaskState *__restrict__ state, uint32_t *__restrict__ alist, uint32_t *status) {
+    TaskState *__restrict__ state, AnnealRec *__restrict__ arec, uint32_t *status) {
+  constexpr int kMode = class_mode(C);
+  constexpr ModeAttr kA = mode_attr(kMode);
   __shared__ uint32_t s_px[kSetupThreads * 17];
   __shared__ uint32_t s_pts[16 * kSetupThreads];
   uint32_t *px = s_px + threadIdx.x * 17;
   uint32_t *pts = s_pts + threadIdx.x;
-  const uint32_t ntasks = ctr->tasks;
-  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntasks;
+  const uint32_t begin = class_begin(local, chunk, ctr, nb, C);
+  const uint32_t end = class_begin(local, chunk, ctr, nb, C + 1);
+  const int lane = threadIdx.x & 31;
+  for (uint32_t t = begin + blockIdx.x * blockDim.x + threadIdx.x; t < end;
        t += gridDim.x * blockDim.x) {
     const uint2 d = desc[t];
     const uint32_t gl = d.x;
-    const int cls = (int)(d.y & 0xFF), i = (int)(d.y >> 8);
-    const int mode = class_mode(cls);
+    const int i = (int)(d.y >> 8);
     const BlockSel bs = sel[gl];
     const JobDev &jb = jobs[bs.job];
     const Selection s = sel_of(bs);
-    const Task tk = class_task(s, cls, i);
+    const Task tk = class_task(s, C, i);
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       const uint4 v = load_row_p(jb, bs.lin, r);
@@ -417,8 +429,8 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     const uint32_t bw = jb.width >> 2;
     const uint32_t bx = bs.lin % bw, by = bs.lin / bw;
     ModeCtx m;
-    m.mode = mode;
-    m.a = mode_attr(mode);
+    m.mode = kMode;
+    m.a = kA;
     m.steps = (int)jb.steps;
     m.metric = (int)jb.metric;
     m.rot = tk.rot;
@@ -427,7 +439,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     m.lcg = 0;
     m.sct = g_sct;
     Cluster c;
-    make_cluster(px, part_word_of(s, mode, tk.slot), tk.subset, pts, kSetupThreads, c);
+    make_cluster(px, part_word_of(s, kMode, tk.slot), tk.subset, pts, kSetupThreads, c);
     FitSetup st;
     st.idx = 0;
     st.pbit = 0;
@@ -435,7 +447,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     o.aerr = 0.0;
     o.aidx = 0;
     o.a1 = o.a2 = 0.0f;
-    if (m.a.has_rotation) {
+    if (kA.has_rotation) {
       fit_alpha_setup(m, c, q_opt6, st, o.a1, o.a2, o.aidx, o.aerr);
     } else {
       fit_rgb_setup(m, c, st);
@@ -445,25 +457,32 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     o.p1 = to_pixel(st.p1, 0xFFFFFFFFu, -1);
     o.p2 = to_pixel(st.p2, 0xFFFFFFFFu, -1);
     o.gl = gl;
-    o.mode = (uint8_t)mode;
+    o.mode = (uint8_t)kMode;
     o.slot = (uint8_t)tk.slot;
     o.subset = (uint8_t)tk.subset;
     o.rotim = (uint8_t)((tk.rot << 1) | tk.im);
     o.lcg = fit_seed(jb.seed, bx, by,
-                     (uint32_t)((mode << 8) | (tk.slot << 7) | (tk.subset << 4) | (tk.rot << 1) | tk.im));
+                     (uint32_t)((kMode << 8) | (tk.slot << 7) | (tk.subset << 4) | (tk.rot << 1) | tk.im));
     o.steps = (uint16_t)jb.steps;
     o.pbit = (uint8_t)st.pbit;
     o.flags = (uint8_t)((st.anneal ? kTaskAnneal : 0u) | (jb.metric ? kTaskNonuniform : 0u));
     state[t] = o;
+    // append to the class's annealing list (warp-aggregated)
+    const uint32_t peers = __ballot_sync(__activemask(), st.anneal);
     if (st.anneal) {
-      // append to the class's annealing list (warp-aggregated per class)
-      const uint32_t peers = __match_any_sync(__activemask(), cls);
       const int leader = __ffs(peers) - 1;
-      const int lane = threadIdx.x & 31;
       uint32_t pos = 0;
-      if (lane == leader) pos = atomicAdd(&ctr->anneal_count[cls], (uint32_t)__popc(peers));
+      if (lane == leader) pos = atomicAdd(&ctr->anneal_count[C], (uint32_t)__popc(peers));
       pos = __shfl_sync(peers, pos, leader) + __popc(peers & ((1u << lane) - 1u));
-      alist[scanned(local, chunk, (uint64_t)cls * nb) + pos] = t;
+      uint4 *r = reinterpret_cast<uint4 *>(arec + begin + pos);
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        r[q] = make_uint4(pts[(4 * q + 0) * kSetupThreads], pts[(4 * q + 1) * kSetupThreads],
+                          pts[(4 * q + 2) * kSetupThreads], pts[(4 * q + 3) * kSetupThreads]);
+      r[4] = make_uint4((uint32_t)c.tex, (uint32_t)(c.tex >> 32), o.p1, o.p2);
+      r[5] = make_uint4(__float_as_uint((float)o.err), o.lcg, t,
+                        (uint32_t)o.steps | ((uint32_t)c.n << 16) | ((uint32_t)o.pbit << 24));
+      r[6] = make_uint4((uint32_t)tk.rot | ((uint32_t)o.flags << 8), 0u, 0u, 0u);
     }
   }
 }
@@ -509,11 +528,14 @@ __device__ __forceinline__ uint32_t qpix(const uint8_t *lut, uint32_t v, int pbi
 template <bool kUniform>
 __device__ __forceinline__ float texel_err(uint32_t e, uint32_t pal, const float *w) {
   const uint32_t ad = __vabsdiffu4(e, pal);
-  if (kUniform) return (float)__dp4a(ad, ad, 0u);
-  float ev[4];
+  if constexpr (kUniform) {
+    return (float)__dp4a(ad, ad, 0u);
+  } else {
+    float ev[4];
 #pragma unroll
-  for (int c = 0; c < 4; c++) ev[c] = __fmul_rn((float)((ad >> (8 * c)) & 0xFF), w[c]);
-  return dot4(ev, ev);
+    for (int c = 0; c < 4; c++) ev[c] = __fmul_rn((float)((ad >> (8 * c)) & 0xFF), w[c]);
+    return dot4(ev, ev);
+  }
 }
 
 // QuantizedError (RGBAEndpoints.cpp:190-310) for integer endpoints q1/q2 and
@@ -701,9 +723,8 @@ __device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t *pts, const 
 
 template <int C>
 __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
-    const JobDev *__restrict__ jobs, uint32_t nb, const BlockSel *__restrict__ sel,
-    const uint16_t *__restrict__ local, const uint32_t *__restrict__ chunk,
-    PipelineCounters *__restrict__ ctr, const uint32_t *__restrict__ alist,
+    uint32_t nb, const uint16_t *__restrict__ local, const uint32_t *__restrict__ chunk,
+    PipelineCounters *__restrict__ ctr, const AnnealRec *__restrict__ arec,
     TaskState *__restrict__ state) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr a = mode_attr(kMode);
@@ -737,38 +758,35 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
         if (k >= count) {
           exhausted = true;
         } else {
-          const uint32_t t = alist[base + (uint32_t)k];
-          const TaskState o = state[t];
-          const BlockSel bs = sel[o.gl];
-          const JobDev &jb = jobs[bs.job];
-          const uint32_t part = part_word_of(sel_of(bs), kMode, o.slot);
-          const int rot = o.rotim >> 1;
-          s.t = t;
-          s.p1 = s.b1 = o.p1;
-          s.p2 = s.b2 = o.p2;
-          s.cur_pbit = s.best_pbit = o.pbit;
-          s.cur_err = s.best_err = (float)o.err;
-          s.lcg = o.lcg;
+          const uint4 *r = reinterpret_cast<const uint4 *>(arec + base + (uint32_t)k);
+          uint4 v[7];
+#pragma unroll
+          for (int q = 0; q < 7; q++) v[q] = __ldg(r + q);
+          const int rot = (int)(v[6].x & 0xFF);
+          const uint32_t flags = (v[6].x >> 8) & 0xFF;
+          s.t = v[5].z;
+          s.p1 = s.b1 = v[4].z;
+          s.p2 = s.b2 = v[4].w;
+          s.cur_pbit = s.best_pbit = (int)(v[5].w >> 24);
+          s.cur_err = s.best_err = __uint_as_float(v[5].x);
+          s.lcg = v[5].y;
           s.energy = 0;
-          s.steps = o.steps;
-          s.uniform = !(o.flags & kTaskNonuniform);
+          s.steps = (int)(v[5].w & 0xFFFF);
+          s.n = (int)((v[5].w >> 16) & 0xFF);
+          s.tex = (uint64_t)v[4].x | ((uint64_t)v[4].y << 32);
+          s.uniform = !(flags & kTaskNonuniform);
           ModeCtx m;
           m.a = a;
           m.rot = rot;
           m.metric = s.uniform ? 0 : 1;
           metric_of(m, s.w);
-          int n = 0;
-          uint64_t tex = 0;
 #pragma unroll
-          for (int r = 0; r < 4; r++) {
-            const uint4 v = load_row_p(jb, bs.lin, r);
-            const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
+          for (int q = 0; q < 4; q++) {
+            const uint32_t vv[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
 #pragma unroll
             for (int c = 0; c < 4; c++) {
-              const int ti = r * 4 + c;
-              if ((int)((part >> (2 * ti)) & 3) != o.subset) continue;
               const uint32_t e = vv[c];
-              pts[n * T] = e;
+              pts[(4 * q + c) * T] = e;
               if (kRot) {
                 // the colour fit projects the rotated texel with alpha 255
                 uint32_t pr = e;
@@ -776,14 +794,10 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
                   const uint32_t sh = 8u * (uint32_t)(rot - 1);
                   pr = (pr & ~(0xFFu << sh)) | ((e >> 24) << sh);
                 }
-                proj[n * T] = pr | 0xFF000000u;
+                proj[(4 * q + c) * T] = pr | 0xFF000000u;
               }
-              tex |= (uint64_t)ti << (4 * n);
-              n++;
             }
           }
-          s.n = n;
-          s.tex = tex;
           active = true;
         }
       }
@@ -928,12 +942,77 @@ size_t pipeline_scratch_bytes(uint64_t total_blocks) {
   b += (((n8 + kRankChunk - 1) / kRankChunk) * 4 + 255) & ~255ull;
   b += (tmax * sizeof(uint2) + 255) & ~255ull;
   b += (tmax * sizeof(TaskState) + 255) & ~255ull;
-  b += (tmax * sizeof(uint32_t) + 255) & ~255ull;
+  b += (tmax * sizeof(AnnealRec) + 255) & ~255ull;
   return b;
 }
 
+cudaError_t class_streams_create(ClassStreams *cs) {
+  *cs = ClassStreams{};
+  cudaError_t e = cudaEventCreateWithFlags(&cs->fork, cudaEventDisableTiming);
+  for (int c = 0; c < kClasses && e == cudaSuccess; c++) {
+    e = cudaStreamCreateWithFlags(&cs->side[c], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&cs->join[c], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) class_streams_destroy(cs);
+  return e;
+}
+
+void class_streams_destroy(ClassStreams *cs) {
+  for (int c = 0; c < kClasses; c++) {
+    if (cs->side[c]) cudaStreamDestroy(cs->side[c]);
+    if (cs->join[c]) cudaEventDestroy(cs->join[c]);
+  }
+  if (cs->fork) cudaEventDestroy(cs->fork);
+  *cs = ClassStreams{};
+}
+
+namespace {
+
+struct ChunkArgs {
+  const JobDev *jobs;
+  uint32_t nb;
+  const BlockSel *sel;
+  const uint2 *desc;
+  const uint16_t *local;
+  const uint32_t *chunk;
+  PipelineCounters *ctr;
+  TaskState *state;
+  AnnealRec *arec;
+  uint32_t *status;
+  int sm_count;
+};
+
+template <int C>
+void launch_class(const ChunkArgs &a, cudaStream_t s) {
+  setup_kernel<C><<<a.sm_count * 8, kSetupThreads, 0, s>>>(a.jobs, a.nb, a.sel, a.desc, a.local,
+                                                           a.chunk, a.ctr, a.state, a.arec,
+                                                           a.status);
+  anneal_kernel<C><<<a.sm_count * 8, kAnnealThreads, 0, s>>>(a.nb, a.local, a.chunk, a.ctr,
+                                                             a.arec, a.state);
+}
+
+void launch_class_any(int c, const ChunkArgs &a, cudaStream_t s) {
+  switch (c) {
+    case 0: launch_class<0>(a, s); break;
+    case 1: launch_class<1>(a, s); break;
+    case 2: launch_class<2>(a, s); break;
+    case 3: launch_class<3>(a, s); break;
+    case 4: launch_class<4>(a, s); break;
+    case 5: launch_class<5>(a, s); break;
+    case 6: launch_class<6>(a, s); break;
+    case 7: launch_class<7>(a, s); break;
+    default: launch_class<8>(a, s); break;
+  }
+}
+
+// Classes in the order their work is enqueued: the longest first, so that
+// the short ones fill the tail.
+constexpr int kClassOrder[kClasses] = {6, 7, 5, 4, 3, 1, 8, 2, 0};
+
+}  // namespace
+
 int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
-                    void *scratch, int sm_count, void *stream) {
+                    void *scratch, int sm_count, const ClassStreams *cls, void *stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (total == 0) return 0;
   int e = launch_rank_prepass(jobs, njobs, total, rank, stream);
@@ -955,7 +1034,7 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
   p += ((uint64_t)kMaxBlockTasks * nbmax * sizeof(uint2) + 255) & ~255ull;
   TaskState *state = reinterpret_cast<TaskState *>(p);
   p += ((uint64_t)kMaxBlockTasks * nbmax * sizeof(TaskState) + 255) & ~255ull;
-  uint32_t *alist = reinterpret_cast<uint32_t *>(p);
+  AnnealRec *arec = reinterpret_cast<AnnealRec *>(p);
   for (uint64_t c0 = 0; c0 < total; c0 += cap) {
     const uint32_t nb = (uint32_t)(total - c0 < cap ? total - c0 : cap);
     const uint64_t n8 = (uint64_t)kClasses * nb;
@@ -966,18 +1045,21 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     scan_local_u8_kernel<<<nchunks, kRankChunk, 0, st>>>(counts, n8, local, chunk);
     scan_chunks_kernel<<<1, 1024, 0, st>>>(chunk, nchunks, ctr);
     emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, counts, local, chunk, desc);
-    setup_kernel<<<sm_count * 8, kSetupThreads, 0, st>>>(jobs, nb, sel, desc, local, chunk, ctr,
-                                                         state, alist, rank.status);
-    const int ag = sm_count * 8;
-    anneal_kernel<0><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
-    anneal_kernel<1><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
-    anneal_kernel<2><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
-    anneal_kernel<3><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
-    anneal_kernel<4><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
-    anneal_kernel<5><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
-    anneal_kernel<6><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
-    anneal_kernel<7><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
-    anneal_kernel<8><<<ag, kAnnealThreads, 0, st>>>(jobs, nb, sel, local, chunk, ctr, alist, state);
+    const ChunkArgs args{jobs, nb, sel, desc, local, chunk, ctr, state, arec, rank.status, sm_count};
+    if (cls) {
+      cudaError_t ce = cudaEventRecord(cls->fork, st);
+      for (int c = 0; c < kClasses && ce == cudaSuccess; c++)
+        ce = cudaStreamWaitEvent(cls->side[c], cls->fork, 0);
+      if (ce != cudaSuccess) return (int)ce;
+      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], args, cls->side[kClassOrder[k]]);
+      for (int c = 0; c < kClasses && ce == cudaSuccess; c++) {
+        ce = cudaEventRecord(cls->join[c], cls->side[c]);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(st, cls->join[c], 0);
+      }
+      if (ce != cudaSuccess) return (int)ce;
+    } else {
+      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], args, st);
+    }
     pack_kernel<<<(nb + 127) / 128, 128, 0, st>>>(jobs, nb, sel, local, chunk, state);
     e = (int)cudaPeekAtLastError();
     if (e) return e;

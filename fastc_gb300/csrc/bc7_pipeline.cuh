@@ -1,6 +1,8 @@
 // Data structures of the task-parallel BC7 encoder (bc7_pipeline.cu).
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 #include "bc7_kernels.cuh"
@@ -52,15 +54,44 @@ __host__ __device__ constexpr int class_of(int mode, int im) {
   return mode < 4 ? mode : (mode == 4 ? 4 + im : mode + 1);
 }
 
+// A fit that anneals, as the setup stage hands it to its class's annealing
+// list: everything the loop needs, in one 112-byte record, so that taking
+// the next fit is one atomic and seven 16-byte loads.
+struct __align__(16) AnnealRec {
+  uint32_t pts[16];  // the cluster's texels in texel order (first n used)
+  uint64_t tex;      // texel index of each point, 4 bits per point
+  uint32_t p1, p2;   // starting endpoints (grid values, one byte per channel)
+  float err;         // their QuantizedError
+  uint32_t lcg;      // annealing stream of this fit
+  uint32_t t;        // task index: where the result goes
+  uint16_t steps;
+  uint8_t n, pbit;
+  uint8_t rot, flags, pad[6];
+};
+static_assert(sizeof(AnnealRec) == 112, "AnnealRec layout");
+
 struct PipelineCounters {
   unsigned long long anneal_next[kClasses];  // refill cursors of the annealing lists
   uint32_t anneal_count[kClasses];           // fits of each class that anneal
   uint32_t tasks;                            // tasks in the current chunk
 };
 
+// Side streams that run the classes' setup + annealing concurrently, forked
+// from and joined back into the caller's stream with events (both are
+// recorded into a CUDA graph when the caller's stream is being captured).
+// One set must not be enqueued on by two threads at once.
+struct ClassStreams {
+  cudaStream_t side[kClasses];
+  cudaEvent_t fork;
+  cudaEvent_t join[kClasses];
+};
+cudaError_t class_streams_create(ClassStreams *cs);
+void class_streams_destroy(ClassStreams *cs);
+
 void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t opt6[256]);
 size_t pipeline_scratch_bytes(uint64_t total_blocks);
+// `cls` null: every stage runs in order on `stream`.
 int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
-                    void *scratch, int sm_count, void *stream);
+                    void *scratch, int sm_count, const ClassStreams *cls, void *stream);
 
 }  // namespace fastc

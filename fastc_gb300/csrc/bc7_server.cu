@@ -53,6 +53,7 @@ struct Request {
 
 struct Slot {
   cudaStream_t stream = nullptr;
+  fastc::ClassStreams *cls = nullptr;  // the pipeline's side streams
   void *dev = nullptr;
   uint8_t *pinned = nullptr;
   size_t pinned_cap = 0;
@@ -166,7 +167,8 @@ void fastc_bc7_server_s::launch(Slot &s) {
         std::lock_guard<std::mutex> lk(g_mu);
         shape = pick_shape(total);
       }
-      e = (cudaError_t)launch_engine(dtab, (int)dj.size(), total, scratch, engine, shape, s.stream);
+      e = (cudaError_t)launch_engine(dtab, (int)dj.size(), total, scratch, engine, shape, s.cls,
+                                     s.stream);
     }
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(s.pinned, dout, out_total, cudaMemcpyDeviceToHost, s.stream);
@@ -310,6 +312,7 @@ fastc_bc7_status fastc_bc7_server_create(const fastc_bc7_server_config *cfg,
   s->slots.resize(c.max_inflight);
   for (Slot &sl : s->slots) {
     const cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) sl.cls = acquire_class_streams(dev);
     if (e != cudaSuccess) {
       for (Slot &x : s->slots)
         if (x.stream) cudaStreamDestroy(x.stream);
@@ -480,6 +483,7 @@ fastc_bc7_status fastc_bc7_server_destroy(fastc_bc7_server s) {
       cudaStreamSynchronize(sl.stream);
       cudaStreamDestroy(sl.stream);
     }
+    release_class_streams(s->device, sl.cls);
     if (sl.pinned) cudaFreeHost(sl.pinned);
   }
   delete s;
