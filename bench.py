@@ -369,7 +369,7 @@ def main():
         "batched_equals_plain": bool(identical), "psnr_db": psnr, "device_flags": flags,
         "e2e": {"value": e2e_value, "unit": "MPix/s", "h2d_bytes_per_step": total_px * 4,
                 "d2h_bytes_per_step": total_blocks * 16, "identical_to_device_path": bool(e2e_identical)},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": plan.kernels() * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": (tpb * total_blocks) if tpb else None,

@@ -279,6 +279,10 @@ class Plan:
     def num_blocks(self) -> int:
         return int(load().fastc_bc7_plan_blocks(self._h))
 
+    def kernels(self) -> int:
+        """Kernel launches one launch() makes (kernel nodes of the graph)."""
+        return int(load().fastc_bc7_plan_kernels(self._h))
+
     def launch(self, stream=None) -> None:
         check(load().fastc_bc7_plan_launch(self._h, C.c_void_p(_stream_handle(stream))),
               "fastc_bc7_plan_launch")

@@ -315,6 +315,7 @@ struct fastc_bc7_plan_s {
   int engine = FASTC_BC7_ENGINE_PIPELINE;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  uint64_t kernels = 0;  // kernel nodes of the graph
 };
 
 extern "C" {
@@ -575,6 +576,17 @@ fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
     }
   }
   if (e == cudaSuccess && !p->graph) e = cudaErrorStreamCaptureInvalidated;
+  if (e == cudaSuccess) {
+    size_t nn = 0;
+    e = cudaGraphGetNodes(p->graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (e == cudaSuccess && nn) e = cudaGraphGetNodes(p->graph, nodes.data(), &nn);
+    for (size_t k = 0; k < nn && e == cudaSuccess; k++) {
+      cudaGraphNodeType t;
+      e = cudaGraphNodeGetType(nodes[k], &t);
+      if (t == cudaGraphNodeTypeKernel) p->kernels++;
+    }
+  }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
   fastc::class_streams_destroy(&cls);
   if (cs) cudaStreamDestroy(cs);
@@ -600,6 +612,8 @@ fastc_bc7_status fastc_bc7_plan_flags(fastc_bc7_plan p, uint32_t *flags) {
 }
 
 uint64_t fastc_bc7_plan_blocks(fastc_bc7_plan p) { return p ? p->total : 0; }
+
+uint64_t fastc_bc7_plan_kernels(fastc_bc7_plan p) { return p ? p->kernels : 0; }
 
 fastc_bc7_status fastc_bc7_plan_destroy(fastc_bc7_plan p) {
   if (!p) return FASTC_BC7_OK;

@@ -33,6 +33,7 @@
 #include "bc7_block.cuh"
 #include "bc7_encode.cuh"
 #include "bc7_format.cuh"
+#include "bc7_intqe.cuh"
 #include "bc7_kernels.cuh"
 #include "bc7_pipeline.cuh"
 
@@ -202,13 +203,128 @@ __device__ __forceinline__ uint32_t scanned(const uint16_t *local, const uint32_
 // select
 // ---------------------------------------------------------------------------
 
+// BoxSelection's shape estimate (CP:1626-1655) for the uniform metric in
+// exact integers: the corners of each subset's bounding box are the
+// endpoints of an unquantized QuantizedError over the subset's texels.
+// Loops stay rolled: the select kernel is instruction-fetch bound when the
+// estimate is unrolled.
+template <int kNSub, int kBits>
+__device__ __forceinline__ double estimate_shape_int(const uint32_t *px, uint32_t part,
+                                                     uint32_t *buf, uint2 *pal) {
+  constexpr int T = kLaneStride;
+  double err = 0.0;
+#pragma unroll 1
+  for (int s = 0; s < kNSub; s++) {
+    uint32_t mn = 0xFFFFFFFFu, mx = 0u;
+    int n = 0, se = 0;
+#pragma unroll 4
+    for (int i = 0; i < 16; i++) {
+      const uint32_t e = px[i];
+      if ((int)((part >> (2 * i)) & 3u) == s) {
+        buf[n * T] = e;
+        n++;
+        mn = __vminu4(mn, e);
+        mx = __vmaxu4(mx, e);
+        se += (int)__dp4a(e, e, 0u);
+      }
+    }
+    double e = 0.0;
+    if (mn != mx) {
+      e = 0.0001;
+      uint64_t unused = 0;
+      e = e + (double)qe_smem<kBits, false>(buf, n, 0, se, pal, mn, mx, unused);
+    }
+    err = err + e;
+  }
+  return err;
+}
+
+// The float-metric estimate, kept out of line.
+__device__ __noinline__ double estimate_shape_float(const uint32_t *px, uint32_t part, int nsub,
+                                                    int bits, int metric) {
+  float w[4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) w[c] = base_weight(metric, c);
+  return estimate_shape(px, part, nsub, bits, w);
+}
+
+// One pass of BoxSelection (CP:1670-1750) over the 64 shapes with kNSub
+// subsets, two shapes per lane: the estimates of this lane's shapes.
+template <int kNSub>
+__device__ __forceinline__ void estimate_pair(const uint32_t *px, const uint32_t *part, int metric,
+                                              int lane, uint32_t *buf, uint2 *pal, double &e0,
+                                              double &e1) {
+  constexpr int kBits = kNSub == 2 ? 3 : 2;
+#pragma unroll 1
+  for (int h = 0; h < 2; h++) {
+    const uint32_t pw = part[lane + 32 * h];
+    const double v = metric == 0 ? estimate_shape_int<kNSub, kBits>(px, pw, buf, pal)
+                                 : estimate_shape_float(px, pw, kNSub, kBits, metric);
+    if (h == 0) e0 = v;
+    else e1 = v;
+  }
+}
+
+// BoxSelection with the integer estimate (same result as box_selection_warp).
+__device__ __forceinline__ Selection box_selection_pipe(const uint32_t *px,
+                                                        const uint32_t *part2,
+                                                        const uint32_t *part3, int metric,
+                                                        int lane, uint32_t *buf, uint2 *pal) {
+  Selection r;
+  r.nshapes = 1;
+  r.shape[0] = r.shape[1] = 0;
+  r.nparts[0] = 2;
+  r.nparts[1] = 0;
+  r.modes = 0xFF;
+  bool opaque = true;
+  for (int i = 0; i < 16; i++) opaque = opaque && ((px[i] >> 24) >= 250);
+#pragma unroll
+  for (int pass = 0; pass < 2; pass++) {
+    const int nsub = pass ? 3 : 2;
+    double e0, e1;
+    if (pass) estimate_pair<3>(px, part3, metric, lane, buf, pal, e0, e1);
+    else estimate_pair<2>(px, part2, metric, lane, buf, pal, e0, e1);
+    const uint64_t zero = (uint64_t)__ballot_sync(0xFFFFFFFFu, e0 < 1e-9) |
+                          ((uint64_t)__ballot_sync(0xFFFFFFFFu, e1 < 1e-9) << 32);
+    if (zero) {
+      r.shape[pass] = (uint32_t)(__ffsll((long long)zero) - 1);
+      r.nparts[pass] = (uint32_t)nsub;
+      r.modes = pass ? kModesThree : kModesTwo;
+      return r;
+    }
+    double be = e0;
+    int bi = lane;
+    argmin_pair(be, bi, e1, lane + 32);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+      const double oe = __shfl_xor_sync(0xFFFFFFFFu, be, o);
+      const int oi = __shfl_xor_sync(0xFFFFFFFFu, bi, o);
+      argmin_pair(be, bi, oe, oi);
+    }
+    r.shape[pass] = (uint32_t)bi;
+    r.nparts[pass] = (uint32_t)nsub;
+    if (pass == 0) {
+      if (!opaque) {
+        r.modes &= kModesAlpha;
+        return r;
+      }
+      r.modes &= ~((1u << 4) | (1u << 5));
+      r.nshapes = 2;
+    }
+  }
+  return r;
+}
+
 template <int kWarps>
 __global__ void __launch_bounds__(kWarps * 32) select_kernel(
     const JobDev *__restrict__ jobs, int njobs, uint64_t c0, uint32_t nb,
     const uint16_t *__restrict__ rank_local, const uint32_t *__restrict__ rank_chunk,
     BlockSel *__restrict__ sel, uint8_t *__restrict__ counts, uint32_t *status) {
+  static_assert(kWarps * 32 == kLaneStride, "shared arrays use the lane stride");
   __shared__ uint32_t s_part2[64], s_part3[64];
   __shared__ uint32_t s_px[kWarps][16];
+  __shared__ uint32_t s_buf[16 * kLaneStride];
+  __shared__ uint2 s_pal[8 * kLaneStride];
   for (int i = threadIdx.x; i < 64; i += blockDim.x) {
     s_part2[i] = q_part2[i];
     s_part3[i] = q_part3[i];
@@ -262,7 +378,8 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
       __syncwarp();
       continue;
     }
-    const Selection s = box_selection_warp(px, s_part2, s_part3, (int)jb.metric, lane);
+    const Selection s = box_selection_pipe(px, s_part2, s_part3, (int)jb.metric, lane,
+                                           s_buf + threadIdx.x, s_pal + threadIdx.x);
     uint32_t modes = s.modes & jb.modes;
     if (modes == 0) modes = jb.modes & 0xFF;  // FasTC: undefined behaviour
     const int c = lane < kClasses ? class_task_count(s, modes, lane) : 0;
@@ -492,26 +609,7 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
 // from the class's list
 // ---------------------------------------------------------------------------
 
-constexpr int kAnnealThreads = 128;
-
-// Weight of a `kBits`-bit index (constant divisor).
-template <int kBits>
-__device__ __forceinline__ uint32_t wt(int j) {
-  return (64u * (uint32_t)j + (uint32_t)(((1 << kBits) - 1) / 2)) / (uint32_t)((1 << kBits) - 1);
-}
-
-// d = c + a.h0 * b.b0 + a.h1 * b.b1 (lo) / b.b2, b.b3 (hi); a signed 16-bit
-// pairs, b unsigned bytes.
-__device__ __forceinline__ int dp2a_lo(uint32_t a, uint32_t b, int c) {
-  int d;
-  asm("dp2a.lo.s32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-  return d;
-}
-__device__ __forceinline__ int dp2a_hi(uint32_t a, uint32_t b, int c) {
-  int d;
-  asm("dp2a.hi.s32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-  return d;
-}
+constexpr int kAnnealThreads = kLaneStride;
 
 // ToPixel (RGBAEndpoints.cpp:167-177) of integer endpoints through the table.
 template <int kColorBits, int kAlphaBits>
@@ -636,21 +734,40 @@ struct Lane {
   float cur_err, best_err;
   uint64_t tex;
   float w[4];
+  int se;         // sum of |e|^2 over the fit's texels
+  uint32_t psel;  // byte selector of the projected point (rotation modes)
   bool uniform;
 };
 
-// One iteration of OptimizeEndpointsForCluster's loop (CP:583-624) for
-// class C; returns true when the fit is finished.
-template <int C, bool kUniform>
-__device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t *pts, const uint32_t *proj,
-                                            uint32_t *pal, const uint8_t *lut) {
+// Quantized error of endpoints q1, q2 for class C: integer path for the
+// uniform metric, the float path otherwise.
+template <int C, bool kIdx>
+__device__ __forceinline__ float class_qe(const Lane &s, const uint32_t (&ereg)[16],
+                                          const uint32_t *pts, const uint32_t *proj, uint2 *pal,
+                                          uint32_t *palf, uint32_t q1, uint32_t q2, uint64_t &idx) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr a = mode_attr(kMode);
   constexpr int kBits = class_im(C) ? a.alpha_idx_bits : a.idx_bits;
   constexpr bool kRot = a.has_rotation != 0;
+  constexpr bool kN16 = a.subsets == 1;
+  if (s.uniform) {
+    if constexpr (kN16) return qe_reg<kBits, kRot, kIdx>(ereg, pts, proj, s.psel, s.se, pal, q1, q2, idx);
+    else return qe_smem<kBits, kIdx>(pts, s.n, s.tex, s.se, pal, q1, q2, idx);
+  }
+  // float metric: palette as plain colours in the same buffer
+  return qe_simd<kBits, kRot, false, kIdx>(pts, proj, palf, s.n, q1, q2, s.w, s.tex, idx);
+}
+
+// One iteration of OptimizeEndpointsForCluster's loop (CP:583-624) for
+// class C; returns true when the fit is finished.
+template <int C>
+__device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t (&ereg)[16], const uint32_t *pts,
+                                            const uint32_t *proj, uint2 *pal, uint32_t *palf,
+                                            const uint8_t *lut) {
+  constexpr int kMode = class_mode(C);
+  constexpr ModeAttr a = mode_attr(kMode);
   constexpr bool kHasPbits = a.pbit != kPBitNone;
   if (!(s.best_err > 0.0f && s.energy < s.steps)) return true;
-  const float temp = __fdiv_rn((float)s.energy, (float)(s.steps - 1));
   // PickBestNeighboringEndpoints (CP:426-498) on integer endpoints
   constexpr int sc = 1 << (8 - a.color_bits);
   constexpr int sa = kMode < 4 ? 0 : (1 << (8 - a.alpha_bits));
@@ -692,7 +809,7 @@ __device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t *pts, const 
   const uint32_t q1 = qpix<a.color_bits, a.alpha_bits>(lut, np1, pb_first(pc));
   const uint32_t q2 = qpix<a.color_bits, a.alpha_bits>(lut, np2, pb_second(pc));
   uint64_t unused = 0;
-  const float err = qe_simd<kBits, kRot, kUniform, false>(pts, proj, pal, s.n, q1, q2, s.w, s.tex, unused);
+  const float err = class_qe<C, false>(s, ereg, pts, proj, pal, palf, q1, q2, unused);
   // AcceptNewEndpointError (CP:524-536)
   bool accept = err < s.cur_err;
   if (!accept) {
@@ -700,6 +817,7 @@ __device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t *pts, const 
     const uint32_t mant = (r16 << 8) | (r16 >> 7);
     const float r = __fsub_rn(__uint_as_float((127u << 23) | mant), 1.0f);
     if (r < 1.0f) {
+      const float temp = __fdiv_rn((float)s.energy, (float)(s.steps - 1));
       const float x = __fdiv_rn(__fmul_rn(0.1f, __fsub_rn(s.cur_err, err)), temp);
       accept = mant == 0 ? (x > -745.0f) : (r < portable_expf(x));
     }
@@ -734,16 +852,18 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   __shared__ uint8_t s_lut[8 * 3 * 256];
   __shared__ uint32_t s_pts[16 * T];
   __shared__ uint32_t s_proj[kRot ? 16 * T : 1];
-  __shared__ uint32_t s_pal[(1 << kBits) * T];
+  __shared__ uint2 s_pal[(1 << kBits) * T];
   for (int i = threadIdx.x; i < 8 * 3 * 256; i += blockDim.x) s_lut[i] = (&q_qlut[0][0][0])[i];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   uint32_t *pts = s_pts + threadIdx.x;
   uint32_t *proj = kRot ? s_proj + threadIdx.x : pts;
-  uint32_t *pal = s_pal + threadIdx.x;
+  uint2 *pal = s_pal + threadIdx.x;
+  uint32_t *palf = reinterpret_cast<uint32_t *>(s_pal) + threadIdx.x;  // float-metric palette
   const uint32_t count = ctr->anneal_count[C];
   const uint32_t base = scanned(local, chunk, (uint64_t)C * nb);
   Lane s;
+  uint32_t ereg[16];
   bool active = false, exhausted = false;
   for (;;) {
     const bool need = !active && !exhausted;
@@ -775,46 +895,41 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
           s.n = (int)((v[5].w >> 16) & 0xFF);
           s.tex = (uint64_t)v[4].x | ((uint64_t)v[4].y << 32);
           s.uniform = !(flags & kTaskNonuniform);
+          // projected point: channel rot-1 takes the texel's alpha, alpha is 255
+          s.psel = rot ? (0x4210u & ~(0xFu << (4 * (rot - 1)))) | (3u << (4 * (rot - 1))) : 0x4210u;
           ModeCtx m;
           m.a = a;
           m.rot = rot;
           m.metric = s.uniform ? 0 : 1;
           metric_of(m, s.w);
+          int se = 0;
 #pragma unroll
           for (int q = 0; q < 4; q++) {
             const uint32_t vv[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
 #pragma unroll
             for (int c = 0; c < 4; c++) {
               const uint32_t e = vv[c];
+              ereg[4 * q + c] = e;
+              if (4 * q + c < s.n) se += (int)__dp4a(e, e, 0u);
               pts[(4 * q + c) * T] = e;
-              if (kRot) {
-                // the colour fit projects the rotated texel with alpha 255
-                uint32_t pr = e;
-                if (rot) {
-                  const uint32_t sh = 8u * (uint32_t)(rot - 1);
-                  pr = (pr & ~(0xFFu << sh)) | ((e >> 24) << sh);
-                }
-                proj[(4 * q + c) * T] = pr | 0xFF000000u;
-              }
+              if (kRot) proj[(4 * q + c) * T] = __byte_perm(e, 0xFFFFFFFFu, s.psel);
             }
           }
+          s.se = se;
           active = true;
         }
       }
     }
     if (__all_sync(0xFFFFFFFFu, exhausted && !active)) break;
     if (active) {
-      const bool done = s.uniform ? anneal_step<C, true>(s, pts, proj, pal, s_lut)
-                                  : anneal_step<C, false>(s, pts, proj, pal, s_lut);
-      if (done) {
+      if (anneal_step<C>(s, ereg, pts, proj, pal, palf, s_lut)) {
         // indices of the best endpoints (the same QuantizedError call that
         // found them)
         const int pc = pbit_combo(a, s.best_pbit);
         const uint32_t q1 = qpix<a.color_bits, a.alpha_bits>(s_lut, s.b1, pb_first(pc));
         const uint32_t q2 = qpix<a.color_bits, a.alpha_bits>(s_lut, s.b2, pb_second(pc));
         uint64_t idx = 0;
-        if (s.uniform) qe_simd<kBits, kRot, true, true>(pts, proj, pal, s.n, q1, q2, s.w, s.tex, idx);
-        else qe_simd<kBits, kRot, false, true>(pts, proj, pal, s.n, q1, q2, s.w, s.tex, idx);
+        class_qe<C, true>(s, ereg, pts, proj, pal, palf, q1, q2, idx);
         TaskState &o = state[s.t];
         o.p1 = s.b1;
         o.p2 = s.b2;
@@ -931,11 +1046,13 @@ __global__ void pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
 // launcher
 // ---------------------------------------------------------------------------
 
-size_t pipeline_scratch_bytes(uint64_t total_blocks) {
-  const uint64_t nb = total_blocks < kPipelineChunk ? total_blocks : kPipelineChunk;
+namespace {
+
+// Bytes of one chunk buffer for chunks of at most nb blocks.
+size_t chunk_buffer_bytes(uint64_t nb) {
   const uint64_t n8 = (uint64_t)kClasses * nb;
   const uint64_t tmax = (uint64_t)kMaxBlockTasks * nb;
-  size_t b = 256;
+  size_t b = 256;  // PipelineCounters
   b += (nb * sizeof(BlockSel) + 255) & ~255ull;
   b += (n8 + 255) & ~255ull;
   b += (n8 * 2 + 255) & ~255ull;
@@ -946,23 +1063,67 @@ size_t pipeline_scratch_bytes(uint64_t total_blocks) {
   return b;
 }
 
+struct ChunkBuf {
+  PipelineCounters *ctr;
+  BlockSel *sel;
+  uint8_t *counts;
+  uint16_t *local;
+  uint32_t *chunk;
+  uint2 *desc;
+  TaskState *state;
+  AnnealRec *arec;
+};
+
+ChunkBuf carve_chunk(uint8_t *p, uint64_t nb) {
+  ChunkBuf c;
+  c.ctr = reinterpret_cast<PipelineCounters *>(p);
+  p += 256;
+  c.sel = reinterpret_cast<BlockSel *>(p);
+  p += (nb * sizeof(BlockSel) + 255) & ~255ull;
+  c.counts = p;
+  p += ((uint64_t)kClasses * nb + 255) & ~255ull;
+  c.local = reinterpret_cast<uint16_t *>(p);
+  p += ((uint64_t)kClasses * 2 * nb + 255) & ~255ull;
+  c.chunk = reinterpret_cast<uint32_t *>(p);
+  p += ((((uint64_t)kClasses * nb + kRankChunk - 1) / kRankChunk) * 4 + 255) & ~255ull;
+  c.desc = reinterpret_cast<uint2 *>(p);
+  p += ((uint64_t)kMaxBlockTasks * nb * sizeof(uint2) + 255) & ~255ull;
+  c.state = reinterpret_cast<TaskState *>(p);
+  p += ((uint64_t)kMaxBlockTasks * nb * sizeof(TaskState) + 255) & ~255ull;
+  c.arec = reinterpret_cast<AnnealRec *>(p);
+  return c;
+}
+
+}  // namespace
+
+size_t pipeline_scratch_bytes(uint64_t total_blocks) {
+  const uint64_t nb = total_blocks < kPipelineChunk ? total_blocks : kPipelineChunk;
+  const int nbuf = total_blocks > kPipelineChunk ? 2 : 1;
+  return (size_t)nbuf * chunk_buffer_bytes(nb);
+}
+
 cudaError_t class_streams_create(ClassStreams *cs) {
   *cs = ClassStreams{};
-  cudaError_t e = cudaEventCreateWithFlags(&cs->fork, cudaEventDisableTiming);
-  for (int c = 0; c < kClasses && e == cudaSuccess; c++) {
-    e = cudaStreamCreateWithFlags(&cs->side[c], cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&cs->join[c], cudaEventDisableTiming);
+  cudaError_t e = cudaSuccess;
+  for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+    e = cudaEventCreateWithFlags(&cs->fork[b], cudaEventDisableTiming);
+    for (int c = 0; c < kClasses && e == cudaSuccess; c++)
+      e = cudaEventCreateWithFlags(&cs->join[b][c], cudaEventDisableTiming);
   }
+  for (int c = 0; c < kClasses && e == cudaSuccess; c++)
+    e = cudaStreamCreateWithFlags(&cs->side[c], cudaStreamNonBlocking);
   if (e != cudaSuccess) class_streams_destroy(cs);
   return e;
 }
 
 void class_streams_destroy(ClassStreams *cs) {
-  for (int c = 0; c < kClasses; c++) {
+  for (int c = 0; c < kClasses; c++)
     if (cs->side[c]) cudaStreamDestroy(cs->side[c]);
-    if (cs->join[c]) cudaEventDestroy(cs->join[c]);
+  for (int b = 0; b < 2; b++) {
+    if (cs->fork[b]) cudaEventDestroy(cs->fork[b]);
+    for (int c = 0; c < kClasses; c++)
+      if (cs->join[b][c]) cudaEventDestroy(cs->join[b][c]);
   }
-  if (cs->fork) cudaEventDestroy(cs->fork);
   *cs = ClassStreams{};
 }
 
@@ -982,13 +1143,25 @@ struct ChunkArgs {
   int sm_count;
 };
 
+// Resident CTAs per SM of a kernel (queried once per process; the kernels
+// are the same on every device of one architecture).
+template <typename K>
+int resident_ctas(K kernel, int threads) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0) != cudaSuccess || n < 1)
+    n = 1;
+  return n;
+}
+
 template <int C>
 void launch_class(const ChunkArgs &a, cudaStream_t s) {
+  // the annealing kernel is persistent: no more CTAs than can be resident
+  static const int anneal_per_sm = resident_ctas(anneal_kernel<C>, kAnnealThreads);
   setup_kernel<C><<<a.sm_count * 8, kSetupThreads, 0, s>>>(a.jobs, a.nb, a.sel, a.desc, a.local,
                                                            a.chunk, a.ctr, a.state, a.arec,
                                                            a.status);
-  anneal_kernel<C><<<a.sm_count * 8, kAnnealThreads, 0, s>>>(a.nb, a.local, a.chunk, a.ctr,
-                                                             a.arec, a.state);
+  anneal_kernel<C><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(a.nb, a.local, a.chunk,
+                                                                         a.ctr, a.arec, a.state);
 }
 
 void launch_class_any(int c, const ChunkArgs &a, cudaStream_t s) {
@@ -1011,6 +1184,11 @@ constexpr int kClassOrder[kClasses] = {6, 7, 5, 4, 3, 1, 8, 2, 0};
 
 }  // namespace
 
+// Stage order on the caller's stream `st` for chunks 0, 1, 2, ...:
+//   select(0) fork(0) | select(1) fork(1) join(0) pack(0) | select(2) ...
+// fork(i) starts chunk i's classes on the side streams, join(i) waits for
+// them; chunk i uses buffer i % 2, which select(i) may only overwrite after
+// pack(i - 2), earlier on `st`.
 int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
                     void *scratch, int sm_count, const ClassStreams *cls, void *stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -1018,52 +1196,59 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
   int e = launch_rank_prepass(jobs, njobs, total, rank, stream);
   if (e) return e;
   const uint64_t cap = kPipelineChunk;
-  uint8_t *p = static_cast<uint8_t *>(scratch);
-  PipelineCounters *ctr = reinterpret_cast<PipelineCounters *>(p);
-  p += 256;
   const uint64_t nbmax = total < cap ? total : cap;
-  BlockSel *sel = reinterpret_cast<BlockSel *>(p);
-  p += (nbmax * sizeof(BlockSel) + 255) & ~255ull;
-  uint8_t *counts = p;
-  p += ((uint64_t)kClasses * nbmax + 255) & ~255ull;
-  uint16_t *local = reinterpret_cast<uint16_t *>(p);
-  p += ((uint64_t)kClasses * 2 * nbmax + 255) & ~255ull;
-  uint32_t *chunk = reinterpret_cast<uint32_t *>(p);
-  p += ((((uint64_t)kClasses * nbmax + kRankChunk - 1) / kRankChunk) * 4 + 255) & ~255ull;
-  uint2 *desc = reinterpret_cast<uint2 *>(p);
-  p += ((uint64_t)kMaxBlockTasks * nbmax * sizeof(uint2) + 255) & ~255ull;
-  TaskState *state = reinterpret_cast<TaskState *>(p);
-  p += ((uint64_t)kMaxBlockTasks * nbmax * sizeof(TaskState) + 255) & ~255ull;
-  AnnealRec *arec = reinterpret_cast<AnnealRec *>(p);
-  for (uint64_t c0 = 0; c0 < total; c0 += cap) {
+  ChunkBuf bufs[2];
+  bufs[0] = carve_chunk(static_cast<uint8_t *>(scratch), nbmax);
+  bufs[1] = total > cap ? carve_chunk(static_cast<uint8_t *>(scratch) + chunk_buffer_bytes(nbmax), nbmax)
+                        : bufs[0];
+  auto pack = [&](const ChunkBuf &b, uint32_t nb, int parity) -> int {
+    if (cls) {
+      for (int c = 0; c < kClasses; c++) {
+        const cudaError_t ce = cudaStreamWaitEvent(st, cls->join[parity][c], 0);
+        if (ce != cudaSuccess) return (int)ce;
+      }
+    }
+    pack_kernel<<<(nb + 127) / 128, 128, 0, st>>>(jobs, nb, b.sel, b.local, b.chunk, b.state);
+    return (int)cudaPeekAtLastError();
+  };
+  uint32_t prev_nb = 0;
+  int i = 0;
+  for (uint64_t c0 = 0; c0 < total; c0 += cap, i++) {
+    const ChunkBuf &b = bufs[i & 1];
     const uint32_t nb = (uint32_t)(total - c0 < cap ? total - c0 : cap);
     const uint64_t n8 = (uint64_t)kClasses * nb;
     const uint32_t nchunks = (uint32_t)((n8 + kRankChunk - 1) / kRankChunk);
     const int sel_ctas = (int)((nb + 3) / 4 < (uint64_t)sm_count * 16 ? (nb + 3) / 4 : (uint64_t)sm_count * 16);
     select_kernel<4><<<sel_ctas, 128, 0, st>>>(jobs, njobs, c0, nb, rank.rank_local, rank.chunk_prefix,
-                                               sel, counts, rank.status);
-    scan_local_u8_kernel<<<nchunks, kRankChunk, 0, st>>>(counts, n8, local, chunk);
-    scan_chunks_kernel<<<1, 1024, 0, st>>>(chunk, nchunks, ctr);
-    emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, counts, local, chunk, desc);
-    const ChunkArgs args{jobs, nb, sel, desc, local, chunk, ctr, state, arec, rank.status, sm_count};
+                                               b.sel, b.counts, rank.status);
+    scan_local_u8_kernel<<<nchunks, kRankChunk, 0, st>>>(b.counts, n8, b.local, b.chunk);
+    scan_chunks_kernel<<<1, 1024, 0, st>>>(b.chunk, nchunks, b.ctr);
+    emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, b.counts, b.local, b.chunk, b.desc);
+    const ChunkArgs args{jobs, nb, b.sel, b.desc, b.local, b.chunk, b.ctr, b.state, b.arec,
+                         rank.status, sm_count};
     if (cls) {
-      cudaError_t ce = cudaEventRecord(cls->fork, st);
+      cudaError_t ce = cudaEventRecord(cls->fork[i & 1], st);
       for (int c = 0; c < kClasses && ce == cudaSuccess; c++)
-        ce = cudaStreamWaitEvent(cls->side[c], cls->fork, 0);
+        ce = cudaStreamWaitEvent(cls->side[c], cls->fork[i & 1], 0);
       if (ce != cudaSuccess) return (int)ce;
       for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], args, cls->side[kClassOrder[k]]);
-      for (int c = 0; c < kClasses && ce == cudaSuccess; c++) {
-        ce = cudaEventRecord(cls->join[c], cls->side[c]);
-        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(st, cls->join[c], 0);
-      }
+      for (int c = 0; c < kClasses && ce == cudaSuccess; c++)
+        ce = cudaEventRecord(cls->join[i & 1][c], cls->side[c]);
       if (ce != cudaSuccess) return (int)ce;
+      if (i > 0) {
+        e = pack(bufs[(i - 1) & 1], prev_nb, (i - 1) & 1);
+        if (e) return e;
+      }
     } else {
       for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], args, st);
+      e = pack(b, nb, 0);
+      if (e) return e;
     }
-    pack_kernel<<<(nb + 127) / 128, 128, 0, st>>>(jobs, nb, sel, local, chunk, state);
     e = (int)cudaPeekAtLastError();
     if (e) return e;
+    prev_nb = nb;
   }
+  if (cls) return pack(bufs[(i - 1) & 1], prev_nb, (i - 1) & 1);
   return 0;
 }
 

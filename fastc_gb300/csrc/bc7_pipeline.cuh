@@ -9,7 +9,9 @@
 
 namespace fastc {
 
-// Blocks per pipeline chunk; scratch grows with it.
+// Blocks per pipeline chunk; scratch grows with it. Launches of more than
+// one chunk use two scratch buffers so that the select stage of a chunk
+// runs while the previous chunk anneals.
 constexpr uint64_t kPipelineChunk = 256 * 1024;
 // Cluster fits one block can need. BC7's mode table caps it at 32 (opaque
 // block whose selection falls back to the caller's mask of modes 1,3-7).
@@ -82,8 +84,8 @@ struct PipelineCounters {
 // One set must not be enqueued on by two threads at once.
 struct ClassStreams {
   cudaStream_t side[kClasses];
-  cudaEvent_t fork;
-  cudaEvent_t join[kClasses];
+  cudaEvent_t fork[2];            // per scratch buffer (chunks alternate)
+  cudaEvent_t join[2][kClasses];
 };
 cudaError_t class_streams_create(ClassStreams *cs);
 void class_streams_destroy(ClassStreams *cs);

@@ -206,6 +206,9 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_launch(fastc_bc7_plan plan, void *
  * loop reached its iteration bound). Synchronises with the plan's work. */
 FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_flags(fastc_bc7_plan plan, uint32_t *flags);
 FASTC_BC7_API uint64_t fastc_bc7_plan_blocks(fastc_bc7_plan plan);
+/* Kernel launches one fastc_bc7_plan_launch makes (kernel nodes of the
+ * captured graph). */
+FASTC_BC7_API uint64_t fastc_bc7_plan_kernels(fastc_bc7_plan plan);
 FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_destroy(fastc_bc7_plan plan);
 
 /* --- Request server: continuous batching under a device-memory budget. ---
