@@ -923,19 +923,13 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
     if (__all_sync(0xFFFFFFFFu, exhausted && !active)) break;
     if (active) {
       if (anneal_step<C>(s, ereg, pts, proj, pal, palf, s_lut)) {
-        // indices of the best endpoints (the same QuantizedError call that
-        // found them)
-        const int pc = pbit_combo(a, s.best_pbit);
-        const uint32_t q1 = qpix<a.color_bits, a.alpha_bits>(s_lut, s.b1, pb_first(pc));
-        const uint32_t q2 = qpix<a.color_bits, a.alpha_bits>(s_lut, s.b2, pb_second(pc));
-        uint64_t idx = 0;
-        class_qe<C, true>(s, ereg, pts, proj, pal, palf, q1, q2, idx);
+        // the indices of the best endpoints are recomputed by the pack
+        // stage for the fits that win their block
         TaskState &o = state[s.t];
         o.p1 = s.b1;
         o.p2 = s.b2;
         o.pbit = (uint8_t)s.best_pbit;
         o.err = (double)s.best_err;
-        o.idx = idx;
         active = false;
       }
     }
@@ -960,18 +954,86 @@ __device__ __forceinline__ void fit_out_of(const TaskState &o, FitOut &f) {
   f.pbit = o.pbit;
 }
 
-__global__ void pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
+// Colour indices of an annealed fit at its best endpoints: the
+// QuantizedError call that ends OptimizeEndpointsForCluster (CP:626-629),
+// run by the pack stage for winning fits only. px: the block's 16 texels,
+// thread-private, stride kLaneStride.
+template <int C>
+__device__ __noinline__ uint64_t fit_indices(const TaskState &o, const uint32_t *px, uint32_t part,
+                                             const uint8_t *lut, uint32_t *pts, uint32_t *proj,
+                                             uint2 *pal, uint32_t *palf) {
+  constexpr int kMode = class_mode(C);
+  constexpr ModeAttr a = mode_attr(kMode);
+  constexpr bool kRot = a.has_rotation != 0;
+  constexpr int T = kLaneStride;
+  Lane s;
+  const int rot = o.rotim >> 1;
+  s.uniform = !(o.flags & kTaskNonuniform);
+  s.psel = rot ? (0x4210u & ~(0xFu << (4 * (rot - 1)))) | (3u << (4 * (rot - 1))) : 0x4210u;
+  ModeCtx m;
+  m.a = a;
+  m.rot = rot;
+  m.metric = s.uniform ? 0 : 1;
+  metric_of(m, s.w);
+  uint32_t ereg[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) ereg[k] = px[k * T];
+  int n = 0, se = 0;
+  uint64_t tex = 0;
+  for (int i = 0; i < 16; i++) {
+    if ((int)((part >> (2 * i)) & 3u) != o.subset) continue;
+    const uint32_t e = px[i * T];
+    pts[n * T] = e;
+    if (kRot) proj[n * T] = __byte_perm(e, 0xFFFFFFFFu, s.psel);
+    tex |= (uint64_t)i << (4 * n);
+    se += (int)__dp4a(e, e, 0u);
+    n++;
+  }
+  s.n = n;
+  s.tex = tex;
+  s.se = se;
+  const int pc = pbit_combo(a, o.pbit);
+  const uint32_t q1 = qpix<a.color_bits, a.alpha_bits>(lut, o.p1, pb_first(pc));
+  const uint32_t q2 = qpix<a.color_bits, a.alpha_bits>(lut, o.p2, pb_second(pc));
+  uint64_t idx = 0;
+  class_qe<C, true>(s, ereg, pts, proj, pal, palf, q1, q2, idx);
+  return idx;
+}
+
+__device__ __forceinline__ uint64_t fit_indices_any(int c, const TaskState &o, const uint32_t *px,
+                                                    uint32_t part, const uint8_t *lut, uint32_t *pts,
+                                                    uint32_t *proj, uint2 *pal, uint32_t *palf) {
+  switch (c) {
+    case 0: return fit_indices<0>(o, px, part, lut, pts, proj, pal, palf);
+    case 1: return fit_indices<1>(o, px, part, lut, pts, proj, pal, palf);
+    case 2: return fit_indices<2>(o, px, part, lut, pts, proj, pal, palf);
+    case 3: return fit_indices<3>(o, px, part, lut, pts, proj, pal, palf);
+    case 4: return fit_indices<4>(o, px, part, lut, pts, proj, pal, palf);
+    case 5: return fit_indices<5>(o, px, part, lut, pts, proj, pal, palf);
+    case 6: return fit_indices<6>(o, px, part, lut, pts, proj, pal, palf);
+    case 7: return fit_indices<7>(o, px, part, lut, pts, proj, pal, palf);
+    default: return fit_indices<8>(o, px, part, lut, pts, proj, pal, palf);
+  }
+}
+
+constexpr int kPackThreads = kLaneStride;
+
+__global__ void __launch_bounds__(kPackThreads) pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
                             const BlockSel *__restrict__ sel, const uint16_t *__restrict__ local,
                             const uint32_t *__restrict__ chunk,
                             const TaskState *__restrict__ state) {
   __shared__ uint32_t s_part2[64], s_part3[64];
   __shared__ uint8_t s_anc2[64], s_anc3[64];
+  __shared__ uint8_t s_lut[8 * 3 * 256];
+  __shared__ uint32_t s_px[16 * kPackThreads], s_pts[16 * kPackThreads], s_proj[16 * kPackThreads];
+  __shared__ uint2 s_pal[16 * kPackThreads];
   for (int i = threadIdx.x; i < 64; i += blockDim.x) {
     s_part2[i] = q_part2[i];
     s_part3[i] = q_part3[i];
     s_anc2[i] = q_anchor2[i];
     s_anc3[i] = q_anchor3[i];
   }
+  for (int i = threadIdx.x; i < 8 * 3 * 256; i += blockDim.x) s_lut[i] = (&q_qlut[0][0][0])[i];
   __syncthreads();
   const uint32_t gl = blockIdx.x * blockDim.x + threadIdx.x;
   if (gl >= nb) return;
@@ -1036,7 +1098,24 @@ __global__ void pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
   } else {
     FitOut f[3];
     const int ns = mode_attr(best_mode).subsets;
-    for (int k = 0; k < ns; k++) fit_out_of(state[best_first + k], f[k]);
+    const uint32_t part = part_word_of(s, best_mode, best_slot);
+    uint32_t *px = s_px + threadIdx.x;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const uint4 v = load_row_p(jb, bs.lin, r);
+      px[(4 * r + 0) * kPackThreads] = v.x;
+      px[(4 * r + 1) * kPackThreads] = v.y;
+      px[(4 * r + 2) * kPackThreads] = v.z;
+      px[(4 * r + 3) * kPackThreads] = v.w;
+    }
+    for (int k = 0; k < ns; k++) {
+      const TaskState o = state[best_first + k];
+      fit_out_of(o, f[k]);
+      if (o.flags & kTaskAnneal)
+        f[k].idx = fit_indices_any(class_of(o.mode, o.rotim & 1), o, px, part, s_lut,
+                                   s_pts + threadIdx.x, s_proj + threadIdx.x, s_pal + threadIdx.x,
+                                   reinterpret_cast<uint32_t *>(s_pal) + threadIdx.x);
+    }
     pack_block(best_mode, s, best_slot, f, s_anc2, s_anc3, s_part2, s_part3, best_rot, best_im, out);
   }
   store_block_p(jb, bs.lin, out);
@@ -1110,15 +1189,17 @@ cudaError_t class_streams_create(ClassStreams *cs) {
     for (int c = 0; c < kClasses && e == cudaSuccess; c++)
       e = cudaEventCreateWithFlags(&cs->join[b][c], cudaEventDisableTiming);
   }
-  for (int c = 0; c < kClasses && e == cudaSuccess; c++)
-    e = cudaStreamCreateWithFlags(&cs->side[c], cudaStreamNonBlocking);
+  for (int b = 0; b < 2 && e == cudaSuccess; b++)
+    for (int c = 0; c < kClasses && e == cudaSuccess; c++)
+      e = cudaStreamCreateWithFlags(&cs->side[b][c], cudaStreamNonBlocking);
   if (e != cudaSuccess) class_streams_destroy(cs);
   return e;
 }
 
 void class_streams_destroy(ClassStreams *cs) {
-  for (int c = 0; c < kClasses; c++)
-    if (cs->side[c]) cudaStreamDestroy(cs->side[c]);
+  for (int b = 0; b < 2; b++)
+    for (int c = 0; c < kClasses; c++)
+      if (cs->side[b][c]) cudaStreamDestroy(cs->side[b][c]);
   for (int b = 0; b < 2; b++) {
     if (cs->fork[b]) cudaEventDestroy(cs->fork[b]);
     for (int c = 0; c < kClasses; c++)
@@ -1208,7 +1289,8 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
         if (ce != cudaSuccess) return (int)ce;
       }
     }
-    pack_kernel<<<(nb + 127) / 128, 128, 0, st>>>(jobs, nb, b.sel, b.local, b.chunk, b.state);
+    pack_kernel<<<(nb + kPackThreads - 1) / kPackThreads, kPackThreads, 0, st>>>(jobs, nb, b.sel, b.local,
+                                                                              b.chunk, b.state);
     return (int)cudaPeekAtLastError();
   };
   uint32_t prev_nb = 0;
@@ -1228,12 +1310,13 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
                          rank.status, sm_count};
     if (cls) {
       cudaError_t ce = cudaEventRecord(cls->fork[i & 1], st);
+      const cudaStream_t *side = cls->side[i & 1];
       for (int c = 0; c < kClasses && ce == cudaSuccess; c++)
-        ce = cudaStreamWaitEvent(cls->side[c], cls->fork[i & 1], 0);
+        ce = cudaStreamWaitEvent(side[c], cls->fork[i & 1], 0);
       if (ce != cudaSuccess) return (int)ce;
-      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], args, cls->side[kClassOrder[k]]);
+      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], args, side[kClassOrder[k]]);
       for (int c = 0; c < kClasses && ce == cudaSuccess; c++)
-        ce = cudaEventRecord(cls->join[i & 1][c], cls->side[c]);
+        ce = cudaEventRecord(cls->join[i & 1][c], side[c]);
       if (ce != cudaSuccess) return (int)ce;
       if (i > 0) {
         e = pack(bufs[(i - 1) & 1], prev_nb, (i - 1) & 1);

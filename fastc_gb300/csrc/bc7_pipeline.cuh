@@ -82,9 +82,11 @@ struct PipelineCounters {
 // from and joined back into the caller's stream with events (both are
 // recorded into a CUDA graph when the caller's stream is being captured).
 // One set must not be enqueued on by two threads at once.
+// Chunks alternate between two sets, so that a class of chunk i + 1 starts
+// while the same class of chunk i drains.
 struct ClassStreams {
-  cudaStream_t side[kClasses];
-  cudaEvent_t fork[2];            // per scratch buffer (chunks alternate)
+  cudaStream_t side[2][kClasses];
+  cudaEvent_t fork[2];
   cudaEvent_t join[2][kClasses];
 };
 cudaError_t class_streams_create(ClassStreams *cs);
