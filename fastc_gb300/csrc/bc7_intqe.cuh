@@ -38,24 +38,34 @@ __device__ __forceinline__ int dp2a_hi(uint32_t a, uint32_t b, int c) {
 // indices either side of its projection) share |e|^2, so comparing
 // |c|^2 - 2 e.c picks the same index, and the totals are the same integers.
 
-// Palette of the interpolated colours with their squared lengths.
+// Palette entry j holds colour j and colour j + 1 with their squared
+// lengths, (c_j, |c_j|^2, c_j+1, |c_j+1|^2), so one 16-byte load serves both
+// candidates; the last entry repeats its colour.
 template <int kBits>
-__device__ __forceinline__ void palette_sq(uint32_t q1, uint32_t q2, uint2 *pal) {
+__device__ __forceinline__ void palette_sq(uint32_t q1, uint32_t q2, uint4 *pal) {
   constexpr int T = kLaneStride;
+  constexpr int kN = 1 << kBits;
   const uint32_t rb1 = q1 & 0x00FF00FFu, ga1 = (q1 >> 8) & 0x00FF00FFu;
   const uint32_t rb2 = q2 & 0x00FF00FFu, ga2 = (q2 >> 8) & 0x00FF00FFu;
+  uint32_t prev = 0, prev_sq = 0;
 #pragma unroll
-  for (int j = 0; j < (1 << kBits); j++) {
+  for (int j = 0; j < kN; j++) {
     const uint32_t w1 = wt<kBits>(j), w0 = 64u - w1;
     const uint32_t vrb = rb1 * w0 + rb2 * w1 + 0x00200020u;
     const uint32_t vga = ga1 * w0 + ga2 * w1 + 0x00200020u;
     const uint32_t c = ((vrb >> 6) & 0x00FF00FFu) | (((vga >> 6) & 0x00FF00FFu) << 8);
-    pal[j * T] = make_uint2(c, __dp4a(c, c, 0u));
+    const uint32_t sq = __dp4a(c, c, 0u);
+    if (j > 0) pal[(j - 1) * T] = make_uint4(prev, prev_sq, c, sq);
+    if (j == kN - 1) pal[j * T] = make_uint4(c, sq, c, sq);
+    prev = c;
+    prev_sq = sq;
   }
 }
 
 // The projection onto q2 - q1: D = (p - q1).(q2 - q1) by two dp2a, and
-// floor(D k / L) by a multiply-high with R = ceil(2^32 / L).
+// floor(D k / L) by a multiply-high with R = floor((2^32 - 1) / L) + 1,
+// which never undershoots and overshoots by at most one (never when D k is
+// a multiple of L).
 struct Proj {
   uint32_t dlo, dhi, R;
   int negk, L;
@@ -77,78 +87,39 @@ __device__ __forceinline__ Proj make_proj(uint32_t q1, uint32_t q2) {
   return pj;
 }
 
-// The two palette indices FasTC compares for projected point p (j1 == j2
-// when the projection is clamped or lands on an index), without branches.
-// Returns true in the rare case that needs FasTC's float arithmetic (D k a
-// multiple of L strictly inside the segment); the indices are then those of
-// the exact quotient and float_pair() gives the right ones.
+// The candidates FasTC compares for projected point p: j1 = floor(D k / L)
+// clamped to [0, k], and j1 + 1 unless D k / L is an integer or clamped.
+// FasTC computes the quotient in float, fl(fl(D / L) k); where D k is a
+// multiple of L, D / L is exactly j / k, and fl(fl(j / k) k) == j for every
+// j < k in {3, 7, 15} (checked exhaustively in the tests), so the integer
+// quotient always reproduces FasTC's two indices.
 template <int kBits>
-__device__ __forceinline__ bool nearest_pair(const Proj &pj, uint32_t p, int &j1, int &j2, int &D) {
-  constexpr uint32_t km = (1u << kBits) - 1u;
-  D = dp2a_hi(pj.dhi, p, dp2a_lo(pj.dlo, p, pj.negk));
-  const uint32_t num = (uint32_t)max(D, 0) * km;
-  uint32_t q = __umulhi(num, pj.R);
-  int r = (int)(num - q * (uint32_t)pj.L);
-  q = r < 0 ? q - 1u : q;
-  r = r < 0 ? r + pj.L : r;
-  const bool over = D >= pj.L;
-  q = over ? km : q;
-  r = over ? 0 : r;
-  j1 = (int)q;
-  j2 = (int)q + (r != 0 ? 1 : 0);
-  return (r == 0) & (D > 0) & !over;
-}
-
-// FasTC's float division and product for the case nearest_pair() flags.
-template <int kBits>
-__device__ __noinline__ void float_pair(int D, int L, int &j1, int &j2) {
+__device__ __forceinline__ int nearest_pair(const Proj &pj, uint32_t p, bool &two) {
   constexpr int km = (1 << kBits) - 1;
-  const float sc = __fmul_rn(__fdiv_rn((float)D, (float)L), (float)km);
-  j1 = min(max(0, __float2int_rz(floorf(sc))), km);
-  j2 = min(__float2int_rz(ceilf(sc)), km);
+  const int D = dp2a_hi(pj.dhi, p, dp2a_lo(pj.dlo, p, pj.negk));
+  const uint32_t num = (uint32_t)max(D, 0) * (uint32_t)km;
+  const uint32_t q = __umulhi(num, pj.R);
+  const int r = (int)(num - q * (uint32_t)pj.L);
+  const bool over = D >= pj.L;
+  two = (r != 0) & !over;
+  return over ? km : (int)q - (r < 0 ? 1 : 0);
 }
 
-// |c|^2 - 2 e.c of the better of candidates j1, j2, and its index.
-__device__ __forceinline__ int pair_term(uint32_t e, const uint2 *pal, int j1, int j2, int &bj) {
+// |c|^2 - 2 e.c of the better candidate, and its index.
+__device__ __forceinline__ int pair_term(uint32_t e, const uint4 *pal, int j1, bool two, int &bj) {
   constexpr int T = kLaneStride;
-  const uint2 a1 = pal[j1 * T], a2 = pal[j2 * T];
-  const int t1 = (int)a1.y - 2 * (int)__dp4a(e, a1.x, 0u);
-  const int t2 = (int)a2.y - 2 * (int)__dp4a(e, a2.x, 0u);
-  const bool second = t2 < t1;
-  bj = second ? j2 : j1;
+  const uint4 a = pal[j1 * T];
+  const int t1 = (int)a.y - 2 * (int)__dp4a(e, a.x, 0u);
+  const int t2 = (int)a.w - 2 * (int)__dp4a(e, a.z, 0u);
+  const bool second = two & (t2 < t1);
+  bj = j1 + (second ? 1 : 0);
   return second ? t2 : t1;
 }
 
-// Redo the flagged texels (bit k of `mask`: point k) with the float indices.
-// pts holds the points, proj (if kRot) the projected points.
-template <int kBits, bool kRot, bool kIdx>
-__device__ __forceinline__ void fix_exact(uint32_t mask, const uint32_t *pts, const uint32_t *proj,
-                                          uint64_t tex, const Proj &pj, const uint2 *pal, int &acc,
-                                          uint64_t &idx) {
-  constexpr int T = kLaneStride;
-  while (mask) {
-    const int k = __ffs(mask) - 1;
-    mask &= mask - 1;
-    const uint32_t e = pts[k * T];
-    const uint32_t p = kRot ? proj[k * T] : e;
-    int j1, j2, D, bj;
-    nearest_pair<kBits>(pj, p, j1, j2, D);
-    const int old = pair_term(e, pal, j1, j2, bj);
-    float_pair<kBits>(D, pj.L, j1, j2);
-    acc += pair_term(e, pal, j1, j2, bj) - old;
-    if (kIdx) {
-      const int t = (int)((tex >> (4 * k)) & 15);
-      idx = (idx & ~(0xFull << (4 * t))) | ((uint64_t)bj << (4 * t));
-    }
-  }
-}
-
-// Sixteen texels in registers (one-subset modes; texel k is point k); the
-// same points are in pts/proj (shared memory) for the rare fix-up.
+// Sixteen texels in registers (one-subset modes; texel k is point k).
 // `psel` builds the projected point of the rotation modes from the texel.
 template <int kBits, bool kRot, bool kIdx>
-__device__ __forceinline__ float qe_reg(const uint32_t (&e)[16], const uint32_t *pts,
-                                        const uint32_t *proj, uint32_t psel, int se, uint2 *pal,
+__device__ __forceinline__ float qe_reg(const uint32_t (&e)[16], uint32_t psel, int se, uint4 *pal,
                                         uint32_t q1, uint32_t q2, uint64_t &idx) {
   const Proj pj = make_proj(q1, q2);
   int acc = 0;
@@ -159,23 +130,22 @@ __device__ __forceinline__ float qe_reg(const uint32_t (&e)[16], const uint32_t 
     return (float)(se + acc);
   }
   palette_sq<kBits>(q1, q2, pal);
-  uint32_t mask = 0;
 #pragma unroll
   for (int k = 0; k < 16; k++) {
     const uint32_t p = kRot ? __byte_perm(e[k], 0xFFFFFFFFu, psel) : e[k];
-    int j1, j2, D, bj;
-    mask |= (uint32_t)nearest_pair<kBits>(pj, p, j1, j2, D) << k;
-    acc += pair_term(e[k], pal, j1, j2, bj);
+    bool two;
+    const int j1 = nearest_pair<kBits>(pj, p, two);
+    int bj;
+    acc += pair_term(e[k], pal, j1, two, bj);
     if (kIdx) idx |= (uint64_t)bj << (4 * k);
   }
-  if (mask) fix_exact<kBits, kRot, kIdx>(mask, pts, proj, 0xFEDCBA9876543210ull, pj, pal, acc, idx);
   return (float)(se + acc);
 }
 
 // n texels from shared memory (multi-subset modes), texel ids in `tex`.
 template <int kBits, bool kIdx>
 __device__ __forceinline__ float qe_smem(const uint32_t *pts, int n, uint64_t tex, int se,
-                                         uint2 *pal, uint32_t q1, uint32_t q2, uint64_t &idx) {
+                                         uint4 *pal, uint32_t q1, uint32_t q2, uint64_t &idx) {
   constexpr int T = kLaneStride;
   const Proj pj = make_proj(q1, q2);
   int acc = 0;
@@ -185,16 +155,15 @@ __device__ __forceinline__ float qe_smem(const uint32_t *pts, int n, uint64_t te
     return (float)(se + acc);
   }
   palette_sq<kBits>(q1, q2, pal);
-  uint32_t mask = 0;
 #pragma unroll 4
   for (int k = 0; k < n; k++) {
     const uint32_t e = pts[k * T];
-    int j1, j2, D, bj;
-    mask |= (uint32_t)nearest_pair<kBits>(pj, e, j1, j2, D) << k;
-    acc += pair_term(e, pal, j1, j2, bj);
+    bool two;
+    const int j1 = nearest_pair<kBits>(pj, e, two);
+    int bj;
+    acc += pair_term(e, pal, j1, two, bj);
     if (kIdx) idx |= (uint64_t)bj << (4 * ((tex >> (4 * k)) & 15));
   }
-  if (mask) fix_exact<kBits, false, kIdx>(mask, pts, pts, tex, pj, pal, acc, idx);
   return (float)(se + acc);
 }
 

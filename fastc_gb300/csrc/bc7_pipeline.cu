@@ -87,6 +87,8 @@ static uint8_t host_quantize(uint32_t val, uint32_t mask, int pbit) {
   return (uint8_t)(dl < dh ? l8 : h8);
 }
 
+static void set_pack_attributes();  // after pack_kernel
+
 void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t opt6[256]) {
   static bool done[64] = {false};
   if (device < 0 || device >= 64 || done[device]) return;
@@ -100,6 +102,7 @@ void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t
   cudaMemcpyToSymbol(q_opt6, opt6, 256 * sizeof(uint32_t));
   build_sct_kernel<<<kSctRows, 256>>>();
   cudaDeviceSynchronize();
+  set_pack_attributes();
   done[device] = true;
 }
 
@@ -210,7 +213,7 @@ __device__ __forceinline__ uint32_t scanned(const uint16_t *local, const uint32_
 // estimate is unrolled.
 template <int kNSub, int kBits>
 __device__ __forceinline__ double estimate_shape_int(const uint32_t *px, uint32_t part,
-                                                     uint32_t *buf, uint2 *pal) {
+                                                     uint32_t *buf, uint4 *pal) {
   constexpr int T = kLaneStride;
   double err = 0.0;
 #pragma unroll 1
@@ -252,7 +255,7 @@ __device__ __noinline__ double estimate_shape_float(const uint32_t *px, uint32_t
 // subsets, two shapes per lane: the estimates of this lane's shapes.
 template <int kNSub>
 __device__ __forceinline__ void estimate_pair(const uint32_t *px, const uint32_t *part, int metric,
-                                              int lane, uint32_t *buf, uint2 *pal, double &e0,
+                                              int lane, uint32_t *buf, uint4 *pal, double &e0,
                                               double &e1) {
   constexpr int kBits = kNSub == 2 ? 3 : 2;
 #pragma unroll 1
@@ -269,7 +272,7 @@ __device__ __forceinline__ void estimate_pair(const uint32_t *px, const uint32_t
 __device__ __forceinline__ Selection box_selection_pipe(const uint32_t *px,
                                                         const uint32_t *part2,
                                                         const uint32_t *part3, int metric,
-                                                        int lane, uint32_t *buf, uint2 *pal) {
+                                                        int lane, uint32_t *buf, uint4 *pal) {
   Selection r;
   r.nshapes = 1;
   r.shape[0] = r.shape[1] = 0;
@@ -324,7 +327,7 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
   __shared__ uint32_t s_part2[64], s_part3[64];
   __shared__ uint32_t s_px[kWarps][16];
   __shared__ uint32_t s_buf[16 * kLaneStride];
-  __shared__ uint2 s_pal[8 * kLaneStride];
+  __shared__ uint4 s_pal[8 * kLaneStride];
   for (int i = threadIdx.x; i < 64; i += blockDim.x) {
     s_part2[i] = q_part2[i];
     s_part3[i] = q_part3[i];
@@ -743,7 +746,7 @@ struct Lane {
 // uniform metric, the float path otherwise.
 template <int C, bool kIdx>
 __device__ __forceinline__ float class_qe(const Lane &s, const uint32_t (&ereg)[16],
-                                          const uint32_t *pts, const uint32_t *proj, uint2 *pal,
+                                          const uint32_t *pts, const uint32_t *proj, uint4 *pal,
                                           uint32_t *palf, uint32_t q1, uint32_t q2, uint64_t &idx) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr a = mode_attr(kMode);
@@ -751,7 +754,7 @@ __device__ __forceinline__ float class_qe(const Lane &s, const uint32_t (&ereg)[
   constexpr bool kRot = a.has_rotation != 0;
   constexpr bool kN16 = a.subsets == 1;
   if (s.uniform) {
-    if constexpr (kN16) return qe_reg<kBits, kRot, kIdx>(ereg, pts, proj, s.psel, s.se, pal, q1, q2, idx);
+    if constexpr (kN16) return qe_reg<kBits, kRot, kIdx>(ereg, s.psel, s.se, pal, q1, q2, idx);
     else return qe_smem<kBits, kIdx>(pts, s.n, s.tex, s.se, pal, q1, q2, idx);
   }
   // float metric: palette as plain colours in the same buffer
@@ -762,7 +765,7 @@ __device__ __forceinline__ float class_qe(const Lane &s, const uint32_t (&ereg)[
 // class C; returns true when the fit is finished.
 template <int C>
 __device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t (&ereg)[16], const uint32_t *pts,
-                                            const uint32_t *proj, uint2 *pal, uint32_t *palf,
+                                            const uint32_t *proj, uint4 *pal, uint32_t *palf,
                                             const uint8_t *lut) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr a = mode_attr(kMode);
@@ -852,13 +855,13 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   __shared__ uint8_t s_lut[8 * 3 * 256];
   __shared__ uint32_t s_pts[16 * T];
   __shared__ uint32_t s_proj[kRot ? 16 * T : 1];
-  __shared__ uint2 s_pal[(1 << kBits) * T];
+  __shared__ uint4 s_pal[(1 << kBits) * T];
   for (int i = threadIdx.x; i < 8 * 3 * 256; i += blockDim.x) s_lut[i] = (&q_qlut[0][0][0])[i];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   uint32_t *pts = s_pts + threadIdx.x;
   uint32_t *proj = kRot ? s_proj + threadIdx.x : pts;
-  uint2 *pal = s_pal + threadIdx.x;
+  uint4 *pal = s_pal + threadIdx.x;
   uint32_t *palf = reinterpret_cast<uint32_t *>(s_pal) + threadIdx.x;  // float-metric palette
   const uint32_t count = ctr->anneal_count[C];
   const uint32_t base = scanned(local, chunk, (uint64_t)C * nb);
@@ -961,7 +964,7 @@ __device__ __forceinline__ void fit_out_of(const TaskState &o, FitOut &f) {
 template <int C>
 __device__ __noinline__ uint64_t fit_indices(const TaskState &o, const uint32_t *px, uint32_t part,
                                              const uint8_t *lut, uint32_t *pts, uint32_t *proj,
-                                             uint2 *pal, uint32_t *palf) {
+                                             uint4 *pal, uint32_t *palf) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr a = mode_attr(kMode);
   constexpr bool kRot = a.has_rotation != 0;
@@ -1002,7 +1005,7 @@ __device__ __noinline__ uint64_t fit_indices(const TaskState &o, const uint32_t 
 
 __device__ __forceinline__ uint64_t fit_indices_any(int c, const TaskState &o, const uint32_t *px,
                                                     uint32_t part, const uint8_t *lut, uint32_t *pts,
-                                                    uint32_t *proj, uint2 *pal, uint32_t *palf) {
+                                                    uint32_t *proj, uint4 *pal, uint32_t *palf) {
   switch (c) {
     case 0: return fit_indices<0>(o, px, part, lut, pts, proj, pal, palf);
     case 1: return fit_indices<1>(o, px, part, lut, pts, proj, pal, palf);
@@ -1017,6 +1020,7 @@ __device__ __forceinline__ uint64_t fit_indices_any(int c, const TaskState &o, c
 }
 
 constexpr int kPackThreads = kLaneStride;
+constexpr size_t kPackDynSmem = (size_t)kPackThreads * (16 * sizeof(uint4) + 3 * 16 * sizeof(uint32_t));
 
 __global__ void __launch_bounds__(kPackThreads) pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
                             const BlockSel *__restrict__ sel, const uint16_t *__restrict__ local,
@@ -1025,8 +1029,12 @@ __global__ void __launch_bounds__(kPackThreads) pack_kernel(const JobDev *__rest
   __shared__ uint32_t s_part2[64], s_part3[64];
   __shared__ uint8_t s_anc2[64], s_anc3[64];
   __shared__ uint8_t s_lut[8 * 3 * 256];
-  __shared__ uint32_t s_px[16 * kPackThreads], s_pts[16 * kPackThreads], s_proj[16 * kPackThreads];
-  __shared__ uint2 s_pal[16 * kPackThreads];
+  // per-thread arrays of the index recomputation (kPackDynSmem bytes)
+  extern __shared__ uint4 s_dyn[];
+  uint4 *s_pal = s_dyn;                                                  // 16 entries
+  uint32_t *s_px = reinterpret_cast<uint32_t *>(s_dyn + 16 * kPackThreads);  // 16 words
+  uint32_t *s_pts = s_px + 16 * kPackThreads;
+  uint32_t *s_proj = s_pts + 16 * kPackThreads;
   for (int i = threadIdx.x; i < 64; i += blockDim.x) {
     s_part2[i] = q_part2[i];
     s_part3[i] = q_part3[i];
@@ -1119,6 +1127,10 @@ __global__ void __launch_bounds__(kPackThreads) pack_kernel(const JobDev *__rest
     pack_block(best_mode, s, best_slot, f, s_anc2, s_anc3, s_part2, s_part3, best_rot, best_im, out);
   }
   store_block_p(jb, bs.lin, out);
+}
+
+static void set_pack_attributes() {
+  cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPackDynSmem);
 }
 
 // ---------------------------------------------------------------------------
@@ -1289,8 +1301,8 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
         if (ce != cudaSuccess) return (int)ce;
       }
     }
-    pack_kernel<<<(nb + kPackThreads - 1) / kPackThreads, kPackThreads, 0, st>>>(jobs, nb, b.sel, b.local,
-                                                                              b.chunk, b.state);
+    pack_kernel<<<(nb + kPackThreads - 1) / kPackThreads, kPackThreads, kPackDynSmem, st>>>(
+        jobs, nb, b.sel, b.local, b.chunk, b.state);
     return (int)cudaPeekAtLastError();
   };
   uint32_t prev_nb = 0;

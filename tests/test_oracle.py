@@ -122,3 +122,14 @@ def test_against_live_reference(port):
     st = np.array([4242, 0], np.uint32)
     got = port.compress(img, steps=20, rng_mode=O.RNG_SINGLE_STREAM, exp_mode=O.EXP_LIBM, state=st)
     assert np.array_equal(got, ref.compress(img, steps=20, seed=4242))
+
+
+def test_exact_projection_rounds_to_the_integer_index():
+    """FasTC picks the palette indices around fl(fl(D / L) * k) (RGBAEndpoints.cpp:
+    190-310). When D * k is a multiple of L, D / L equals j / k exactly, and the
+    two float roundings give back j for every j < k, k in {3, 7, 15}: the GPU's
+    integer quotient (j1 = j2 = j there) therefore needs no float path."""
+    for k in (3, 7, 15):
+        for j in range(1, k):
+            sc = (np.float32(j) / np.float32(k)) * np.float32(k)
+            assert sc.dtype == np.float32 and float(sc) == j, (k, j, sc)
