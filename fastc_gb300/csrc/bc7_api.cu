@@ -93,10 +93,22 @@ size_t rank_scratch_bytes(uint64_t total) {
   return (256 + ((nchunks * 4 + 255) & ~255ull) + total * 2 + 256 + 255) & ~255ull;
 }
 
-size_t scratch_bytes(uint64_t total, int engine) {
+size_t scratch_bytes(uint64_t total, int engine, int task_bound) {
   size_t b = rank_scratch_bytes(total);
-  if (engine == FASTC_BC7_ENGINE_PIPELINE) b += fastc::pipeline_scratch_bytes(total);
+  if (engine == FASTC_BC7_ENGINE_PIPELINE) b += fastc::pipeline_scratch_bytes(total, task_bound);
   return b;
+}
+
+size_t scratch_bytes_worst(uint64_t total, int engine) {
+  return std::max(scratch_bytes(total, engine, 16), scratch_bytes(total, engine, fastc::kMaxBlockTasks));
+}
+
+int task_bound_of(const fastc_bc7_settings *s, int per_job, uint32_t n) {
+  if (!s) return fastc::block_task_bound(FASTC_BC7_ALL_MODES);
+  int tb = 0;
+  const uint32_t m = per_job ? n : 1;
+  for (uint32_t i = 0; i < m; i++) tb = std::max(tb, fastc::block_task_bound(s[i].block_modes));
+  return tb;
 }
 
 EncodeScratch carve_scratch(void *base, uint64_t total) {
@@ -142,12 +154,12 @@ uint32_t align_flags(const void *in, const void *out) {
 // Encode `total` blocks of the device job table with the selected engine,
 // carving the rank and pipeline scratch out of `scratch`.
 int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
-                  LaunchShape shape, const ClassStreams *cls, cudaStream_t st) {
+                  LaunchShape shape, int task_bound, const ClassStreams *cls, cudaStream_t st) {
   const EncodeScratch rank = carve_scratch(scratch, total);
   if (engine == FASTC_BC7_ENGINE_PIPELINE) {
     void *pipe = static_cast<uint8_t *>(scratch) + rank_scratch_bytes(total);
     return fastc::launch_pipeline(jobs, njobs, total, rank, pipe,
-                                  fastc::device_sm_count(current_device()), cls, st);
+                                  fastc::device_sm_count(current_device()), task_bound, cls, st);
   }
   return fastc::launch_encode(jobs, njobs, total, rank, shape, st);
 }
@@ -273,7 +285,8 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
   CK(g_host.in.ensure(in_total));
   CK(g_host.out.ensure(out_total));
   CK(g_host.jobs.ensure(n * sizeof(JobDev)));
-  CK(g_host.scratch.ensure(scratch_bytes(total, g_engine)));
+  const int tb = task_bound_of(s, per_job, n);
+  CK(g_host.scratch.ensure(scratch_bytes(total, g_engine, tb)));
   cudaStream_t cs = g_host.stream;
   uint8_t *din = static_cast<uint8_t *>(g_host.in.p);
   uint8_t *dout = static_cast<uint8_t *>(g_host.out.p);
@@ -288,7 +301,7 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
   CK(cudaMemcpyAsync(g_host.jobs.p, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs));
   const EncodeScratch sc = carve_scratch(g_host.scratch.p, total);
   const int le = launch_engine(static_cast<const JobDev *>(g_host.jobs.p), (int)n, total,
-                               g_host.scratch.p, g_engine, pick_shape(total), g_host.cls, cs);
+                               g_host.scratch.p, g_engine, pick_shape(total), tb, g_host.cls, cs);
   if (le) return fail_cuda((cudaError_t)le);
   for (uint32_t i = 0; i < n; i++) {
     if (!dj[i].nblocks) continue;
@@ -501,13 +514,14 @@ fastc_bc7_status fastc_bc7_compress_device(const fastc_bc7_job *jobs, uint32_t n
   }
   void *buf = nullptr;
   const size_t jb = (n * sizeof(JobDev) + 255) & ~(size_t)255;
-  CK(cudaMallocAsync(&buf, jb + scratch_bytes(total, engine), cs));
+  const int tb = task_bound_of(settings, per_job_settings, n);
+  CK(cudaMallocAsync(&buf, jb + scratch_bytes(total, engine, tb), cs));
   cudaError_t e = cudaMemcpyAsync(buf, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs);
   const int dev = current_device();
   ClassStreams *cls = engine == FASTC_BC7_ENGINE_PIPELINE ? acquire_class_streams(dev) : nullptr;
   if (e == cudaSuccess)
     e = (cudaError_t)launch_engine(static_cast<const JobDev *>(buf), (int)n, total,
-                                   static_cast<uint8_t *>(buf) + jb, engine, shape, cls, cs);
+                                   static_cast<uint8_t *>(buf) + jb, engine, shape, tb, cls, cs);
   release_class_streams(dev, cls);
   cudaError_t ef = cudaFreeAsync(buf, cs);
   if (e != cudaSuccess) return fail_cuda(e);
@@ -557,7 +571,8 @@ fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
   cudaStream_t cs = nullptr;
   cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p->d_jobs), n * sizeof(JobDev));
   p->engine = g_engine;
-  if (e == cudaSuccess) e = cudaMalloc(&p->d_scratch, scratch_bytes(total > 0 ? total : 1, p->engine));
+  const int tb = task_bound_of(settings, per_job_settings, n);
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_scratch, scratch_bytes(total > 0 ? total : 1, p->engine, tb));
   if (e == cudaSuccess)
     e = cudaMemcpy(p->d_jobs, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
@@ -570,7 +585,7 @@ fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
       const int le = launch_engine(p->d_jobs, (int)n, total, p->d_scratch, p->engine,
-                                   pick_shape(total), use_cls ? &cls : nullptr, cs);
+                                   pick_shape(total), tb, use_cls ? &cls : nullptr, cs);
       cudaError_t ee = cudaStreamEndCapture(cs, &p->graph);
       e = le ? (cudaError_t)le : ee;
     }

@@ -37,14 +37,19 @@ bool job_range(const fastc_bc7_job &j, uint32_t *first, uint32_t *count);
 int current_device();
 LaunchShape pick_shape(uint64_t total);
 size_t rank_scratch_bytes(uint64_t total);
-size_t scratch_bytes(uint64_t total, int engine);
+// Scratch of a launch; task_bound: most cluster fits per block of its jobs.
+size_t scratch_bytes(uint64_t total, int engine, int task_bound);
+// Largest scratch any mask can need (admission bound).
+size_t scratch_bytes_worst(uint64_t total, int engine);
+// Most block_task_bound() over the jobs' settings.
+int task_bound_of(const fastc_bc7_settings *s, int per_job, uint32_t n);
 EncodeScratch carve_scratch(void *base, uint64_t total);
 JobDev make_job(const fastc_bc7_job &j, const fastc_bc7_settings &s, uint32_t first,
                 uint32_t count, uint64_t begin);
 uint32_t align_flags(const void *in, const void *out);
 // `cls`: side streams for the pipeline engine's classes (null: one stream).
 int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
-                  LaunchShape shape, const ClassStreams *cls, cudaStream_t st);
+                  LaunchShape shape, int task_bound, const ClassStreams *cls, cudaStream_t st);
 // Side-stream sets for callers without their own: taken for one enqueue
 // and given back (per device; created on first need).
 ClassStreams *acquire_class_streams(int device);

@@ -322,7 +322,7 @@ template <int kWarps>
 __global__ void __launch_bounds__(kWarps * 32) select_kernel(
     const JobDev *__restrict__ jobs, int njobs, uint64_t c0, uint32_t nb,
     const uint16_t *__restrict__ rank_local, const uint32_t *__restrict__ rank_chunk,
-    BlockSel *__restrict__ sel, uint8_t *__restrict__ counts, uint32_t *status) {
+    BlockSel *__restrict__ sel, uint8_t *__restrict__ counts, int task_bound, uint32_t *status) {
   static_assert(kWarps * 32 == kLaneStride, "shared arrays use the lane stride");
   __shared__ uint32_t s_part2[64], s_part3[64];
   __shared__ uint32_t s_px[kWarps][16];
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
     int total = c;
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) total += __shfl_xor_sync(0xFFFFFFFFu, total, o);
-    const bool overflow = total > kMaxBlockTasks;  // not reachable with BC7's mode table
+    const bool overflow = total > task_bound;  // not reachable: the host computed the bound
     if (lane < kClasses) counts[(uint64_t)lane * nb + gl] = overflow ? 0 : (uint8_t)c;
     if (lane == 0) {
       bs.shape0 = (uint8_t)s.shape[0];
@@ -1140,9 +1140,9 @@ static void set_pack_attributes() {
 namespace {
 
 // Bytes of one chunk buffer for chunks of at most nb blocks.
-size_t chunk_buffer_bytes(uint64_t nb) {
+size_t chunk_buffer_bytes(uint64_t nb, int tb) {
   const uint64_t n8 = (uint64_t)kClasses * nb;
-  const uint64_t tmax = (uint64_t)kMaxBlockTasks * nb;
+  const uint64_t tmax = (uint64_t)tb * nb;
   size_t b = 256;  // PipelineCounters
   b += (nb * sizeof(BlockSel) + 255) & ~255ull;
   b += (n8 + 255) & ~255ull;
@@ -1165,7 +1165,7 @@ struct ChunkBuf {
   AnnealRec *arec;
 };
 
-ChunkBuf carve_chunk(uint8_t *p, uint64_t nb) {
+ChunkBuf carve_chunk(uint8_t *p, uint64_t nb, int tb) {
   ChunkBuf c;
   c.ctr = reinterpret_cast<PipelineCounters *>(p);
   p += 256;
@@ -1178,19 +1178,47 @@ ChunkBuf carve_chunk(uint8_t *p, uint64_t nb) {
   c.chunk = reinterpret_cast<uint32_t *>(p);
   p += ((((uint64_t)kClasses * nb + kRankChunk - 1) / kRankChunk) * 4 + 255) & ~255ull;
   c.desc = reinterpret_cast<uint2 *>(p);
-  p += ((uint64_t)kMaxBlockTasks * nb * sizeof(uint2) + 255) & ~255ull;
+  p += ((uint64_t)tb * nb * sizeof(uint2) + 255) & ~255ull;
   c.state = reinterpret_cast<TaskState *>(p);
-  p += ((uint64_t)kMaxBlockTasks * nb * sizeof(TaskState) + 255) & ~255ull;
+  p += ((uint64_t)tb * nb * sizeof(TaskState) + 255) & ~255ull;
   c.arec = reinterpret_cast<AnnealRec *>(p);
   return c;
 }
 
 }  // namespace
 
-size_t pipeline_scratch_bytes(uint64_t total_blocks) {
-  const uint64_t nb = total_blocks < kPipelineChunk ? total_blocks : kPipelineChunk;
-  const int nbuf = total_blocks > kPipelineChunk ? 2 : 1;
-  return (size_t)nbuf * chunk_buffer_bytes(nb);
+int block_task_bound(uint32_t modes) {
+  modes &= 0xFFu;
+  // BoxSelection's outcomes (CP:1670-1750): opaque blocks search two shape
+  // slots (2 and 3 subsets) with modes 4 and 5 removed, or one slot's modes
+  // after an exact fit; other blocks one 2-subset slot with the alpha modes.
+  struct Outcome { uint32_t modes; int nshapes; };
+  const Outcome outs[4] = {{0xFFu & ~((1u << 4) | (1u << 5)), 2}, {kModesTwo, 1}, {kModesThree, 2},
+                           {kModesAlpha, 1}};
+  int worst = 0;
+  for (const Outcome &o : outs) {
+    uint32_t m = o.modes & modes;
+    if (m == 0) m = modes;  // the fallback to the caller's mask
+    int n = 0;
+    for (int mode = 0; mode < 8; mode++) {
+      if (!(m & (1u << mode))) continue;
+      const ModeAttr a = mode_attr(mode);
+      for (int sl = 0; sl < o.nshapes; sl++) {
+        const int nparts = sl == 0 ? 2 : 3;
+        if (a.subsets != 1 && a.subsets != nparts) continue;
+        n += a.has_rotation ? 4 * (mode == 4 ? 2 : 1) : a.subsets;
+      }
+    }
+    worst = n > worst ? n : worst;
+  }
+  return worst;
+}
+
+size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound) {
+  const uint64_t cap = pipeline_chunk(task_bound);
+  const uint64_t nb = total_blocks < cap ? total_blocks : cap;
+  const int nbuf = total_blocks > cap ? 2 : 1;
+  return (size_t)nbuf * chunk_buffer_bytes(nb, task_bound);
 }
 
 cudaError_t class_streams_create(ClassStreams *cs) {
@@ -1283,16 +1311,19 @@ constexpr int kClassOrder[kClasses] = {6, 7, 5, 4, 3, 1, 8, 2, 0};
 // them; chunk i uses buffer i % 2, which select(i) may only overwrite after
 // pack(i - 2), earlier on `st`.
 int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
-                    void *scratch, int sm_count, const ClassStreams *cls, void *stream) {
+                    void *scratch, int sm_count, int task_bound, const ClassStreams *cls,
+                    void *stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (total == 0) return 0;
+  const int tb = task_bound < 1 ? 1 : (task_bound > kMaxBlockTasks ? kMaxBlockTasks : task_bound);
   int e = launch_rank_prepass(jobs, njobs, total, rank, stream);
   if (e) return e;
-  const uint64_t cap = kPipelineChunk;
+  const uint64_t cap = pipeline_chunk(tb);
   const uint64_t nbmax = total < cap ? total : cap;
   ChunkBuf bufs[2];
-  bufs[0] = carve_chunk(static_cast<uint8_t *>(scratch), nbmax);
-  bufs[1] = total > cap ? carve_chunk(static_cast<uint8_t *>(scratch) + chunk_buffer_bytes(nbmax), nbmax)
+  bufs[0] = carve_chunk(static_cast<uint8_t *>(scratch), nbmax, tb);
+  bufs[1] = total > cap ? carve_chunk(static_cast<uint8_t *>(scratch) + chunk_buffer_bytes(nbmax, tb),
+                                      nbmax, tb)
                         : bufs[0];
   auto pack = [&](const ChunkBuf &b, uint32_t nb, int parity) -> int {
     if (cls) {
@@ -1314,7 +1345,7 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     const uint32_t nchunks = (uint32_t)((n8 + kRankChunk - 1) / kRankChunk);
     const int sel_ctas = (int)((nb + 3) / 4 < (uint64_t)sm_count * 16 ? (nb + 3) / 4 : (uint64_t)sm_count * 16);
     select_kernel<4><<<sel_ctas, 128, 0, st>>>(jobs, njobs, c0, nb, rank.rank_local, rank.chunk_prefix,
-                                               b.sel, b.counts, rank.status);
+                                               b.sel, b.counts, tb, rank.status);
     scan_local_u8_kernel<<<nchunks, kRankChunk, 0, st>>>(b.counts, n8, b.local, b.chunk);
     scan_chunks_kernel<<<1, 1024, 0, st>>>(b.chunk, nchunks, b.ctr);
     emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, b.counts, b.local, b.chunk, b.desc);

@@ -9,13 +9,20 @@
 
 namespace fastc {
 
-// Blocks per pipeline chunk; scratch grows with it. Launches of more than
-// one chunk use two scratch buffers so that the select stage of a chunk
-// runs while the previous chunk anneals.
-constexpr uint64_t kPipelineChunk = 256 * 1024;
 // Cluster fits one block can need. BC7's mode table caps it at 32 (opaque
-// block whose selection falls back to the caller's mask of modes 1,3-7).
+// block whose selection falls back to the caller's mask of modes 1,3-7);
+// with all modes enabled it is 15 (block_task_bound() computes the bound of
+// a mask). Scratch is sized by the bound of the launch's masks.
 constexpr int kMaxBlockTasks = 32;
+// Blocks per pipeline chunk: scratch grows with chunk x task bound, and
+// longer annealing lists keep more lanes busy, so the chunk is larger when
+// the bound is small. Launches of more than one chunk use two scratch
+// buffers so that the select stage of a chunk runs while the previous chunk
+// anneals.
+constexpr uint64_t kChunkTaskBudget = 8ull * 1024 * 1024;  // chunk blocks x task bound
+__host__ __device__ constexpr uint64_t pipeline_chunk(int task_bound) {
+  return kChunkTaskBudget / (uint64_t)(task_bound > 16 ? 32 : 16);
+}
 
 // Per-block outcome of the select stage (16 bytes).
 struct BlockSel {
@@ -93,9 +100,13 @@ cudaError_t class_streams_create(ClassStreams *cs);
 void class_streams_destroy(ClassStreams *cs);
 
 void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t opt6[256]);
-size_t pipeline_scratch_bytes(uint64_t total_blocks);
-// `cls` null: every stage runs in order on `stream`.
+// Most cluster fits a block can need when the caller enables `modes`.
+int block_task_bound(uint32_t modes);
+size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound);
+// `cls` null: every stage runs in order on `stream`. `task_bound`: the most
+// block_task_bound() of the jobs' masks.
 int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
-                    void *scratch, int sm_count, const ClassStreams *cls, void *stream);
+                    void *scratch, int sm_count, int task_bound, const ClassStreams *cls,
+                    void *stream);
 
 }  // namespace fastc

@@ -93,7 +93,7 @@ struct fastc_bc7_server_s {
 
   // device bytes a batch needs, beyond the per-request texels and blocks
   size_t batch_overhead(uint64_t blocks, size_t njobs) const {
-    return round_up(njobs * sizeof(JobDev)) + scratch_bytes(blocks, engine);
+    return round_up(njobs * sizeof(JobDev)) + scratch_bytes_worst(blocks, engine);
   }
 
   void loop();
@@ -130,7 +130,9 @@ void fastc_bc7_server_s::launch(Slot &s) {
     total += s.reqs[i]->count;
   }
   const size_t table = round_up(s.reqs.size() * sizeof(JobDev));
-  const size_t need = in_total + out_total + table + scratch_bytes(total, engine);
+  int tb = 0;
+  for (Request *r : s.reqs) tb = std::max(tb, fastc::block_task_bound(r->settings.block_modes));
+  const size_t need = in_total + out_total + table + scratch_bytes(total, engine, tb);
   if (s.pinned_cap < out_total) {
     if (s.pinned) cudaFreeHost(s.pinned);
     s.pinned = nullptr;
@@ -167,7 +169,7 @@ void fastc_bc7_server_s::launch(Slot &s) {
         std::lock_guard<std::mutex> lk(g_mu);
         shape = pick_shape(total);
       }
-      e = (cudaError_t)launch_engine(dtab, (int)dj.size(), total, scratch, engine, shape, s.cls,
+      e = (cudaError_t)launch_engine(dtab, (int)dj.size(), total, scratch, engine, shape, tb, s.cls,
                                      s.stream);
     }
     if (e == cudaSuccess)
