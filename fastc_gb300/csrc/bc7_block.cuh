@@ -171,8 +171,10 @@ __device__ inline void run_task(const Task &t, const Selection &sel, const uint3
   const uint32_t shape = sel.shape[t.slot];
   const uint32_t part = m.a.subsets == 2 ? part2[shape] : (m.a.subsets == 3 ? part3[shape] : 0u);
   Cluster c;
-  uint32_t buf[16];
+  uint32_t buf[16], aux[16];
   make_cluster(px, part, t.subset, buf, 1, c);
+  c.aux = aux;
+  c.aux_stride = 1;
   o.idx = 0;
   o.aidx = 0;
   o.pbit = 0;

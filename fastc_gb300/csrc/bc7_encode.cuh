@@ -200,6 +200,8 @@ struct Cluster {
   int rot;    // alpha path: channel (1..3) swapped into alpha, 0 = none
   bool a255;  // alpha path: alpha of every point forced to 255
   float avg[4], mn[4], mx[4];
+  uint32_t *aux;  // 16 words of scratch (principal_axis), element k at aux[k * aux_stride]
+  int aux_stride;
 };
 
 __device__ __forceinline__ uint32_t cl_pixel(const Cluster &c, int k) { return c.px[k * c.stride]; }
@@ -220,6 +222,8 @@ __device__ __forceinline__ void make_cluster(const uint32_t *px, uint32_t part_w
                                              int subset, uint32_t *buf, int bstride, Cluster &c) {
   c.px = buf;
   c.stride = bstride;
+  c.aux = nullptr;
+  c.aux_stride = 0;
   c.tex = 0;
   c.n = 0;
   c.rot = 0;
@@ -361,38 +365,42 @@ __device__ inline void power_method(const float m[4][4], float *out) {
   for (int k = 0; k < 4; k++) out[k] = b[k];
 }
 
+__device__ __forceinline__ uint32_t cl_packed(const Cluster &c, int k);
+
+// The unique points are kept packed (they are bytes) in the cluster's
+// scratch words instead of a float array.
 __device__ inline void principal_axis(const Cluster &c, float *axis) {
-  // unique points, in order; slots past the unique count stay (-1,-1,-1,-1)
-  float upts[16][4];
+  // unique points, in order; slots past the unique count read (-1,-1,-1,-1)
+  uint32_t *up = c.aux;
+  const int us = c.aux_stride;
   int nu = 0;
   for (int i = 0; i < c.n; i++) {
-    float p[4];
-    cl_point(c, i, p);
+    const uint32_t q = cl_packed(c, i);
     bool has = false;
     for (int j = 0; j < nu; j++)
-      if (eq4(upts[j], p)) has = true;
+      if (up[j * us] == q) has = true;
     if (!has) {
-#pragma unroll
-      for (int k = 0; k < 4; k++) upts[nu][k] = p[k];
+      up[nu * us] = q;
       nu++;
     }
   }
-  for (int j = nu; j < 16; j++)
-#pragma unroll
-    for (int k = 0; k < 4; k++) upts[j][k] = -1.0f;
   if (nu == 1) {
     axis[0] = axis[1] = axis[2] = axis[3] = 0.0f;
     return;
   }
-  float dir[4];
+  float u0[4], u1[4], dir[4];
+  unpack4(up[0], u0);
+  unpack4(up[us], u1);
 #pragma unroll
-  for (int k = 0; k < 4; k++) dir[k] = __fsub_rn(upts[1][k], upts[0][k]);
+  for (int k = 0; k < 4; k++) dir[k] = __fsub_rn(u1[k], u0[k]);
   normalize4(dir);
   bool collinear = true;
   for (int i = 2; i < c.n; i++) {  // bounded by the point count, not nu
+    float ui[4] = {-1.0f, -1.0f, -1.0f, -1.0f};
+    if (i < nu) unpack4(up[i * us], ui);
     float v[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) v[k] = __fsub_rn(upts[i][k], upts[0][k]);
+    for (int k = 0; k < 4; k++) v[k] = __fsub_rn(ui[k], u0[k]);
     if (fabs(fabs((double)dot4(v, dir)) - (double)length4(v)) > 1e-7) {
       collinear = false;
       break;
@@ -724,9 +732,25 @@ struct FitSetup {
   bool anneal;      // the annealing loop has work (steps > 0, error > 0)
 };
 
-// CompressionMode::CompressCluster, colour version (CP:921-1094), up to the
-// annealing (the first QuantizedError and the grid snap of CP:546-566).
-__device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st) {
+// Point k of the cluster as packed bytes: cl_point() without the float
+// conversion (the rotation swap and forced alpha of the alpha path applied).
+__device__ __forceinline__ uint32_t cl_packed(const Cluster &c, int k) {
+  const uint32_t px = cl_pixel(c, k);
+  if (!c.a255) return px;
+  uint32_t sel = 0x4210u;  // bytes 0-2 from the pixel, byte 3 = 0xFF
+  if (c.rot) sel = (sel & ~(0xFu << (4 * (c.rot - 1)))) | (3u << (4 * (c.rot - 1)));
+  return __byte_perm(px, 0xFFFFFFFFu, sel);
+}
+
+// CompressionMode::CompressCluster (CP:921-1094) up to the annealing, for
+// kNB = 2^index-bits palette entries: single colour, PCA endpoints, the
+// k-means refinement, least squares, grid clamp and the first
+// QuantizedError. With kNB a constant the level loops unroll and the k-means
+// levels stay in registers; the members' per-level sums are exact integers
+// (sums of at most 16 bytes), so they are accumulated as integers, which
+// equals FasTC's float sums.
+template <int kNB>
+__device__ inline void fit_rgb_setup_t(ModeCtx &m, const Cluster &c, FitSetup &st) {
   float *p1 = st.p1, *p2 = st.p2;
   uint64_t &idx = st.idx;
   uint32_t &pbit = st.pbit;
@@ -740,8 +764,8 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
     st.err = (double)c.n * e;
     return;
   }
-  const int ib = bits_index(m, -1);
-  const int nb = 1 << ib;
+  constexpr int nb = kNB;
+  constexpr int kUnroll = kNB <= 8 ? kNB : 1;
   float axis[4];
   principal_axis(c, axis);
   float mindp = FLT_MAX, maxdp = -FLT_MAX;
@@ -761,15 +785,15 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
   }
   clamp_endpoints(p1, p2);
 
-  float pts[16][4];
-  uint32_t npts[16];
+  float pts[kNB][4];
+  uint32_t npts[kNB];
+#pragma unroll kUnroll
   for (int i = 0; i < nb; i++) {
     const float s = __fdiv_rn((float)i, (float)(nb - 1));
 #pragma unroll
     for (int k = 0; k < 4; k++)
       pts[i][k] = __fadd_rn(__fmul_rn(p1[k], __fsub_rn(1.0f, s)), __fmul_rn(p2[k], s));
   }
-  uint64_t bidx = 0;
   bool fixed = false;
   int iters = 0;
   while (!fixed) {
@@ -777,11 +801,16 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
       atomicOr(m.status, kStatusKMeansCap);
       break;
     }
+    // per level: channel sums in 13-bit fields, member count from bit 52
+    uint64_t acc[kNB];
+#pragma unroll kUnroll
+    for (int j = 0; j < nb; j++) acc[j] = 0;
     for (int i = 0; i < c.n; i++) {
       float p[4];
       cl_point(c, i, p);
       int minb = 0;
       float mind = FLT_MAX;
+#pragma unroll kUnroll
       for (int j = 0; j < nb; j++) {
         float v[4];
 #pragma unroll
@@ -792,23 +821,23 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
           minb = j;
         }
       }
-      set_nib(bidx, i, (uint32_t)minb);
+      const uint32_t q = cl_packed(c, i);
+      const uint64_t add = (uint64_t)(q & 0xFF) | ((uint64_t)((q >> 8) & 0xFF) << 13) |
+                           ((uint64_t)((q >> 16) & 0xFF) << 26) | ((uint64_t)(q >> 24) << 39) |
+                           (1ull << 52);
+#pragma unroll kUnroll
+      for (int j = 0; j < nb; j++) acc[j] += j == minb ? add : 0ull;
     }
     fixed = true;
+#pragma unroll kUnroll
     for (int j = 0; j < nb; j++) {
-      float np[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      uint32_t cnt = 0;
-      for (int i = 0; i < c.n; i++) {
-        if (get_nib(bidx, i) != (uint32_t)j) continue;
-        float p[4];
-        cl_point(c, i, p);
-        cnt++;
+      const uint32_t cnt = (uint32_t)(acc[j] >> 52);
+      float np[4];
 #pragma unroll
-        for (int k = 0; k < 4; k++) np[k] = __fadd_rn(np[k], p[k]);
+      for (int k = 0; k < 4; k++) {
+        np[k] = (float)(uint32_t)((acc[j] >> (13 * k)) & 0x1FFFu);
+        if (cnt) np[k] = __fdiv_rn(np[k], (float)cnt);
       }
-      if (cnt)
-#pragma unroll
-        for (int k = 0; k < 4; k++) np[k] = __fdiv_rn(np[k], (float)cnt);
       npts[j] = cnt;
       if (!eq4(pts[j], np)) fixed = false;
 #pragma unroll
@@ -816,19 +845,27 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
     }
   }
   int filled = 0, last = -1;
+#pragma unroll kUnroll
   for (int j = 0; j < nb; j++)
     if (npts[j] > 0) {
       filled++;
       last = j;
     }
   if (filled == 1) {
-    const double e = single_color(m, pts[last], p1, p2, pbit);
+    float pl[4];
+#pragma unroll kUnroll
+    for (int j = 0; j < nb; j++)
+      if (j == last)
+#pragma unroll
+        for (int k = 0; k < 4; k++) pl[k] = pts[j][k];
+    const double e = single_color(m, pl, p1, p2, pbit);
     for (int i = 0; i < c.n; i++) set_nib(idx, cl_texel(c, i), 1);
     st.err = (double)c.n * e;
     return;
   }
   float asq = 0.0f, bsq = 0.0f, ab = 0.0f;
   float ax[4] = {0.0f, 0.0f, 0.0f, 0.0f}, bx[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll kUnroll
   for (int j = 0; j < nb; j++) {
     const float fb = (float)(nb - 1);
     const float a = __fdiv_rn((float)(nb - 1 - j), fb), b = __fdiv_rn((float)j, fb);
@@ -863,6 +900,14 @@ __device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st)
   st.anneal = m.steps > 0 && st.errf > 0.0f;
 }
 
+__device__ inline void fit_rgb_setup(ModeCtx &m, const Cluster &c, FitSetup &st) {
+  switch (bits_index(m, -1)) {
+    case 2: fit_rgb_setup_t<4>(m, c, st); break;
+    case 3: fit_rgb_setup_t<8>(m, c, st); break;
+    default: fit_rgb_setup_t<16>(m, c, st); break;
+  }
+}
+
 __device__ inline double fit_rgb(ModeCtx &m, const Cluster &c, float *p1, float *p2,
                           uint64_t &idx, uint32_t &pbit) {
   FitSetup st;
@@ -880,9 +925,22 @@ __device__ inline double fit_rgb(ModeCtx &m, const Cluster &c, float *p1, float 
   return st.err;
 }
 
-__device__ inline void alpha_fit(const ModeCtx &m, const float *avals, float amin, float amax,
-                          const uint32_t *opt6, float &a1_out, float &a2_out, uint64_t &aidx,
-                          double &aerr_out);
+template <int kANB>
+__device__ inline void alpha_fit_t(const ModeCtx &m, const Cluster &c, uint32_t ch, float amin,
+                                   float amax, const uint32_t *opt6, float &a1_out, float &a2_out,
+                                   uint64_t &aidx, double &aerr_out);
+
+// The alpha channel (channel `ch` of the texels) of the block, and its range.
+__device__ __forceinline__ float cl_alpha(const Cluster &c, int i, uint32_t ch) {
+  return (float)((cl_pixel(c, i) >> (8 * ch)) & 0xFF);
+}
+
+__device__ inline void alpha_fit_any(const ModeCtx &m, const Cluster &c, uint32_t ch, float amin,
+                                     float amax, const uint32_t *opt6, float &a1, float &a2,
+                                     uint64_t &aidx, double &aerr) {
+  if (bits_alpha(m, -1) == 2) alpha_fit_t<4>(m, c, ch, amin, amax, opt6, a1, a2, aidx, aerr);
+  else alpha_fit_t<8>(m, c, ch, amin, amax, opt6, a1, a2, aidx, aerr);
+}
 
 // CompressionMode::CompressCluster, separate-alpha version (CP:632-919).
 // `c` is the whole block; the colour fit runs on a rotated copy whose
@@ -893,21 +951,19 @@ __device__ inline double fit_alpha(ModeCtx &m, const Cluster &c, const uint32_t 
   rgb.rot = rotation_of(m);
   rgb.a255 = true;
   const int r = rgb.rot;
-  float avals[16];
+  const uint32_t ch = r ? r - 1 : 3;
   float amin = FLT_MAX, amax = -FLT_MAX;
   for (int i = 0; i < 16; i++) {
-    const uint32_t px = cl_pixel(c, i);
-    const uint32_t ch = r ? r - 1 : 3;
-    avals[i] = (float)((px >> (8 * ch)) & 0xFF);
-    amin = min_std(avals[i], amin);
-    amax = max_std(avals[i], amax);
+    const float av = cl_alpha(c, i, ch);
+    amin = min_std(av, amin);
+    amax = max_std(av, amax);
   }
   uint32_t dummy = 0;
   float rp1[4], rp2[4];
   const double rgb_err = fit_rgb(m, rgb, rp1, rp2, idx, dummy);
   double aerr;
   float a1, a2;
-  alpha_fit(m, avals, amin, amax, opt6, a1, a2, aidx, aerr);
+  alpha_fit_any(m, c, ch, amin, amax, opt6, a1, a2, aidx, aerr);
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     p1[k] = rp1[k];
@@ -919,7 +975,9 @@ __device__ inline double fit_alpha(ModeCtx &m, const Cluster &c, const uint32_t 
 }
 
 // The separate-alpha fit up to the colour fit's annealing: the colour part
-// in `st` (rotated cluster, CP:664-701), the alpha part complete.
+// in `st` (rotated cluster, CP:664-701), the alpha part complete. kNB: the
+// colour and alpha palette sizes (0: from the mode context).
+template <int kNB = 0, int kANB = 0>
 __device__ inline void fit_alpha_setup(ModeCtx &m, const Cluster &c, const uint32_t *opt6,
                                 FitSetup &st, float &a1, float &a2, uint64_t &aidx,
                                 double &aerr) {
@@ -927,34 +985,40 @@ __device__ inline void fit_alpha_setup(ModeCtx &m, const Cluster &c, const uint3
   rgb.rot = rotation_of(m);
   rgb.a255 = true;
   const int r = rgb.rot;
-  float avals[16];
+  const uint32_t ch = r ? r - 1 : 3;
   float amin = FLT_MAX, amax = -FLT_MAX;
   for (int i = 0; i < 16; i++) {
-    const uint32_t ch = r ? r - 1 : 3;
-    avals[i] = (float)((cl_pixel(c, i) >> (8 * ch)) & 0xFF);
-    amin = min_std(avals[i], amin);
-    amax = max_std(avals[i], amax);
+    const float av = cl_alpha(c, i, ch);
+    amin = min_std(av, amin);
+    amax = max_std(av, amax);
   }
   st.idx = 0;
   st.pbit = 0;
-  fit_rgb_setup(m, rgb, st);
-  alpha_fit(m, avals, amin, amax, opt6, a1, a2, aidx, aerr);
+  if constexpr (kNB > 0) {
+    fit_rgb_setup_t<kNB>(m, rgb, st);
+    alpha_fit_t<kANB>(m, c, ch, amin, amax, opt6, a1, a2, aidx, aerr);
+  } else {
+    fit_rgb_setup(m, rgb, st);
+    alpha_fit_any(m, c, ch, amin, amax, opt6, a1, a2, aidx, aerr);
+  }
 }
 
 // The alpha half of CompressCluster's separate-alpha version (CP:703-911):
 // 1-D k-means on the rotated channel, least squares, quantisation and the
-// per-texel bucket search. Independent of the colour fit's annealing.
-__device__ inline void alpha_fit(const ModeCtx &m, const float *avals, float amin, float amax,
-                          const uint32_t *opt6, float &a1_out, float &a2_out, uint64_t &aidx,
-                          double &aerr_out) {
-
+// per-texel bucket search, for kANB = 2^alpha-index-bits levels.
+// Independent of the colour fit's annealing. Bucket sums are sums of at
+// most 16 bytes, exact in float, so they are accumulated as integers.
+template <int kANB>
+__device__ inline void alpha_fit_t(const ModeCtx &m, const Cluster &c, uint32_t ch, float amin,
+                                   float amax, const uint32_t *opt6, float &a1_out, float &a2_out,
+                                   uint64_t &aidx, double &aerr_out) {
   float a1 = amin, a2 = amax;
   double aerr;
   const int abits = bits_alpha(m, -1);
   float w[4];
   metric_of(m, w);
   const float wa = w[3];
-  const int nb = 1 << abits;
+  constexpr int nb = kANB;
   if (a1 == a2) {
     const uint32_t abe = (uint32_t)a1;
     if (m.mode == 5) {
@@ -973,25 +1037,28 @@ __device__ inline void alpha_fit(const ModeCtx &m, const float *avals, float ami
       aerr = (double)__fmul_rn(16.0f, pe);
     }
   } else {
-    float vals[8];
-    uint32_t bk[16];
-    for (int j = 0; j < 8; j++) vals[j] = 0.0f;
+    float vals[nb];
+#pragma unroll
     for (int j = 0; j < nb; j++) {
       const float fb = (float)(nb - 1);
       vals[j] = __fadd_rn(amin, __fmul_rn(__fdiv_rn((float)j, fb), __fsub_rn(amax, amin)));
     }
+    uint64_t bk = 0;  // bucket of texel i in nibble i
     for (int i = 0; i < 16; i++) {
+      const float av = cl_alpha(c, i, ch);
       float md = 255.0f;
-      bk[i] = 0;
+      uint32_t b = 0;
+#pragma unroll
       for (int j = 0; j < nb; j++) {
-        const float d = fabsf(__fsub_rn(avals[i], vals[j]));
+        const float d = fabsf(__fsub_rn(av, vals[j]));
         if (d < md) {
           md = d;
-          bk[i] = (uint32_t)j;
+          b = (uint32_t)j;
         }
       }
+      bk |= (uint64_t)b << (4 * i);
     }
-    float npts[8];
+    float npts[nb];
     bool fixed = false;
     int iters = 0;
     while (!fixed) {
@@ -999,34 +1066,46 @@ __device__ inline void alpha_fit(const ModeCtx &m, const float *avals, float ami
         atomicOr(m.status, kStatusKMeansCap);
         break;
       }
-      float avg[8];
-      for (int j = 0; j < 8; j++) {
-        avg[j] = 0.0f;
-        npts[j] = 0.0f;
-      }
-      for (int j = 0; j < nb; j++) {
-        for (int i = 0; i < 16; i++)
-          if (bk[i] == (uint32_t)j) {
-            avg[j] = __fadd_rn(avg[j], avals[i]);
-            npts[j] = __fadd_rn(npts[j], 1.0f);
-          }
-        if (npts[j] > 0.0f) avg[j] = __fdiv_rn(avg[j], npts[j]);
-      }
-      fixed = true;
-      for (int j = 0; j < nb; j++) fixed = fixed && (avg[j] == vals[j]);
-      for (int j = 0; j < 8; j++) vals[j] = avg[j];
+      uint32_t sum[nb], cnt[nb];
+#pragma unroll
+      for (int j = 0; j < nb; j++) sum[j] = cnt[j] = 0;
       for (int i = 0; i < 16; i++) {
-        float md = 255.0f;
+        const uint32_t av = (cl_pixel(c, i) >> (8 * ch)) & 0xFF;
+        const uint32_t b = (uint32_t)((bk >> (4 * i)) & 15);
+#pragma unroll
         for (int j = 0; j < nb; j++) {
-          const float d = fabsf(__fsub_rn(avals[i], vals[j]));
+          sum[j] += b == (uint32_t)j ? av : 0u;
+          cnt[j] += b == (uint32_t)j ? 1u : 0u;
+        }
+      }
+      float avg[nb];
+      fixed = true;
+#pragma unroll
+      for (int j = 0; j < nb; j++) {
+        npts[j] = (float)cnt[j];
+        avg[j] = (float)sum[j];
+        if (npts[j] > 0.0f) avg[j] = __fdiv_rn(avg[j], npts[j]);
+        fixed = fixed && (avg[j] == vals[j]);
+        vals[j] = avg[j];
+      }
+      bk = 0;
+      for (int i = 0; i < 16; i++) {
+        const float av = cl_alpha(c, i, ch);
+        float md = 255.0f;
+        uint32_t b = 0;
+#pragma unroll
+        for (int j = 0; j < nb; j++) {
+          const float d = fabsf(__fsub_rn(av, vals[j]));
           if (d < md) {
             md = d;
-            bk[i] = (uint32_t)j;
+            b = (uint32_t)j;
           }
         }
+        bk |= (uint64_t)b << (4 * i);
       }
     }
     float asq = 0.0f, bsq = 0.0f, ab = 0.0f, ax = 0.0f, bx = 0.0f;
+#pragma unroll
     for (int j = 0; j < nb; j++) {
       const float fb = (float)(nb - 1);
       const float a = __fdiv_rn((float)(nb - 1 - j), fb), b = __fdiv_rn((float)j, fb);
@@ -1047,9 +1126,10 @@ __device__ inline void alpha_fit(const ModeCtx &m, const float *avals, float ami
     const uint32_t a2b = quantize_channel((uint32_t)a2 & 0xFF, amask, -1);
     aerr = 0.0;
     for (int i = 0; i < 16; i++) {
-      const uint32_t val = (uint32_t)avals[i];
+      const uint32_t val = (cl_pixel(c, i) >> (8 * ch)) & 0xFF;
       float me = FLT_MAX;
       uint32_t bb = 0;
+#pragma unroll
       for (int j = 0; j < nb; j++) {
         const uint32_t w1 = weight1(abits, (uint32_t)j), w0 = 64u - w1;
         const uint32_t ip = ((a1b * w0 + a2b * w1 + 32u) >> 6) & 0xFF;

@@ -515,7 +515,7 @@ __device__ __forceinline__ uint32_t class_begin(const uint16_t *local, const uin
 // One launch per class (the mode is a compile-time constant, so each
 // kernel holds only its own mode's path).
 template <int C>
-__global__ void __launch_bounds__(kSetupThreads) setup_kernel(
+__global__ void __launch_bounds__(kSetupThreads, 4) setup_kernel(
     const JobDev *__restrict__ jobs, uint32_t nb, const BlockSel *__restrict__ sel,
     const uint2 *__restrict__ desc, const uint16_t *__restrict__ local,
     const uint32_t *__restrict__ chunk, PipelineCounters *__restrict__ ctr,
@@ -560,6 +560,8 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     m.sct = g_sct;
     Cluster c;
     make_cluster(px, part_word_of(s, kMode, tk.slot), tk.subset, pts, kSetupThreads, c);
+    c.aux = px;  // the block's texels are not read again
+    c.aux_stride = 1;
     FitSetup st;
     st.idx = 0;
     st.pbit = 0;
@@ -567,10 +569,12 @@ __global__ void __launch_bounds__(kSetupThreads) setup_kernel(
     o.aerr = 0.0;
     o.aidx = 0;
     o.a1 = o.a2 = 0.0f;
-    if (kA.has_rotation) {
-      fit_alpha_setup(m, c, q_opt6, st, o.a1, o.a2, o.aidx, o.aerr);
+    constexpr int kNB = 1 << (class_im(C) ? kA.alpha_idx_bits : kA.idx_bits);
+    constexpr int kANB = 1 << (class_im(C) ? kA.idx_bits : kA.alpha_idx_bits);
+    if constexpr (kA.has_rotation != 0) {
+      fit_alpha_setup<kNB, kANB>(m, c, q_opt6, st, o.a1, o.a2, o.aidx, o.aerr);
     } else {
-      fit_rgb_setup(m, c, st);
+      fit_rgb_setup_t<kNB>(m, c, st);
     }
     o.err = st.err;
     o.idx = st.idx;
