@@ -765,7 +765,7 @@ __device__ inline void fit_rgb_setup_t(ModeCtx &m, const Cluster &c, FitSetup &s
     return;
   }
   constexpr int nb = kNB;
-  constexpr int kUnroll = kNB <= 8 ? kNB : 1;
+  constexpr int kUnroll = kNB;
   float axis[4];
   principal_axis(c, axis);
   float mindp = FLT_MAX, maxdp = -FLT_MAX;
@@ -825,7 +825,7 @@ __device__ inline void fit_rgb_setup_t(ModeCtx &m, const Cluster &c, FitSetup &s
       const uint64_t add = (uint64_t)(q & 0xFF) | ((uint64_t)((q >> 8) & 0xFF) << 13) |
                            ((uint64_t)((q >> 16) & 0xFF) << 26) | ((uint64_t)(q >> 24) << 39) |
                            (1ull << 52);
-#pragma unroll kUnroll
+#pragma unroll
       for (int j = 0; j < nb; j++) acc[j] += j == minb ? add : 0ull;
     }
     fixed = true;
