@@ -95,7 +95,8 @@ size_t rank_scratch_bytes(uint64_t total) {
 
 size_t scratch_bytes(uint64_t total, int engine, int task_bound) {
   size_t b = rank_scratch_bytes(total);
-  if (engine == FASTC_BC7_ENGINE_PIPELINE) b += fastc::pipeline_scratch_bytes(total, task_bound);
+  if (engine == FASTC_BC7_ENGINE_PIPELINE)
+    b += fastc::pipeline_scratch_bytes(total, task_bound, fastc::device_sm_count(current_device()));
   return b;
 }
 

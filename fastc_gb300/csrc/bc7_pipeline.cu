@@ -478,6 +478,8 @@ __global__ void __launch_bounds__(1024) scan_chunks_kernel(uint32_t *chunk, uint
   if (threadIdx.x < kClasses) {
     ctr->anneal_next[threadIdx.x] = 0ull;
     ctr->anneal_count[threadIdx.x] = 0u;
+    ctr->cont_next[threadIdx.x] = 0ull;
+    ctr->cont_count[threadIdx.x] = 0u;
   }
   if (threadIdx.x == 0) ctr->tasks = s_carry;
 }
@@ -603,10 +605,12 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 2 : 4)) s
       for (int q = 0; q < 4; q++)
         r[q] = make_uint4(pts[(4 * q + 0) * kSetupThreads], pts[(4 * q + 1) * kSetupThreads],
                           pts[(4 * q + 2) * kSetupThreads], pts[(4 * q + 3) * kSetupThreads]);
+      const uint32_t ef = __float_as_uint((float)o.err);
       r[4] = make_uint4((uint32_t)c.tex, (uint32_t)(c.tex >> 32), o.p1, o.p2);
-      r[5] = make_uint4(__float_as_uint((float)o.err), o.lcg, t,
+      r[5] = make_uint4(ef, o.lcg, t,
                         (uint32_t)o.steps | ((uint32_t)c.n << 16) | ((uint32_t)o.pbit << 24));
-      r[6] = make_uint4((uint32_t)tk.rot | ((uint32_t)o.flags << 8), 0u, 0u, 0u);
+      r[6] = make_uint4((uint32_t)tk.rot | ((uint32_t)o.flags << 8), o.p1, o.p2, ef);
+      r[7] = make_uint4((uint32_t)o.pbit, 0u, 0u, 0u);
     }
   }
 }
@@ -617,6 +621,7 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 2 : 4)) s
 // ---------------------------------------------------------------------------
 
 constexpr int kAnnealThreads = kLaneStride;
+constexpr int kYieldLanes = 12;
 
 // ToPixel (RGBAEndpoints.cpp:167-177) of integer endpoints through the table.
 template <int kColorBits, int kAlphaBits>
@@ -743,6 +748,7 @@ struct Lane {
   float w[4];
   int se;         // sum of |e|^2 over the fit's texels
   uint32_t psel;  // byte selector of the projected point (rotation modes)
+  int rot;
   bool uniform;
 };
 
@@ -846,16 +852,23 @@ __device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t (&ereg)[16],
   return false;
 }
 
-template <int C>
+// kCont = false: the class's list of fits from the setup stage. When that
+// list is empty, a warp with at most kYieldLanes lanes still annealing
+// writes their fits, mid-flight, to the class's continuation list and
+// exits, instead of running on with most lanes idle (fit lengths vary about
+// threefold). kCont = true: the continuation list, run to completion.
+template <int C, bool kCont>
 __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
     uint32_t nb, const uint16_t *__restrict__ local, const uint32_t *__restrict__ chunk,
     PipelineCounters *__restrict__ ctr, const AnnealRec *__restrict__ arec,
-    TaskState *__restrict__ state) {
+    AnnealRec *__restrict__ cont, uint32_t cont_cap, TaskState *__restrict__ state) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr a = mode_attr(kMode);
   constexpr int kBits = class_im(C) ? a.alpha_idx_bits : a.idx_bits;
   constexpr bool kRot = a.has_rotation != 0;
   constexpr int T = kAnnealThreads;
+  AnnealRec *clist = cont + (size_t)C * cont_cap;
+  if (kCont && blockIdx.x * (uint32_t)T >= ctr->cont_count[C]) return;
   __shared__ uint8_t s_lut[8 * 3 * 256];
   __shared__ uint32_t s_pts[16 * T];
   __shared__ uint32_t s_proj[kRot ? 16 * T : 1];
@@ -867,8 +880,9 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   uint32_t *proj = kRot ? s_proj + threadIdx.x : pts;
   uint4 *pal = s_pal + threadIdx.x;
   uint32_t *palf = reinterpret_cast<uint32_t *>(s_pal) + threadIdx.x;  // float-metric palette
-  const uint32_t count = ctr->anneal_count[C];
-  const uint32_t base = scanned(local, chunk, (uint64_t)C * nb);
+  const uint32_t count = kCont ? ctr->cont_count[C] : ctr->anneal_count[C];
+  const AnnealRec *list = kCont ? clist : arec + scanned(local, chunk, (uint64_t)C * nb);
+  unsigned long long *cursor = kCont ? &ctr->cont_next[C] : &ctr->anneal_next[C];
   Lane s;
   uint32_t ereg[16];
   bool active = false, exhausted = false;
@@ -878,32 +892,37 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
     if (nmask) {
       unsigned long long b0 = 0;
       const int leader = __ffs(nmask) - 1;
-      if (lane == leader) b0 = atomicAdd(&ctr->anneal_next[C], (unsigned long long)__popc(nmask));
+      if (lane == leader) b0 = atomicAdd(cursor, (unsigned long long)__popc(nmask));
       b0 = __shfl_sync(0xFFFFFFFFu, b0, leader);
       if (need) {
         const unsigned long long k = b0 + __popc(nmask & ((1u << lane) - 1u));
         if (k >= count) {
           exhausted = true;
         } else {
-          const uint4 *r = reinterpret_cast<const uint4 *>(arec + base + (uint32_t)k);
-          uint4 v[7];
+          const uint4 *r = reinterpret_cast<const uint4 *>(list + (uint32_t)k);
+          uint4 v[8];
 #pragma unroll
-          for (int q = 0; q < 7; q++) v[q] = __ldg(r + q);
+          for (int q = 0; q < 8; q++) v[q] = kCont ? r[q] : __ldg(r + q);
           const int rot = (int)(v[6].x & 0xFF);
           const uint32_t flags = (v[6].x >> 8) & 0xFF;
           s.t = v[5].z;
-          s.p1 = s.b1 = v[4].z;
-          s.p2 = s.b2 = v[4].w;
-          s.cur_pbit = s.best_pbit = (int)(v[5].w >> 24);
-          s.cur_err = s.best_err = __uint_as_float(v[5].x);
+          s.p1 = v[4].z;
+          s.p2 = v[4].w;
+          s.b1 = v[6].y;
+          s.b2 = v[6].z;
+          s.cur_pbit = (int)(v[5].w >> 24);
+          s.best_pbit = (int)(v[7].x & 0xFF);
+          s.cur_err = __uint_as_float(v[5].x);
+          s.best_err = __uint_as_float(v[6].w);
           s.lcg = v[5].y;
-          s.energy = 0;
+          s.energy = (int)(v[6].x >> 16);
           s.steps = (int)(v[5].w & 0xFFFF);
           s.n = (int)((v[5].w >> 16) & 0xFF);
           s.tex = (uint64_t)v[4].x | ((uint64_t)v[4].y << 32);
           s.uniform = !(flags & kTaskNonuniform);
           // projected point: channel rot-1 takes the texel's alpha, alpha is 255
           s.psel = rot ? (0x4210u & ~(0xFu << (4 * (rot - 1)))) | (3u << (4 * (rot - 1))) : 0x4210u;
+          s.rot = rot;
           ModeCtx m;
           m.a = a;
           m.rot = rot;
@@ -928,6 +947,32 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
       }
     }
     if (__all_sync(0xFFFFFFFFu, exhausted && !active)) break;
+    if (!kCont) {
+      const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
+      if (__any_sync(0xFFFFFFFFu, exhausted) && __popc(act) <= kYieldLanes) {
+        // hand the unfinished fits on and retire the warp
+        const int leader = __ffs(act) - 1;
+        uint32_t pos = 0;
+        if (lane == leader) pos = atomicAdd(&ctr->cont_count[C], (uint32_t)__popc(act));
+        pos = __shfl_sync(0xFFFFFFFFu, pos, leader) + __popc(act & ((1u << lane) - 1u));
+        if (active) {
+          // the list holds one record per lane of the grid, so pos < cont_cap
+          uint4 *w = reinterpret_cast<uint4 *>(clist + pos);
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+            w[q] = make_uint4(pts[(4 * q + 0) * T], pts[(4 * q + 1) * T], pts[(4 * q + 2) * T],
+                              pts[(4 * q + 3) * T]);
+          w[4] = make_uint4((uint32_t)s.tex, (uint32_t)(s.tex >> 32), s.p1, s.p2);
+          w[5] = make_uint4(__float_as_uint(s.cur_err), s.lcg, s.t,
+                            (uint32_t)s.steps | ((uint32_t)s.n << 16) | ((uint32_t)s.cur_pbit << 24));
+          w[6] = make_uint4((uint32_t)s.rot | ((s.uniform ? 0u : (uint32_t)kTaskNonuniform) << 8) |
+                                ((uint32_t)s.energy << 16),
+                            s.b1, s.b2, __float_as_uint(s.best_err));
+          w[7] = make_uint4((uint32_t)s.best_pbit, 0u, 0u, 0u);
+        }
+        break;
+      }
+    }
     if (active) {
       if (anneal_step<C>(s, ereg, pts, proj, pal, palf, s_lut)) {
         // the indices of the best endpoints are recomputed by the pack
@@ -1143,8 +1188,16 @@ static void set_pack_attributes() {
 
 namespace {
 
+// Continuation records per class: one per lane of an annealing grid at
+// most (a lane hands on at most one fit), and never more than the tasks.
+uint64_t cont_capacity(uint64_t nb, int tb, int sm_count) {
+  const uint64_t lanes = (uint64_t)sm_count * 2048u;  // resident threads per SM
+  const uint64_t tasks = (uint64_t)tb * nb;
+  return lanes < tasks ? lanes : tasks;
+}
+
 // Bytes of one chunk buffer for chunks of at most nb blocks.
-size_t chunk_buffer_bytes(uint64_t nb, int tb) {
+size_t chunk_buffer_bytes(uint64_t nb, int tb, int sm_count) {
   const uint64_t n8 = (uint64_t)kClasses * nb;
   const uint64_t tmax = (uint64_t)tb * nb;
   size_t b = 256;  // PipelineCounters
@@ -1155,6 +1208,7 @@ size_t chunk_buffer_bytes(uint64_t nb, int tb) {
   b += (tmax * sizeof(uint2) + 255) & ~255ull;
   b += (tmax * sizeof(TaskState) + 255) & ~255ull;
   b += (tmax * sizeof(AnnealRec) + 255) & ~255ull;
+  b += (kClasses * cont_capacity(nb, tb, sm_count) * sizeof(AnnealRec) + 255) & ~255ull;
   return b;
 }
 
@@ -1167,9 +1221,11 @@ struct ChunkBuf {
   uint2 *desc;
   TaskState *state;
   AnnealRec *arec;
+  AnnealRec *cont;
+  uint32_t cont_cap;
 };
 
-ChunkBuf carve_chunk(uint8_t *p, uint64_t nb, int tb) {
+ChunkBuf carve_chunk(uint8_t *p, uint64_t nb, int tb, int sm_count) {
   ChunkBuf c;
   c.ctr = reinterpret_cast<PipelineCounters *>(p);
   p += 256;
@@ -1186,6 +1242,9 @@ ChunkBuf carve_chunk(uint8_t *p, uint64_t nb, int tb) {
   c.state = reinterpret_cast<TaskState *>(p);
   p += ((uint64_t)tb * nb * sizeof(TaskState) + 255) & ~255ull;
   c.arec = reinterpret_cast<AnnealRec *>(p);
+  p += ((uint64_t)tb * nb * sizeof(AnnealRec) + 255) & ~255ull;
+  c.cont = reinterpret_cast<AnnealRec *>(p);
+  c.cont_cap = (uint32_t)cont_capacity(nb, tb, sm_count);
   return c;
 }
 
@@ -1218,11 +1277,11 @@ int block_task_bound(uint32_t modes) {
   return worst;
 }
 
-size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound) {
+size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound, int sm_count) {
   const uint64_t cap = pipeline_chunk(task_bound);
   const uint64_t nb = total_blocks < cap ? total_blocks : cap;
   const int nbuf = total_blocks > cap ? 2 : 1;
-  return (size_t)nbuf * chunk_buffer_bytes(nb, task_bound);
+  return (size_t)nbuf * chunk_buffer_bytes(nb, task_bound, sm_count);
 }
 
 cudaError_t class_streams_create(ClassStreams *cs) {
@@ -1264,6 +1323,8 @@ struct ChunkArgs {
   PipelineCounters *ctr;
   TaskState *state;
   AnnealRec *arec;
+  AnnealRec *cont;
+  uint32_t cont_cap;
   uint32_t *status;
   int sm_count;
 };
@@ -1281,12 +1342,14 @@ int resident_ctas(K kernel, int threads) {
 template <int C>
 void launch_class(const ChunkArgs &a, cudaStream_t s) {
   // the annealing kernel is persistent: no more CTAs than can be resident
-  static const int anneal_per_sm = resident_ctas(anneal_kernel<C>, kAnnealThreads);
+  static const int anneal_per_sm = resident_ctas(anneal_kernel<C, false>, kAnnealThreads);
   setup_kernel<C><<<a.sm_count * 8, kSetupThreads, 0, s>>>(a.jobs, a.nb, a.sel, a.desc, a.local,
                                                            a.chunk, a.ctr, a.state, a.arec,
                                                            a.status);
-  anneal_kernel<C><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(a.nb, a.local, a.chunk,
-                                                                         a.ctr, a.arec, a.state);
+  anneal_kernel<C, false><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
+      a.nb, a.local, a.chunk, a.ctr, a.arec, a.cont, a.cont_cap, a.state);
+  anneal_kernel<C, true><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
+      a.nb, a.local, a.chunk, a.ctr, a.arec, a.cont, a.cont_cap, a.state);
 }
 
 void launch_class_any(int c, const ChunkArgs &a, cudaStream_t s) {
@@ -1325,9 +1388,10 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
   const uint64_t cap = pipeline_chunk(tb);
   const uint64_t nbmax = total < cap ? total : cap;
   ChunkBuf bufs[2];
-  bufs[0] = carve_chunk(static_cast<uint8_t *>(scratch), nbmax, tb);
-  bufs[1] = total > cap ? carve_chunk(static_cast<uint8_t *>(scratch) + chunk_buffer_bytes(nbmax, tb),
-                                      nbmax, tb)
+  bufs[0] = carve_chunk(static_cast<uint8_t *>(scratch), nbmax, tb, sm_count);
+  bufs[1] = total > cap ? carve_chunk(static_cast<uint8_t *>(scratch) +
+                                          chunk_buffer_bytes(nbmax, tb, sm_count),
+                                      nbmax, tb, sm_count)
                         : bufs[0];
   auto pack = [&](const ChunkBuf &b, uint32_t nb, int parity) -> int {
     if (cls) {
@@ -1353,8 +1417,8 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     scan_local_u8_kernel<<<nchunks, kRankChunk, 0, st>>>(b.counts, n8, b.local, b.chunk);
     scan_chunks_kernel<<<1, 1024, 0, st>>>(b.chunk, nchunks, b.ctr);
     emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, b.counts, b.local, b.chunk, b.desc);
-    const ChunkArgs args{jobs, nb, b.sel, b.desc, b.local, b.chunk, b.ctr, b.state, b.arec,
-                         rank.status, sm_count};
+    const ChunkArgs args{jobs,   nb,      b.sel,      b.desc,      b.local,  b.chunk, b.ctr,
+                         b.state, b.arec, b.cont, b.cont_cap, rank.status, sm_count};
     if (cls) {
       cudaError_t ce = cudaEventRecord(cls->fork[i & 1], st);
       const cudaStream_t *side = cls->side[i & 1];

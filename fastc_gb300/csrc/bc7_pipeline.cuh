@@ -64,26 +64,34 @@ __host__ __device__ constexpr int class_of(int mode, int im) {
 }
 
 // A fit that anneals, as the setup stage hands it to its class's annealing
-// list: everything the loop needs, in one 112-byte record, so that taking
-// the next fit is one atomic and seven 16-byte loads.
+// list, or as a sparse warp hands an unfinished fit on (a continuation):
+// everything the loop needs in one 128-byte record, so that taking the next
+// fit is one atomic and eight 16-byte loads.
 struct __align__(16) AnnealRec {
   uint32_t pts[16];  // the cluster's texels in texel order (first n used)
   uint64_t tex;      // texel index of each point, 4 bits per point
-  uint32_t p1, p2;   // starting endpoints (grid values, one byte per channel)
+  uint32_t p1, p2;   // current endpoints (grid values, one byte per channel)
   float err;         // their QuantizedError
   uint32_t lcg;      // annealing stream of this fit
   uint32_t t;        // task index: where the result goes
   uint16_t steps;
-  uint8_t n, pbit;
-  uint8_t rot, flags, pad[6];
+  uint8_t n, pbit;   // point count, current p-bit combination
+  uint8_t rot, flags;
+  uint16_t energy;   // steps since the last improvement
+  uint32_t b1, b2;   // best endpoints so far
+  float best_err;
+  uint8_t best_pbit, pad[15];
 };
-static_assert(sizeof(AnnealRec) == 112, "AnnealRec layout");
+static_assert(sizeof(AnnealRec) == 128, "AnnealRec layout");
 
 struct PipelineCounters {
   unsigned long long anneal_next[kClasses];  // refill cursors of the annealing lists
   uint32_t anneal_count[kClasses];           // fits of each class that anneal
   uint32_t tasks;                            // tasks in the current chunk
+  unsigned long long cont_next[kClasses];    // refill cursors of the continuation lists
+  uint32_t cont_count[kClasses];             // continuations of each class
 };
+static_assert(sizeof(PipelineCounters) <= 256, "PipelineCounters fits its slot");
 
 // Side streams that run the classes' setup + annealing concurrently, forked
 // from and joined back into the caller's stream with events (both are
@@ -102,7 +110,8 @@ void class_streams_destroy(ClassStreams *cs);
 void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t opt6[256]);
 // Most cluster fits a block can need when the caller enables `modes`.
 int block_task_bound(uint32_t modes);
-size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound);
+// sm_count: of the device that runs the launch (bounds the continuation lists).
+size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound, int sm_count);
 // `cls` null: every stage runs in order on `stream`. `task_bound`: the most
 // block_task_bound() of the jobs' masks.
 int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
