@@ -1339,11 +1339,32 @@ int resident_ctas(K kernel, int threads) {
   return n;
 }
 
+// Most fits of class C one block can have: four rotations per shape slot
+// for the rotation modes, one fit per subset otherwise; one-subset modes
+// repeat for both shape slots.
+constexpr int class_block_fits(int c) {
+  return mode_attr(class_mode(c)).has_rotation ? 8
+         : mode_attr(class_mode(c)).subsets == 1 ? 2
+                                                  : mode_attr(class_mode(c)).subsets;
+}
+
+// Annealing CTAs per SM: below the resident limit, so that setup and select
+// CTAs of other chunks and classes share the SMs (measured best on the
+// texture-set workload).
+constexpr int kAnnealCtasPerSm = 5;
+
 template <int C>
 void launch_class(const ChunkArgs &a, cudaStream_t s) {
   // the annealing kernel is persistent: no more CTAs than can be resident
-  static const int anneal_per_sm = resident_ctas(anneal_kernel<C, false>, kAnnealThreads);
-  setup_kernel<C><<<a.sm_count * 8, kSetupThreads, 0, s>>>(a.jobs, a.nb, a.sel, a.desc, a.local,
+  static const int anneal_res = resident_ctas(anneal_kernel<C, false>, kAnnealThreads);
+  const int anneal_per_sm = anneal_res < kAnnealCtasPerSm ? anneal_res : kAnnealCtasPerSm;
+  // setup: one thread per fit (latency-bound; threads past the class's
+  // fits return at once)
+  const uint64_t fits = (uint64_t)a.nb * class_block_fits(C);
+  const uint64_t setup_ctas_max = (uint64_t)a.sm_count * 128;
+  uint64_t setup_ctas = (fits + kSetupThreads - 1) / kSetupThreads;
+  if (setup_ctas > setup_ctas_max) setup_ctas = setup_ctas_max;
+  setup_kernel<C><<<(unsigned)setup_ctas, kSetupThreads, 0, s>>>(a.jobs, a.nb, a.sel, a.desc, a.local,
                                                            a.chunk, a.ctr, a.state, a.arec,
                                                            a.status);
   anneal_kernel<C, false><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
