@@ -87,8 +87,6 @@ static uint8_t host_quantize(uint32_t val, uint32_t mask, int pbit) {
   return (uint8_t)(dl < dh ? l8 : h8);
 }
 
-static void set_pack_attributes();  // after pack_kernel
-
 void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t opt6[256]) {
   static bool done[64] = {false};
   if (device < 0 || device >= 64 || done[device]) return;
@@ -102,7 +100,6 @@ void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t
   cudaMemcpyToSymbol(q_opt6, opt6, 256 * sizeof(uint32_t));
   build_sct_kernel<<<kSctRows, 256>>>();
   cudaDeviceSynchronize();
-  set_pack_attributes();
   done[device] = true;
 }
 
@@ -480,6 +477,7 @@ __global__ void __launch_bounds__(1024) scan_chunks_kernel(uint32_t *chunk, uint
     ctr->anneal_count[threadIdx.x] = 0u;
     ctr->cont_next[threadIdx.x] = 0ull;
     ctr->cont_count[threadIdx.x] = 0u;
+    ctr->reindex_count[threadIdx.x] = 0u;
   }
   if (threadIdx.x == 0) ctr->tasks = s_carry;
 }
@@ -867,6 +865,9 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   constexpr int kBits = class_im(C) ? a.alpha_idx_bits : a.idx_bits;
   constexpr bool kRot = a.has_rotation != 0;
   constexpr int T = kAnnealThreads;
+  // only classes with long fits (the rotation modes) hand fits on; short
+  // fits drain quickly
+  constexpr bool kYields = kRot;
   AnnealRec *clist = cont + (size_t)C * cont_cap;
   if (kCont && blockIdx.x * (uint32_t)T >= ctr->cont_count[C]) return;
   __shared__ uint8_t s_lut[8 * 3 * 256];
@@ -947,7 +948,7 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
       }
     }
     if (__all_sync(0xFFFFFFFFu, exhausted && !active)) break;
-    if (!kCont) {
+    if (!kCont && kYields) {
       const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
       if (__any_sync(0xFFFFFFFFu, exhausted) && __popc(act) <= kYieldLanes) {
         // hand the unfinished fits on and retire the warp
@@ -1052,51 +1053,30 @@ __device__ __noinline__ uint64_t fit_indices(const TaskState &o, const uint32_t 
   return idx;
 }
 
-__device__ __forceinline__ uint64_t fit_indices_any(int c, const TaskState &o, const uint32_t *px,
-                                                    uint32_t part, const uint8_t *lut, uint32_t *pts,
-                                                    uint32_t *proj, uint4 *pal, uint32_t *palf) {
-  switch (c) {
-    case 0: return fit_indices<0>(o, px, part, lut, pts, proj, pal, palf);
-    case 1: return fit_indices<1>(o, px, part, lut, pts, proj, pal, palf);
-    case 2: return fit_indices<2>(o, px, part, lut, pts, proj, pal, palf);
-    case 3: return fit_indices<3>(o, px, part, lut, pts, proj, pal, palf);
-    case 4: return fit_indices<4>(o, px, part, lut, pts, proj, pal, palf);
-    case 5: return fit_indices<5>(o, px, part, lut, pts, proj, pal, palf);
-    case 6: return fit_indices<6>(o, px, part, lut, pts, proj, pal, palf);
-    case 7: return fit_indices<7>(o, px, part, lut, pts, proj, pal, palf);
-    default: return fit_indices<8>(o, px, part, lut, pts, proj, pal, palf);
-  }
+constexpr int kPackThreads = kLaneStride;
+
+// The winning fit of a block: mode | slot << 4 | rotation << 8 | index mode
+// << 12 (mode 8: no fit, 9: block already written), first task index.
+__device__ __forceinline__ uint2 make_winner(int mode, int slot, int rot, int im, uint32_t first) {
+  return make_uint2((uint32_t)mode | ((uint32_t)slot << 4) | ((uint32_t)rot << 8) | ((uint32_t)im << 12),
+                    first);
 }
 
-constexpr int kPackThreads = kLaneStride;
-constexpr size_t kPackDynSmem = (size_t)kPackThreads * (16 * sizeof(uint4) + 3 * 16 * sizeof(uint32_t));
-
-__global__ void __launch_bounds__(kPackThreads) pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
-                            const BlockSel *__restrict__ sel, const uint16_t *__restrict__ local,
-                            const uint32_t *__restrict__ chunk,
-                            const TaskState *__restrict__ state) {
-  __shared__ uint32_t s_part2[64], s_part3[64];
-  __shared__ uint8_t s_anc2[64], s_anc3[64];
-  __shared__ uint8_t s_lut[8 * 3 * 256];
-  // per-thread arrays of the index recomputation (kPackDynSmem bytes)
-  extern __shared__ uint4 s_dyn[];
-  uint4 *s_pal = s_dyn;                                                  // 16 entries
-  uint32_t *s_px = reinterpret_cast<uint32_t *>(s_dyn + 16 * kPackThreads);  // 16 words
-  uint32_t *s_pts = s_px + 16 * kPackThreads;
-  uint32_t *s_proj = s_pts + 16 * kPackThreads;
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
-    s_part2[i] = q_part2[i];
-    s_part3[i] = q_part3[i];
-    s_anc2[i] = q_anchor2[i];
-    s_anc3[i] = q_anchor3[i];
-  }
-  for (int i = threadIdx.x; i < 8 * 3 * 256; i += blockDim.x) s_lut[i] = (&q_qlut[0][0][0])[i];
-  __syncthreads();
+// Per block: FasTC's arg-min over modes and shape slots (CompressClusters,
+// CP:1752-1817, strict <, mode order {0,2,1,3,7,4,5,6}); the winner's
+// annealed fits go to their class's re-index list.
+__global__ void __launch_bounds__(kPackThreads) choose_kernel(
+    uint32_t nb, const BlockSel *__restrict__ sel, const uint16_t *__restrict__ local,
+    const uint32_t *__restrict__ chunk, const TaskState *__restrict__ state,
+    PipelineCounters *__restrict__ ctr, uint2 *__restrict__ win, uint32_t *__restrict__ rlist,
+    uint32_t rcap) {
   const uint32_t gl = blockIdx.x * blockDim.x + threadIdx.x;
   if (gl >= nb) return;
   const BlockSel bs = sel[gl];
-  if (bs.done) return;
-  const JobDev &jb = jobs[bs.job];
+  if (bs.done) {
+    win[gl] = make_winner(9, 0, 0, 0, 0);
+    return;
+  }
   const Selection s = sel_of(bs);
   const uint32_t modes = bs.modes;
   double best = DBL_MAX;
@@ -1148,38 +1128,94 @@ __global__ void __launch_bounds__(kPackThreads) pack_kernel(const JobDev *__rest
       }
     }
   }
+  win[gl] = make_winner(best_mode, best_slot, best_rot, best_im, best_first);
+  if (best_mode == 8) return;
+  const int ns = mode_attr(best_mode).subsets;
+  for (int k = 0; k < ns; k++) {
+    const uint32_t tt = best_first + (uint32_t)k;
+    if (!(state[tt].flags & kTaskAnneal)) continue;
+    const int c = class_of(best_mode, best_im);
+    const uint32_t pos = atomicAdd(&ctr->reindex_count[c], 1u);
+    rlist[(size_t)c * rcap + pos] = tt;  // at most one winner per block and 3 subsets: pos < rcap
+  }
+}
+
+// One thread per annealed winning fit of class C: its indices at the best
+// endpoints (the QuantizedError call that ends the annealing, CP:626-629).
+template <int C>
+__global__ void __launch_bounds__(kPackThreads) reindex_kernel(
+    const JobDev *__restrict__ jobs, const BlockSel *__restrict__ sel,
+    const PipelineCounters *__restrict__ ctr, const uint32_t *__restrict__ rlist, uint32_t rcap,
+    TaskState *__restrict__ state) {
+  constexpr int T = kPackThreads;
+  constexpr ModeAttr kA = mode_attr(class_mode(C));
+  constexpr bool kN16 = kA.subsets == 1;  // the points are the block's texels, in order
+  constexpr bool kRot = kA.has_rotation != 0;
+  const uint32_t count = ctr->reindex_count[C];
+  if (blockIdx.x * (uint32_t)T >= count) return;
+  __shared__ uint8_t s_lut[8 * 3 * 256];
+  __shared__ uint32_t s_px[16 * T], s_pts[kN16 ? 1 : 16 * T], s_proj[kRot ? 16 * T : 1];
+  __shared__ uint4 s_pal[(1 << (class_im(C) ? mode_attr(class_mode(C)).alpha_idx_bits
+                                            : mode_attr(class_mode(C)).idx_bits)) * T];
+  for (int i = threadIdx.x; i < 8 * 3 * 256; i += blockDim.x) s_lut[i] = (&q_qlut[0][0][0])[i];
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * T + threadIdx.x; i < count; i += gridDim.x * T) {
+    const uint32_t tt = rlist[(size_t)C * rcap + i];
+    TaskState &o = state[tt];
+    const BlockSel bs = sel[o.gl];
+    const JobDev &jb = jobs[bs.job];
+    uint32_t *px = s_px + threadIdx.x;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const uint4 v = load_row_p(jb, bs.lin, r);
+      px[(4 * r + 0) * T] = v.x;
+      px[(4 * r + 1) * T] = v.y;
+      px[(4 * r + 2) * T] = v.z;
+      px[(4 * r + 3) * T] = v.w;
+    }
+    const uint32_t part = part_word_of(sel_of(bs), class_mode(C), o.slot);
+    const TaskState oc = o;
+    uint32_t *pts = kN16 ? px : s_pts + threadIdx.x;
+    uint32_t *proj = kRot ? s_proj + threadIdx.x : pts;
+    o.idx = fit_indices<C>(oc, px, part, s_lut, pts, proj, s_pal + threadIdx.x,
+                           reinterpret_cast<uint32_t *>(s_pal) + threadIdx.x);
+  }
+}
+
+// Per block: the 128-bit packing of the winner (CompressionMode::Pack,
+// CP:1096-1298).
+__global__ void __launch_bounds__(kPackThreads) pack_kernel(const JobDev *__restrict__ jobs, uint32_t nb,
+                            const BlockSel *__restrict__ sel, const uint2 *__restrict__ win,
+                            const TaskState *__restrict__ state) {
+  __shared__ uint32_t s_part2[64], s_part3[64];
+  __shared__ uint8_t s_anc2[64], s_anc3[64];
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+    s_part2[i] = q_part2[i];
+    s_part3[i] = q_part3[i];
+    s_anc2[i] = q_anchor2[i];
+    s_anc3[i] = q_anchor3[i];
+  }
+  __syncthreads();
+  const uint32_t gl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gl >= nb) return;
+  const uint2 w = win[gl];
+  const int best_mode = (int)(w.x & 15);
+  if (best_mode == 9) return;
+  const BlockSel bs = sel[gl];
+  const JobDev &jb = jobs[bs.job];
   uint32_t out[4];
   if (best_mode == 8) {
     out[0] = 1u << 6;
     out[1] = out[2] = out[3] = 0;
   } else {
+    const Selection s = sel_of(bs);
     FitOut f[3];
     const int ns = mode_attr(best_mode).subsets;
-    const uint32_t part = part_word_of(s, best_mode, best_slot);
-    uint32_t *px = s_px + threadIdx.x;
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-      const uint4 v = load_row_p(jb, bs.lin, r);
-      px[(4 * r + 0) * kPackThreads] = v.x;
-      px[(4 * r + 1) * kPackThreads] = v.y;
-      px[(4 * r + 2) * kPackThreads] = v.z;
-      px[(4 * r + 3) * kPackThreads] = v.w;
-    }
-    for (int k = 0; k < ns; k++) {
-      const TaskState o = state[best_first + k];
-      fit_out_of(o, f[k]);
-      if (o.flags & kTaskAnneal)
-        f[k].idx = fit_indices_any(class_of(o.mode, o.rotim & 1), o, px, part, s_lut,
-                                   s_pts + threadIdx.x, s_proj + threadIdx.x, s_pal + threadIdx.x,
-                                   reinterpret_cast<uint32_t *>(s_pal) + threadIdx.x);
-    }
-    pack_block(best_mode, s, best_slot, f, s_anc2, s_anc3, s_part2, s_part3, best_rot, best_im, out);
+    for (int k = 0; k < ns; k++) fit_out_of(state[w.y + k], f[k]);
+    pack_block(best_mode, s, (int)((w.x >> 4) & 15), f, s_anc2, s_anc3, s_part2, s_part3,
+               (int)((w.x >> 8) & 15), (int)((w.x >> 12) & 15), out);
   }
   store_block_p(jb, bs.lin, out);
-}
-
-static void set_pack_attributes() {
-  cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPackDynSmem);
 }
 
 // ---------------------------------------------------------------------------
@@ -1209,6 +1245,8 @@ size_t chunk_buffer_bytes(uint64_t nb, int tb, int sm_count) {
   b += (tmax * sizeof(TaskState) + 255) & ~255ull;
   b += (tmax * sizeof(AnnealRec) + 255) & ~255ull;
   b += (kClasses * cont_capacity(nb, tb, sm_count) * sizeof(AnnealRec) + 255) & ~255ull;
+  b += (nb * sizeof(uint2) + 255) & ~255ull;                      // winners
+  b += ((uint64_t)kClasses * 3 * nb * sizeof(uint32_t) + 255) & ~255ull;  // re-index lists
   return b;
 }
 
@@ -1223,6 +1261,9 @@ struct ChunkBuf {
   AnnealRec *arec;
   AnnealRec *cont;
   uint32_t cont_cap;
+  uint2 *win;
+  uint32_t *rlist;
+  uint32_t rcap;
 };
 
 ChunkBuf carve_chunk(uint8_t *p, uint64_t nb, int tb, int sm_count) {
@@ -1245,6 +1286,11 @@ ChunkBuf carve_chunk(uint8_t *p, uint64_t nb, int tb, int sm_count) {
   p += ((uint64_t)tb * nb * sizeof(AnnealRec) + 255) & ~255ull;
   c.cont = reinterpret_cast<AnnealRec *>(p);
   c.cont_cap = (uint32_t)cont_capacity(nb, tb, sm_count);
+  p += ((uint64_t)kClasses * c.cont_cap * sizeof(AnnealRec) + 255) & ~255ull;
+  c.win = reinterpret_cast<uint2 *>(p);
+  p += (nb * sizeof(uint2) + 255) & ~255ull;
+  c.rlist = reinterpret_cast<uint32_t *>(p);
+  c.rcap = (uint32_t)(3 * nb);
   return c;
 }
 
@@ -1369,8 +1415,9 @@ void launch_class(const ChunkArgs &a, cudaStream_t s) {
                                                            a.status);
   anneal_kernel<C, false><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
       a.nb, a.local, a.chunk, a.ctr, a.arec, a.cont, a.cont_cap, a.state);
-  anneal_kernel<C, true><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
-      a.nb, a.local, a.chunk, a.ctr, a.arec, a.cont, a.cont_cap, a.state);
+  if (mode_attr(class_mode(C)).has_rotation)
+    anneal_kernel<C, true><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
+        a.nb, a.local, a.chunk, a.ctr, a.arec, a.cont, a.cont_cap, a.state);
 }
 
 void launch_class_any(int c, const ChunkArgs &a, cudaStream_t s) {
@@ -1390,6 +1437,24 @@ void launch_class_any(int c, const ChunkArgs &a, cudaStream_t s) {
 // Classes in the order their work is enqueued: the longest first, so that
 // the short ones fill the tail.
 constexpr int kClassOrder[kClasses] = {6, 7, 5, 4, 3, 1, 8, 2, 0};
+
+template <int C>
+void reindex_class(const JobDev *jobs, const ChunkBuf &b, int sm_count, cudaStream_t st) {
+  reindex_kernel<C><<<sm_count * 4, kPackThreads, 0, st>>>(jobs, b.sel, b.ctr, b.rlist, b.rcap,
+                                                           b.state);
+}
+
+void reindex_all(const JobDev *jobs, const ChunkBuf &b, int sm_count, cudaStream_t st) {
+  reindex_class<0>(jobs, b, sm_count, st);
+  reindex_class<1>(jobs, b, sm_count, st);
+  reindex_class<2>(jobs, b, sm_count, st);
+  reindex_class<3>(jobs, b, sm_count, st);
+  reindex_class<4>(jobs, b, sm_count, st);
+  reindex_class<5>(jobs, b, sm_count, st);
+  reindex_class<6>(jobs, b, sm_count, st);
+  reindex_class<7>(jobs, b, sm_count, st);
+  reindex_class<8>(jobs, b, sm_count, st);
+}
 
 }  // namespace
 
@@ -1421,8 +1486,11 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
         if (ce != cudaSuccess) return (int)ce;
       }
     }
-    pack_kernel<<<(nb + kPackThreads - 1) / kPackThreads, kPackThreads, kPackDynSmem, st>>>(
-        jobs, nb, b.sel, b.local, b.chunk, b.state);
+    const unsigned ctas = (nb + kPackThreads - 1) / kPackThreads;
+    choose_kernel<<<ctas, kPackThreads, 0, st>>>(nb, b.sel, b.local, b.chunk, b.state, b.ctr, b.win,
+                                                 b.rlist, b.rcap);
+    reindex_all(jobs, b, sm_count, st);
+    pack_kernel<<<ctas, kPackThreads, 0, st>>>(jobs, nb, b.sel, b.win, b.state);
     return (int)cudaPeekAtLastError();
   };
   uint32_t prev_nb = 0;

@@ -90,6 +90,7 @@ struct PipelineCounters {
   uint32_t tasks;                            // tasks in the current chunk
   unsigned long long cont_next[kClasses];    // refill cursors of the continuation lists
   uint32_t cont_count[kClasses];             // continuations of each class
+  uint32_t reindex_count[kClasses];          // annealed winning fits of each class
 };
 static_assert(sizeof(PipelineCounters) <= 256, "PipelineCounters fits its slot");
 
