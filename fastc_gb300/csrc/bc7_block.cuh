@@ -166,6 +166,7 @@ __device__ inline void run_task(const Task &t, const Selection &sel, const uint3
   m.idx_mode = t.im;
   m.status = status;
   m.sct = nullptr;
+  m.pal = nullptr;
   m.lcg = fit_seed(jb.seed, bx, by,
                    (uint32_t)((t.mode << 8) | (t.slot << 7) | (t.subset << 4) | (t.rot << 1) | t.im));
   const uint32_t shape = sel.shape[t.slot];

@@ -24,6 +24,7 @@
 #include <cstdint>
 
 #include "bc7_format.cuh"
+#include "bc7_intqe.cuh"
 
 namespace fastc {
 
@@ -127,6 +128,9 @@ struct ModeCtx {
   uint32_t lcg;  // this fit's annealing stream
   uint32_t *status;
   const uint32_t *sct;  // single_color_table() results, or nullptr to search
+  // Palette scratch (stride kLaneStride) for the exact integer
+  // QuantizedError of the uniform metric; nullptr: the float restatement.
+  uint4 *pal;
 };
 
 // kErrorMetrics (CP:205-208)
@@ -887,13 +891,41 @@ __device__ inline void fit_rgb_setup_t(ModeCtx &m, const Cluster &c, FitSetup &s
   }
   clamp_to_grid(m, p1, p2, pbit);
   const uint32_t qm = qmask_of(m.a);
-  float w[4];
-  metric_of(m, w);
   const int pc = pbit_combo(m.a, (int)pbit);
-  st.errf = quantized_error(c, p1, p2, bits_index(m, -1), qm, w, pc, &idx);
   const bool hp = m.a.pbit != kPBitNone;
   const uint32_t q1 = to_pixel(p1, qm, hp ? pb_first(pc) : -1);
   const uint32_t q2 = to_pixel(p2, qm, hp ? pb_second(pc) : -1);
+  if (kNB <= 8 && m.pal && m.metric == 0 && c.stride == kLaneStride) {
+    // The same QuantizedError in exact integers (bc7_intqe.cuh); the
+    // points are the cluster's (rotated) points, the error pixels its
+    // texels, as in the float restatement, and the endpoints are quantized
+    // the way it quantizes them: with the combination's p-bits even for
+    // modes without p-bits (FasTC passes kPBits[0] there).
+    constexpr int kBits = kNB == 4 ? 2 : 3;
+    const uint32_t e1 = to_pixel(p1, qm, pb_first(pc));
+    const uint32_t e2 = to_pixel(p2, qm, pb_second(pc));
+    int se = 0;
+    for (int i = 0; i < c.n; i++) {
+      const uint32_t e = cl_pixel(c, i);
+      se += (int)__dp4a(e, e, 0u);
+    }
+    uint64_t ix = 0;
+    if (c.a255) {
+      uint32_t e[16];
+#pragma unroll
+      for (int k = 0; k < 16; k++) e[k] = cl_pixel(c, k);
+      uint32_t psel = 0x4210u;
+      if (c.rot) psel = (psel & ~(0xFu << (4 * (c.rot - 1)))) | (3u << (4 * (c.rot - 1)));
+      st.errf = qe_reg<kBits, true, true>(e, psel, se, m.pal, e1, e2, ix);
+    } else {
+      st.errf = qe_smem<kBits, true>(c.px, c.n, c.tex, se, m.pal, e1, e2, ix);
+    }
+    idx = ix;
+  } else {
+    float w[4];
+    metric_of(m, w);
+    st.errf = quantized_error(c, p1, p2, bits_index(m, -1), qm, w, pc, &idx);
+  }
   unpack4(q1, p1);
   unpack4(q2, p2);
   st.err = (double)st.errf;

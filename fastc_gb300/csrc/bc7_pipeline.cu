@@ -505,6 +505,7 @@ __global__ void emit_kernel(uint32_t nb, const uint8_t *__restrict__ counts,
 // ---------------------------------------------------------------------------
 
 constexpr int kSetupThreads = 128;
+static_assert(kSetupThreads == kLaneStride, "setup arrays use the lane stride");
 
 // First task of class C in the chunk's class-major task arrays.
 __device__ __forceinline__ uint32_t class_begin(const uint16_t *local, const uint32_t *chunk,
@@ -524,6 +525,9 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 2 : 4)) s
   constexpr ModeAttr kA = mode_attr(kMode);
   __shared__ uint32_t s_px[kSetupThreads * 17];
   __shared__ uint32_t s_pts[16 * kSetupThreads];
+  // palette of the integer QuantizedError (up to 8 entries; the 16-entry
+  // class uses the float restatement)
+  __shared__ uint4 s_pal[8 * kSetupThreads];
   uint32_t *px = s_px + threadIdx.x * 17;
   uint32_t *pts = s_pts + threadIdx.x;
   const uint32_t begin = class_begin(local, chunk, ctr, nb, C);
@@ -558,6 +562,7 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 2 : 4)) s
     m.status = status;
     m.lcg = 0;
     m.sct = g_sct;
+    m.pal = s_pal + threadIdx.x;
     Cluster c;
     make_cluster(px, part_word_of(s, kMode, tk.slot), tk.subset, pts, kSetupThreads, c);
     c.aux = px;  // the block's texels are not read again
