@@ -19,7 +19,7 @@ constexpr int kMaxBlockTasks = 32;
 // the bound is small. Launches of more than one chunk use two scratch
 // buffers so that the select stage of a chunk runs while the previous chunk
 // anneals.
-constexpr uint64_t kChunkTaskBudget = 8ull * 1024 * 1024;  // chunk blocks x task bound
+constexpr uint64_t kChunkTaskBudget = 16ull * 1024 * 1024;  // chunk blocks x task bound
 __host__ __device__ constexpr uint64_t pipeline_chunk(int task_bound) {
   return kChunkTaskBudget / (uint64_t)(task_bound > 16 ? 32 : 16);
 }
