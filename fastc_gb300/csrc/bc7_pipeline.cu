@@ -479,6 +479,7 @@ __global__ void __launch_bounds__(1024) scan_chunks_kernel(uint32_t *chunk, uint
     ctr->cont_count[threadIdx.x] = 0u;
     ctr->reindex_count[threadIdx.x] = 0u;
   }
+  if (threadIdx.x < kClasses * 17) (&ctr->nhist[0][0])[threadIdx.x] = 0u;
   if (threadIdx.x == 0) ctr->tasks = s_carry;
 }
 
@@ -520,7 +521,8 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 2 : 4)) s
     const JobDev *__restrict__ jobs, uint32_t nb, const BlockSel *__restrict__ sel,
     const uint2 *__restrict__ desc, const uint16_t *__restrict__ local,
     const uint32_t *__restrict__ chunk, PipelineCounters *__restrict__ ctr,
-    TaskState *__restrict__ state, AnnealRec *__restrict__ arec, uint32_t *status) {
+    TaskState *__restrict__ state, AnnealRec *__restrict__ arec, uint32_t *__restrict__ keys,
+    uint32_t *status) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr kA = mode_attr(kMode);
   __shared__ uint32_t s_px[kSetupThreads * 17];
@@ -614,7 +616,40 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 2 : 4)) s
                         (uint32_t)o.steps | ((uint32_t)c.n << 16) | ((uint32_t)o.pbit << 24));
       r[6] = make_uint4((uint32_t)tk.rot | ((uint32_t)o.flags << 8), o.p1, o.p2, ef);
       r[7] = make_uint4((uint32_t)o.pbit, 0u, 0u, 0u);
+      if (kA.subsets > 1) {
+        // rank among the class's fits with as many points (sorted below)
+        const uint32_t rank = atomicAdd(&ctr->nhist[C][c.n], 1u);
+        keys[begin + pos] = ((uint32_t)c.n << 24) | rank;
+      }
     }
+  }
+}
+
+// Multi-subset classes: the order in which the annealing lanes take the
+// class's fits, by point count (most points first), so that the lanes of a
+// warp loop over the same number of texels. perm[k] = list index of the
+// k-th fit to take.
+template <int C>
+__global__ void __launch_bounds__(128) order_kernel(uint32_t nb, const uint16_t *__restrict__ local,
+                                                    const uint32_t *__restrict__ chunk,
+                                                    const PipelineCounters *__restrict__ ctr,
+                                                    const uint32_t *__restrict__ keys,
+                                                    uint32_t *__restrict__ perm) {
+  __shared__ uint32_t s_off[17];
+  const uint32_t count = ctr->anneal_count[C];
+  if (blockIdx.x * blockDim.x >= count) return;
+  if (threadIdx.x == 0) {
+    uint32_t acc = 0;
+    for (int n = 16; n >= 0; n--) {
+      s_off[n] = acc;
+      acc += ctr->nhist[C][n];
+    }
+  }
+  __syncthreads();
+  const uint32_t base = scanned(local, chunk, (uint64_t)C * nb);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const uint32_t key = keys[base + i];
+    perm[base + s_off[key >> 24] + (key & 0xFFFFFFu)] = i;
   }
 }
 
@@ -864,7 +899,8 @@ template <int C, bool kCont>
 __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
     uint32_t nb, const uint16_t *__restrict__ local, const uint32_t *__restrict__ chunk,
     PipelineCounters *__restrict__ ctr, const AnnealRec *__restrict__ arec,
-    AnnealRec *__restrict__ cont, uint32_t cont_cap, TaskState *__restrict__ state) {
+    const uint32_t *__restrict__ perm, AnnealRec *__restrict__ cont, uint32_t cont_cap,
+    TaskState *__restrict__ state) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr a = mode_attr(kMode);
   constexpr int kBits = class_im(C) ? a.alpha_idx_bits : a.idx_bits;
@@ -887,7 +923,9 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   uint4 *pal = s_pal + threadIdx.x;
   uint32_t *palf = reinterpret_cast<uint32_t *>(s_pal) + threadIdx.x;  // float-metric palette
   const uint32_t count = kCont ? ctr->cont_count[C] : ctr->anneal_count[C];
-  const AnnealRec *list = kCont ? clist : arec + scanned(local, chunk, (uint64_t)C * nb);
+  const uint32_t lbase = scanned(local, chunk, (uint64_t)C * nb);
+  const AnnealRec *list = kCont ? clist : arec + lbase;
+  constexpr bool kOrdered = !kCont && a.subsets > 1;  // taken in point-count order
   unsigned long long *cursor = kCont ? &ctr->cont_next[C] : &ctr->anneal_next[C];
   Lane s;
   uint32_t ereg[16];
@@ -905,7 +943,8 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
         if (k >= count) {
           exhausted = true;
         } else {
-          const uint4 *r = reinterpret_cast<const uint4 *>(list + (uint32_t)k);
+          const uint32_t li = kOrdered ? __ldg(perm + lbase + (uint32_t)k) : (uint32_t)k;
+          const uint4 *r = reinterpret_cast<const uint4 *>(list + li);
           uint4 v[8];
 #pragma unroll
           for (int q = 0; q < 8; q++) v[q] = kCont ? r[q] : __ldg(r + q);
@@ -1241,7 +1280,7 @@ uint64_t cont_capacity(uint64_t nb, int tb, int sm_count) {
 size_t chunk_buffer_bytes(uint64_t nb, int tb, int sm_count) {
   const uint64_t n8 = (uint64_t)kClasses * nb;
   const uint64_t tmax = (uint64_t)tb * nb;
-  size_t b = 256;  // PipelineCounters
+  size_t b = kCountersSlot;  // PipelineCounters
   b += (nb * sizeof(BlockSel) + 255) & ~255ull;
   b += (n8 + 255) & ~255ull;
   b += (n8 * 2 + 255) & ~255ull;
@@ -1252,6 +1291,7 @@ size_t chunk_buffer_bytes(uint64_t nb, int tb, int sm_count) {
   b += (kClasses * cont_capacity(nb, tb, sm_count) * sizeof(AnnealRec) + 255) & ~255ull;
   b += (nb * sizeof(uint2) + 255) & ~255ull;                      // winners
   b += ((uint64_t)kClasses * 3 * nb * sizeof(uint32_t) + 255) & ~255ull;  // re-index lists
+  b += 2 * ((tmax * sizeof(uint32_t) + 255) & ~255ull);           // point-count keys, order
   return b;
 }
 
@@ -1269,12 +1309,13 @@ struct ChunkBuf {
   uint2 *win;
   uint32_t *rlist;
   uint32_t rcap;
+  uint32_t *keys, *perm;
 };
 
 ChunkBuf carve_chunk(uint8_t *p, uint64_t nb, int tb, int sm_count) {
   ChunkBuf c;
   c.ctr = reinterpret_cast<PipelineCounters *>(p);
-  p += 256;
+  p += kCountersSlot;
   c.sel = reinterpret_cast<BlockSel *>(p);
   p += (nb * sizeof(BlockSel) + 255) & ~255ull;
   c.counts = p;
@@ -1296,6 +1337,10 @@ ChunkBuf carve_chunk(uint8_t *p, uint64_t nb, int tb, int sm_count) {
   p += (nb * sizeof(uint2) + 255) & ~255ull;
   c.rlist = reinterpret_cast<uint32_t *>(p);
   c.rcap = (uint32_t)(3 * nb);
+  p += ((uint64_t)kClasses * 3 * nb * sizeof(uint32_t) + 255) & ~255ull;
+  c.keys = reinterpret_cast<uint32_t *>(p);
+  p += ((uint64_t)tb * nb * sizeof(uint32_t) + 255) & ~255ull;
+  c.perm = reinterpret_cast<uint32_t *>(p);
   return c;
 }
 
@@ -1376,6 +1421,7 @@ struct ChunkArgs {
   AnnealRec *arec;
   AnnealRec *cont;
   uint32_t cont_cap;
+  uint32_t *keys, *perm;
   uint32_t *status;
   int sm_count;
 };
@@ -1417,12 +1463,15 @@ void launch_class(const ChunkArgs &a, cudaStream_t s) {
   if (setup_ctas > setup_ctas_max) setup_ctas = setup_ctas_max;
   setup_kernel<C><<<(unsigned)setup_ctas, kSetupThreads, 0, s>>>(a.jobs, a.nb, a.sel, a.desc, a.local,
                                                            a.chunk, a.ctr, a.state, a.arec,
-                                                           a.status);
+                                                           a.keys, a.status);
+  if (mode_attr(class_mode(C)).subsets > 1)
+    order_kernel<C><<<(unsigned)setup_ctas, 128, 0, s>>>(a.nb, a.local, a.chunk, a.ctr, a.keys,
+                                                         a.perm);
   anneal_kernel<C, false><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
-      a.nb, a.local, a.chunk, a.ctr, a.arec, a.cont, a.cont_cap, a.state);
+      a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.state);
   if (mode_attr(class_mode(C)).has_rotation)
     anneal_kernel<C, true><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
-        a.nb, a.local, a.chunk, a.ctr, a.arec, a.cont, a.cont_cap, a.state);
+        a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.state);
 }
 
 void launch_class_any(int c, const ChunkArgs &a, cudaStream_t s) {
@@ -1511,8 +1560,8 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     scan_local_u8_kernel<<<nchunks, kRankChunk, 0, st>>>(b.counts, n8, b.local, b.chunk);
     scan_chunks_kernel<<<1, 1024, 0, st>>>(b.chunk, nchunks, b.ctr);
     emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, b.counts, b.local, b.chunk, b.desc);
-    const ChunkArgs args{jobs,   nb,      b.sel,      b.desc,      b.local,  b.chunk, b.ctr,
-                         b.state, b.arec, b.cont, b.cont_cap, rank.status, sm_count};
+    const ChunkArgs args{jobs,   nb,     b.sel,  b.desc,     b.local, b.chunk, b.ctr,      b.state,
+                         b.arec, b.cont, b.cont_cap, b.keys, b.perm, rank.status, sm_count};
     if (cls) {
       cudaError_t ce = cudaEventRecord(cls->fork[i & 1], st);
       const cudaStream_t *side = cls->side[i & 1];

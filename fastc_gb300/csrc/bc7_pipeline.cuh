@@ -91,8 +91,10 @@ struct PipelineCounters {
   unsigned long long cont_next[kClasses];    // refill cursors of the continuation lists
   uint32_t cont_count[kClasses];             // continuations of each class
   uint32_t reindex_count[kClasses];          // annealed winning fits of each class
+  uint32_t nhist[kClasses][17];              // annealing fits by point count (multi-subset classes)
 };
-static_assert(sizeof(PipelineCounters) <= 256, "PipelineCounters fits its slot");
+constexpr size_t kCountersSlot = 1024;
+static_assert(sizeof(PipelineCounters) <= kCountersSlot, "PipelineCounters fits its slot");
 
 // Side streams that run the classes' setup + annealing concurrently, forked
 // from and joined back into the caller's stream with events (both are
