@@ -914,9 +914,10 @@ __device__ inline void fit_rgb_setup_t(ModeCtx &m, const Cluster &c, FitSetup &s
       uint32_t e[16];
 #pragma unroll
       for (int k = 0; k < 16; k++) e[k] = cl_pixel(c, k);
-      uint32_t psel = 0x4210u;
-      if (c.rot) psel = (psel & ~(0xFu << (4 * (c.rot - 1)))) | (3u << (4 * (c.rot - 1)));
-      st.errf = qe_reg<kBits, true, true>(e, psel, se, m.pal, e1, e2, ix);
+      uint32_t pr[16];
+#pragma unroll
+      for (int k = 0; k < 16; k++) pr[k] = cl_packed(c, k);
+      st.errf = qe_reg<kBits, true, true>(e, pr, se, m.pal, e1, e2, ix);
     } else {
       st.errf = qe_smem<kBits, true>(c.px, c.n, c.tex, se, m.pal, e1, e2, ix);
     }

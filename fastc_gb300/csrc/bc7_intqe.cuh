@@ -117,10 +117,11 @@ __device__ __forceinline__ int pair_term(uint32_t e, const uint4 *pal, int j1, b
 }
 
 // Sixteen texels in registers (one-subset modes; texel k is point k).
-// `psel` builds the projected point of the rotation modes from the texel.
+// pr: the projected points of the rotation modes (the texel with the
+// rotated channel and alpha 255); for other modes the texels themselves.
 template <int kBits, bool kRot, bool kIdx>
-__device__ __forceinline__ float qe_reg(const uint32_t (&e)[16], uint32_t psel, int se, uint4 *pal,
-                                        uint32_t q1, uint32_t q2, uint64_t &idx) {
+__device__ __forceinline__ float qe_reg(const uint32_t (&e)[16], const uint32_t (&pr)[16], int se,
+                                        uint4 *pal, uint32_t q1, uint32_t q2, uint64_t &idx) {
   const Proj pj = make_proj(q1, q2);
   int acc = 0;
   if (pj.L == 0) {
@@ -132,9 +133,8 @@ __device__ __forceinline__ float qe_reg(const uint32_t (&e)[16], uint32_t psel, 
   palette_sq<kBits>(q1, q2, pal);
 #pragma unroll
   for (int k = 0; k < 16; k++) {
-    const uint32_t p = kRot ? __byte_perm(e[k], 0xFFFFFFFFu, psel) : e[k];
     bool two;
-    const int j1 = nearest_pair<kBits>(pj, p, two);
+    const int j1 = nearest_pair<kBits>(pj, kRot ? pr[k] : e[k], two);
     int bj;
     acc += pair_term(e[k], pal, j1, two, bj);
     if (kIdx) idx |= (uint64_t)bj << (4 * k);

@@ -794,6 +794,7 @@ struct Lane {
 // uniform metric, the float path otherwise.
 template <int C, bool kIdx>
 __device__ __forceinline__ float class_qe(const Lane &s, const uint32_t (&ereg)[16],
+                                          const uint32_t (&preg)[16],
                                           const uint32_t *pts, const uint32_t *proj, uint4 *pal,
                                           uint32_t *palf, uint32_t q1, uint32_t q2, uint64_t &idx) {
   constexpr int kMode = class_mode(C);
@@ -802,7 +803,7 @@ __device__ __forceinline__ float class_qe(const Lane &s, const uint32_t (&ereg)[
   constexpr bool kRot = a.has_rotation != 0;
   constexpr bool kN16 = a.subsets == 1;
   if (s.uniform) {
-    if constexpr (kN16) return qe_reg<kBits, kRot, kIdx>(ereg, s.psel, s.se, pal, q1, q2, idx);
+    if constexpr (kN16) return qe_reg<kBits, kRot, kIdx>(ereg, preg, s.se, pal, q1, q2, idx);
     else return qe_smem<kBits, kIdx>(pts, s.n, s.tex, s.se, pal, q1, q2, idx);
   }
   // float metric: palette as plain colours in the same buffer
@@ -812,7 +813,8 @@ __device__ __forceinline__ float class_qe(const Lane &s, const uint32_t (&ereg)[
 // One iteration of OptimizeEndpointsForCluster's loop (CP:583-624) for
 // class C; returns true when the fit is finished.
 template <int C>
-__device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t (&ereg)[16], const uint32_t *pts,
+__device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t (&ereg)[16],
+                                            const uint32_t (&preg)[16], const uint32_t *pts,
                                             const uint32_t *proj, uint4 *pal, uint32_t *palf,
                                             const uint8_t *lut) {
   constexpr int kMode = class_mode(C);
@@ -860,14 +862,20 @@ __device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t (&ereg)[16],
   const uint32_t q1 = qpix<a.color_bits, a.alpha_bits>(lut, np1, pb_first(pc));
   const uint32_t q2 = qpix<a.color_bits, a.alpha_bits>(lut, np2, pb_second(pc));
   uint64_t unused = 0;
-  const float err = class_qe<C, false>(s, ereg, pts, proj, pal, palf, q1, q2, unused);
+  const float err = class_qe<C, false>(s, ereg, preg, pts, proj, pal, palf, q1, q2, unused);
   // AcceptNewEndpointError (CP:524-536)
   bool accept = err < s.cur_err;
   if (!accept) {
     const uint32_t r16 = lcg_next(s.lcg) & 0xFFFF;
     const uint32_t mant = (r16 << 8) | (r16 >> 7);
     const float r = __fsub_rn(__uint_as_float((127u << 23) | mant), 1.0f);
-    if (r < 1.0f) {
+    // A nonzero draw is at least 2^-15 and exp(x) < 2^-15 for x < -10.5, so
+    // when 0.1 (err - cur) (steps - 1) > 12 energy (x < -12 with room for
+    // rounding) the move is rejected without FasTC's divisions and exp.
+    const bool hopeless = mant != 0 && s.energy > 0 &&
+                          __fmul_rn(__fmul_rn(__fsub_rn(err, s.cur_err), 0.1f), (float)(s.steps - 1)) >
+                              12.0f * (float)s.energy;
+    if (r < 1.0f && !hopeless) {
       const float temp = __fdiv_rn((float)s.energy, (float)(s.steps - 1));
       const float x = __fdiv_rn(__fmul_rn(0.1f, __fsub_rn(s.cur_err, err)), temp);
       accept = mant == 0 ? (x > -745.0f) : (r < portable_expf(x));
@@ -928,7 +936,7 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   constexpr bool kOrdered = !kCont && a.subsets > 1;  // taken in point-count order
   unsigned long long *cursor = kCont ? &ctr->cont_next[C] : &ctr->anneal_next[C];
   Lane s;
-  uint32_t ereg[16];
+  uint32_t ereg[16], preg[16];
   bool active = false, exhausted = false;
   for (;;) {
     const bool need = !active && !exhausted;
@@ -983,7 +991,10 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
               ereg[4 * q + c] = e;
               if (4 * q + c < s.n) se += (int)__dp4a(e, e, 0u);
               pts[(4 * q + c) * T] = e;
-              if (kRot) proj[(4 * q + c) * T] = __byte_perm(e, 0xFFFFFFFFu, s.psel);
+              if (kRot) {
+                preg[4 * q + c] = __byte_perm(e, 0xFFFFFFFFu, s.psel);
+                proj[(4 * q + c) * T] = preg[4 * q + c];
+              }
             }
           }
           s.se = se;
@@ -992,7 +1003,8 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
       }
     }
     if (__all_sync(0xFFFFFFFFu, exhausted && !active)) break;
-    if (!kCont && kYields) {
+    // a lane finished (nmask != 0): with the list empty, maybe retire
+    if (!kCont && kYields && nmask) {
       const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
       if (__any_sync(0xFFFFFFFFu, exhausted) && __popc(act) <= kYieldLanes) {
         // hand the unfinished fits on and retire the warp
@@ -1019,7 +1031,7 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
       }
     }
     if (active) {
-      if (anneal_step<C>(s, ereg, pts, proj, pal, palf, s_lut)) {
+      if (anneal_step<C>(s, ereg, preg, pts, proj, pal, palf, s_lut)) {
         // the indices of the best endpoints are recomputed by the pack
         // stage for the fits that win their block
         TaskState &o = state[s.t];
@@ -1072,9 +1084,12 @@ __device__ __noinline__ uint64_t fit_indices(const TaskState &o, const uint32_t 
   m.rot = rot;
   m.metric = s.uniform ? 0 : 1;
   metric_of(m, s.w);
-  uint32_t ereg[16];
+  uint32_t ereg[16], preg[16];
 #pragma unroll
-  for (int k = 0; k < 16; k++) ereg[k] = px[k * T];
+  for (int k = 0; k < 16; k++) {
+    ereg[k] = px[k * T];
+    preg[k] = __byte_perm(ereg[k], 0xFFFFFFFFu, s.psel);
+  }
   int n = 0, se = 0;
   uint64_t tex = 0;
   for (int i = 0; i < 16; i++) {
@@ -1093,7 +1108,7 @@ __device__ __noinline__ uint64_t fit_indices(const TaskState &o, const uint32_t 
   const uint32_t q1 = qpix<a.color_bits, a.alpha_bits>(lut, o.p1, pb_first(pc));
   const uint32_t q2 = qpix<a.color_bits, a.alpha_bits>(lut, o.p2, pb_second(pc));
   uint64_t idx = 0;
-  class_qe<C, true>(s, ereg, pts, proj, pal, palf, q1, q2, idx);
+  class_qe<C, true>(s, ereg, preg, pts, proj, pal, palf, q1, q2, idx);
   return idx;
 }
 
