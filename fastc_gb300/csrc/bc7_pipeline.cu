@@ -917,6 +917,7 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   // only classes with long fits (the rotation modes) hand fits on; short
   // fits drain quickly
   constexpr bool kYields = kRot;
+  constexpr int kRefillBatch = kRot || kCont ? 1 : 4;
   AnnealRec *clist = cont + (size_t)C * cont_cap;
   if (kCont && blockIdx.x * (uint32_t)T >= ctr->cont_count[C]) return;
   __shared__ uint8_t s_lut[8 * 3 * 256];
@@ -940,7 +941,11 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   bool active = false, exhausted = false;
   for (;;) {
     const bool need = !active && !exhausted;
-    const uint32_t nmask = __ballot_sync(0xFFFFFFFFu, need);
+    uint32_t nmask = __ballot_sync(0xFFFFFFFFu, need);
+    // Short fits finish every few steps somewhere in the warp; refilling in
+    // batches of kRefillBatch lanes (or when no lane is left running) keeps
+    // the divergent refill and its two memory round trips rare.
+    if (__popc(nmask) < kRefillBatch && __ballot_sync(0xFFFFFFFFu, active) != 0) nmask = 0;
     if (nmask) {
       unsigned long long b0 = 0;
       const int leader = __ffs(nmask) - 1;
