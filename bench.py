@@ -6,6 +6,7 @@ tile_mix content (fastc_gb300.synth), 115.6 MP / 7.22 M blocks in total,
 encoded at 50 annealing steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --serve [--serve-rates 20,60,120] [--serve-seconds 4]
 
 A step is one pass of the encoder over the whole texture set:
   * value       -- batched: one graph launch of the captured plan over all
@@ -214,6 +215,77 @@ def reference_impl(args):
     print(json.dumps(line))
 
 
+SERVE_SEED = 11
+
+
+def _gen_serve(args):
+    from fastc_gb300 import synth
+
+    i, w, h = args
+    return synth.tile_mix(SERVE_SEED * 1000 + i, w, h)
+
+
+def serve_bench(args):
+    """--serve: the request server under a Poisson stream of requests (sides
+    log-uniform in 32..4096 rounded to multiples of 4, q drawn from
+    {0, 16, 50} with probabilities {0.3, 0.4, 0.3}, 8 GB device budget) at a
+    sweep of arrival rates. Prints one JSON line with p50/p99 latency and
+    MP/s per rate. Textures come from a pool of seeded images that requests
+    draw from."""
+    import numpy as np
+
+    rng = np.random.default_rng(SERVE_SEED)
+    npool = 48
+    sides = [(int(4 * round(32 * (128 ** rng.random()) / 4)), int(4 * round(32 * (128 ** rng.random()) / 4)))
+             for _ in range(npool)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(max(1, min(16, os.cpu_count() or 1))) as pool:
+        imgs = pool.map(_gen_serve, [(i, w, h) for i, (w, h) in enumerate(sides)], chunksize=1)
+
+    import torch
+
+    torch.cuda.init()
+    from fastc_gb300 import CompressionSettings
+    from fastc_gb300.serve import Server
+
+    qs = [0, 16, 50]
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    results = []
+    # warm the device (tables, allocator)
+    with Server(memory_budget=8 << 30) as srv:
+        srv.wait(srv.submit(imgs[0], CompressionSettings(num_simulated_annealing_steps=0)))
+    for rate in rates:
+        n = max(8, int(rate * args.serve_seconds))
+        picks = rng.integers(0, npool, n)
+        qsel = rng.choice(qs, size=n, p=[0.3, 0.4, 0.3])
+        gaps = rng.exponential(1.0 / rate, n)
+        with Server(memory_budget=8 << 30, max_inflight=3) as srv:
+            reqs = []
+            t0 = time.perf_counter()
+            due = t0
+            for k in range(n):
+                due += gaps[k]
+                wait = due - time.perf_counter()
+                if wait > 0:
+                    time.sleep(wait)
+                reqs.append(srv.submit(imgs[picks[k]],
+                                       CompressionSettings(num_simulated_annealing_steps=int(qsel[k]),
+                                                           seed=k)))
+            for r in reqs:
+                srv.wait(r)
+            dt = time.perf_counter() - t0
+            st = srv.stats()
+        px = sum(imgs[i].shape[0] * imgs[i].shape[1] for i in picks)
+        results.append({"rate_per_s": rate, "requests": n, "mpix": px / 1e6, "mpix_s": px / dt / 1e6,
+                        "p50_ms": st["p50_latency_ms"], "p99_ms": st["p99_latency_ms"],
+                        "batches": st["batches"], "peak_bytes": st["peak_bytes"]})
+    print(json.dumps({"metric": "BC7 serving: p50/p99 latency and MPix/s under Poisson arrivals",
+                      "config": {"workload": "poisson_mixed_q_8gb", "sides": "log-uniform 32..4096",
+                                 "q": "{0,16,50} w.p. {0.3,0.4,0.3}", "budget_bytes": 8 << 30,
+                                 "texture_pool": npool},
+                      "sweep": results}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -222,9 +294,15 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-budget-px", type=int, default=400_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve", action="store_true", help="run the serving sweep instead")
+    ap.add_argument("--serve-rates", default="20,60,120")
+    ap.add_argument("--serve-seconds", type=float, default=4.0)
     args = ap.parse_args()
     if args.impl == "reference":
         reference_impl(args)
+        return
+    if args.serve:
+        serve_bench(args)
         return
 
     rank = int(os.environ.get("RANK", "0"))
