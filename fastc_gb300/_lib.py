@@ -99,6 +99,8 @@ SIGNATURES = {
     "fastc_bc7_plan_flags": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
     "fastc_bc7_plan_blocks": (C.c_uint64, [C.c_void_p]),
     "fastc_bc7_plan_kernels": (C.c_uint64, [C.c_void_p]),
+    "fastc_bc7_plan_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "fastc_bc7_plan_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "fastc_bc7_plan_destroy": (C.c_int, [C.c_void_p]),
     "fastc_bc7_set_watermark_counter": (None, [C.c_uint32]),
     "fastc_bc7_get_watermark_counter": (C.c_uint32, []),

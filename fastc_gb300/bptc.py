@@ -283,6 +283,18 @@ class Plan:
         """Kernel launches one launch() makes (kernel nodes of the graph)."""
         return int(load().fastc_bc7_plan_kernels(self._h))
 
+    def autotune(self, stream=None, launches: int = 2) -> dict:
+        """Choose the launch parameters on this plan's own jobs (see
+        fastc_bc7_plan_autotune); returns the chosen parameters."""
+        check(load().fastc_bc7_plan_autotune(self._h, C.c_void_p(_stream_handle(stream)), int(launches)),
+              "fastc_bc7_plan_autotune")
+        return self.tuning()
+
+    def tuning(self) -> dict:
+        a, y = C.c_int(), C.c_int()
+        check(load().fastc_bc7_plan_tuning(self._h, C.byref(a), C.byref(y)), "fastc_bc7_plan_tuning")
+        return {"anneal_ctas_per_sm": int(a.value), "yield_lanes": int(y.value)}
+
     def launch(self, stream=None) -> None:
         check(load().fastc_bc7_plan_launch(self._h, C.c_void_p(_stream_handle(stream))),
               "fastc_bc7_plan_launch")

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <utility>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -155,14 +156,22 @@ uint32_t align_flags(const void *in, const void *out) {
 // Encode `total` blocks of the device job table with the selected engine,
 // carving the rank and pipeline scratch out of `scratch`.
 int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
-                  LaunchShape shape, int task_bound, const ClassStreams *cls, cudaStream_t st) {
+                  LaunchShape shape, int task_bound, const ClassStreams *cls,
+                  const fastc::PipelineTuning &tune, cudaStream_t st) {
   const EncodeScratch rank = carve_scratch(scratch, total);
   if (engine == FASTC_BC7_ENGINE_PIPELINE) {
     void *pipe = static_cast<uint8_t *>(scratch) + rank_scratch_bytes(total);
     return fastc::launch_pipeline(jobs, njobs, total, rank, pipe,
-                                  fastc::device_sm_count(current_device()), task_bound, cls, st);
+                                  fastc::device_sm_count(current_device()), task_bound, cls, tune,
+                                  st);
   }
   return fastc::launch_encode(jobs, njobs, total, rank, shape, st);
+}
+
+int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
+                  LaunchShape shape, int task_bound, const ClassStreams *cls, cudaStream_t st) {
+  return launch_engine(jobs, njobs, total, scratch, engine, shape, task_bound, cls,
+                       fastc::PipelineTuning{}, st);
 }
 
 namespace {
@@ -330,7 +339,59 @@ struct fastc_bc7_plan_s {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   uint64_t kernels = 0;  // kernel nodes of the graph
+  int task_bound = 0;
+  fastc::PipelineTuning tune;
 };
+
+namespace {
+
+// Captures the plan's whole launch with `tune` into a graph (private
+// stream and side streams, released after the capture) and instantiates it.
+cudaError_t capture_plan(const fastc_bc7_plan_s *p, const fastc::PipelineTuning &tune,
+                         cudaGraph_t *graph, cudaGraphExec_t *exec, uint64_t *kernels) {
+  *graph = nullptr;
+  *exec = nullptr;
+  cudaStream_t cs = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  ClassStreams cls{};
+  const bool use_cls = p->engine == FASTC_BC7_ENGINE_PIPELINE;
+  if (e == cudaSuccess && use_cls) e = fastc::class_streams_create(&cls);
+  if (e == cudaSuccess) {
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      const int le = launch_engine(p->d_jobs, p->njobs, p->total, p->d_scratch, p->engine,
+                                   pick_shape(p->total), p->task_bound, use_cls ? &cls : nullptr,
+                                   tune, cs);
+      cudaError_t ee = cudaStreamEndCapture(cs, graph);
+      e = le ? (cudaError_t)le : ee;
+    }
+  }
+  if (e == cudaSuccess && !*graph) e = cudaErrorStreamCaptureInvalidated;
+  if (e == cudaSuccess && kernels) {
+    size_t nn = 0;
+    e = cudaGraphGetNodes(*graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (e == cudaSuccess && nn) e = cudaGraphGetNodes(*graph, nodes.data(), &nn);
+    *kernels = 0;
+    for (size_t k = 0; k < nn && e == cudaSuccess; k++) {
+      cudaGraphNodeType t;
+      e = cudaGraphNodeGetType(nodes[k], &t);
+      if (t == cudaGraphNodeTypeKernel) (*kernels)++;
+    }
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(exec, *graph, 0);
+  fastc::class_streams_destroy(&cls);
+  if (cs) cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    if (*exec) cudaGraphExecDestroy(*exec);
+    if (*graph) cudaGraphDestroy(*graph);
+    *exec = nullptr;
+    *graph = nullptr;
+  }
+  return e;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -569,43 +630,17 @@ fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
   p->device = dev;
   p->total = total;
   p->njobs = (int)n;
-  cudaStream_t cs = nullptr;
   cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p->d_jobs), n * sizeof(JobDev));
   p->engine = g_engine;
-  const int tb = task_bound_of(settings, per_job_settings, n);
-  if (e == cudaSuccess) e = cudaMalloc(&p->d_scratch, scratch_bytes(total > 0 ? total : 1, p->engine, tb));
+  p->task_bound = task_bound_of(settings, per_job_settings, n);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&p->d_scratch, scratch_bytes(total > 0 ? total : 1, p->engine, p->task_bound));
   if (e == cudaSuccess)
     e = cudaMemcpy(p->d_jobs, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-  // private side streams: they belong to the capture until it ends
-  ClassStreams cls{};
-  const bool use_cls = p->engine == FASTC_BC7_ENGINE_PIPELINE;
-  if (e == cudaSuccess && use_cls) e = fastc::class_streams_create(&cls);
   if (e == cudaSuccess) {
     p->sc = carve_scratch(p->d_scratch, total);
-    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) {
-      const int le = launch_engine(p->d_jobs, (int)n, total, p->d_scratch, p->engine,
-                                   pick_shape(total), tb, use_cls ? &cls : nullptr, cs);
-      cudaError_t ee = cudaStreamEndCapture(cs, &p->graph);
-      e = le ? (cudaError_t)le : ee;
-    }
+    e = capture_plan(p, p->tune, &p->graph, &p->exec, &p->kernels);
   }
-  if (e == cudaSuccess && !p->graph) e = cudaErrorStreamCaptureInvalidated;
-  if (e == cudaSuccess) {
-    size_t nn = 0;
-    e = cudaGraphGetNodes(p->graph, nullptr, &nn);
-    std::vector<cudaGraphNode_t> nodes(nn);
-    if (e == cudaSuccess && nn) e = cudaGraphGetNodes(p->graph, nodes.data(), &nn);
-    for (size_t k = 0; k < nn && e == cudaSuccess; k++) {
-      cudaGraphNodeType t;
-      e = cudaGraphNodeGetType(nodes[k], &t);
-      if (t == cudaGraphNodeTypeKernel) p->kernels++;
-    }
-  }
-  if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
-  fastc::class_streams_destroy(&cls);
-  if (cs) cudaStreamDestroy(cs);
   if (e != cudaSuccess) {
     fastc_bc7_plan_destroy(p);
     return fail_cuda(e);
@@ -617,6 +652,67 @@ fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
 fastc_bc7_status fastc_bc7_plan_launch(fastc_bc7_plan p, void *stream) {
   if (!p || !p->exec) return FASTC_BC7_ERR_INVALID_ARGUMENT;
   CK(cudaGraphLaunch(p->exec, static_cast<cudaStream_t>(stream)));
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_plan_autotune(fastc_bc7_plan p, void *stream, uint32_t launches) {
+  if (!p || !p->exec || launches == 0) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  if (p->engine != FASTC_BC7_ENGINE_PIPELINE) return FASTC_BC7_OK;  // nothing to tune
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0));
+  cudaError_t e = cudaEventCreate(&e1);
+  // times `launches` launches of an instantiated graph after one warm launch
+  auto time_exec = [&](cudaGraphExec_t ex, float *ms) -> cudaError_t {
+    cudaError_t r = cudaGraphLaunch(ex, st);
+    if (r == cudaSuccess) r = cudaEventRecord(e0, st);
+    for (uint32_t k = 0; k < launches && r == cudaSuccess; k++) r = cudaGraphLaunch(ex, st);
+    if (r == cudaSuccess) r = cudaEventRecord(e1, st);
+    if (r == cudaSuccess) r = cudaEventSynchronize(e1);
+    if (r == cudaSuccess) r = cudaEventElapsedTime(ms, e0, e1);
+    return r;
+  };
+  float best_ms = 0.0f;
+  if (e == cudaSuccess) e = time_exec(p->exec, &best_ms);
+  // coordinate search: CTAs per SM of the annealing kernels, then the
+  // hand-on threshold at the best CTA count
+  const int ctas[] = {3, 4, 5, 6, 7};
+  const int yields[] = {8, 12, 16};
+  for (int phase = 0; phase < 2 && e == cudaSuccess; phase++) {
+    const int ncand = phase == 0 ? 5 : 3;
+    for (int i = 0; i < ncand && e == cudaSuccess; i++) {
+      fastc::PipelineTuning t = p->tune;
+      if (phase == 0) t.anneal_ctas_per_sm = ctas[i];
+      else t.yield_lanes = yields[i];
+      if (t.anneal_ctas_per_sm == p->tune.anneal_ctas_per_sm && t.yield_lanes == p->tune.yield_lanes)
+        continue;
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ex = nullptr;
+      uint64_t kern = 0;
+      e = capture_plan(p, t, &g, &ex, &kern);
+      float ms = 0.0f;
+      if (e == cudaSuccess) e = time_exec(ex, &ms);
+      if (e == cudaSuccess && ms < best_ms) {
+        std::swap(g, p->graph);
+        std::swap(ex, p->exec);
+        p->kernels = kern;
+        p->tune = t;
+        best_ms = ms;
+      }
+      if (ex) cudaGraphExecDestroy(ex);
+      if (g) cudaGraphDestroy(g);
+    }
+  }
+  cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e != cudaSuccess) return fail_cuda(e);
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_plan_tuning(fastc_bc7_plan p, int *anneal_ctas_per_sm, int *yield_lanes) {
+  if (!p || !anneal_ctas_per_sm || !yield_lanes) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  *anneal_ctas_per_sm = p->tune.anneal_ctas_per_sm;
+  *yield_lanes = p->tune.yield_lanes;
   return FASTC_BC7_OK;
 }
 

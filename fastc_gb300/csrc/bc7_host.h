@@ -50,6 +50,9 @@ uint32_t align_flags(const void *in, const void *out);
 // `cls`: side streams for the pipeline engine's classes (null: one stream).
 int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
                   LaunchShape shape, int task_bound, const ClassStreams *cls, cudaStream_t st);
+int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
+                  LaunchShape shape, int task_bound, const ClassStreams *cls,
+                  const PipelineTuning &tune, cudaStream_t st);
 // Side-stream sets for callers without their own: taken for one enqueue
 // and given back (per device; created on first need).
 ClassStreams *acquire_class_streams(int device);

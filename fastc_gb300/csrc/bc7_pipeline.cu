@@ -659,7 +659,6 @@ __global__ void __launch_bounds__(128) order_kernel(uint32_t nb, const uint16_t 
 // ---------------------------------------------------------------------------
 
 constexpr int kAnnealThreads = kLaneStride;
-constexpr int kYieldLanes = 12;
 
 // ToPixel (RGBAEndpoints.cpp:167-177) of integer endpoints through the table.
 template <int kColorBits, int kAlphaBits>
@@ -899,7 +898,7 @@ __device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t (&ereg)[16],
 }
 
 // kCont = false: the class's list of fits from the setup stage. When that
-// list is empty, a warp with at most kYieldLanes lanes still annealing
+// list is empty, a warp with at most yield_lanes lanes still annealing
 // writes their fits, mid-flight, to the class's continuation list and
 // exits, instead of running on with most lanes idle (fit lengths vary about
 // threefold). kCont = true: the continuation list, run to completion.
@@ -908,7 +907,7 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
     uint32_t nb, const uint16_t *__restrict__ local, const uint32_t *__restrict__ chunk,
     PipelineCounters *__restrict__ ctr, const AnnealRec *__restrict__ arec,
     const uint32_t *__restrict__ perm, AnnealRec *__restrict__ cont, uint32_t cont_cap,
-    TaskState *__restrict__ state) {
+    int yield_lanes, TaskState *__restrict__ state) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr a = mode_attr(kMode);
   constexpr int kBits = class_im(C) ? a.alpha_idx_bits : a.idx_bits;
@@ -1011,7 +1010,7 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
     // a lane finished (nmask != 0): with the list empty, maybe retire
     if (!kCont && kYields && nmask) {
       const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
-      if (__any_sync(0xFFFFFFFFu, exhausted) && __popc(act) <= kYieldLanes) {
+      if (__any_sync(0xFFFFFFFFu, exhausted) && __popc(act) <= yield_lanes) {
         // hand the unfinished fits on and retire the warp
         const int leader = __ffs(act) - 1;
         uint32_t pos = 0;
@@ -1444,6 +1443,7 @@ struct ChunkArgs {
   uint32_t *keys, *perm;
   uint32_t *status;
   int sm_count;
+  int anneal_ctas, yield_lanes;
 };
 
 // Resident CTAs per SM of a kernel (queried once per process; the kernels
@@ -1465,16 +1465,13 @@ constexpr int class_block_fits(int c) {
                                                   : mode_attr(class_mode(c)).subsets;
 }
 
-// Annealing CTAs per SM: below the resident limit, so that setup and select
-// CTAs of other chunks and classes share the SMs (measured best on the
-// texture-set workload).
-constexpr int kAnnealCtasPerSm = 5;
-
 template <int C>
 void launch_class(const ChunkArgs &a, cudaStream_t s) {
   // the annealing kernel is persistent: no more CTAs than can be resident
   static const int anneal_res = resident_ctas(anneal_kernel<C, false>, kAnnealThreads);
-  const int anneal_per_sm = anneal_res < kAnnealCtasPerSm ? anneal_res : kAnnealCtasPerSm;
+  // below the resident limit, so that setup and select CTAs of other
+  // chunks and classes share the SMs
+  const int anneal_per_sm = anneal_res < a.anneal_ctas ? anneal_res : a.anneal_ctas;
   // setup: one thread per fit (latency-bound; threads past the class's
   // fits return at once)
   const uint64_t fits = (uint64_t)a.nb * class_block_fits(C);
@@ -1488,10 +1485,10 @@ void launch_class(const ChunkArgs &a, cudaStream_t s) {
     order_kernel<C><<<(unsigned)setup_ctas, 128, 0, s>>>(a.nb, a.local, a.chunk, a.ctr, a.keys,
                                                          a.perm);
   anneal_kernel<C, false><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
-      a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.state);
+      a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.yield_lanes, a.state);
   if (mode_attr(class_mode(C)).has_rotation)
     anneal_kernel<C, true><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
-        a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.state);
+        a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.yield_lanes, a.state);
 }
 
 void launch_class_any(int c, const ChunkArgs &a, cudaStream_t s) {
@@ -1539,7 +1536,7 @@ void reindex_all(const JobDev *jobs, const ChunkBuf &b, int sm_count, cudaStream
 // pack(i - 2), earlier on `st`.
 int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
                     void *scratch, int sm_count, int task_bound, const ClassStreams *cls,
-                    void *stream) {
+                    const PipelineTuning &tune, void *stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (total == 0) return 0;
   const int tb = task_bound < 1 ? 1 : (task_bound > kMaxBlockTasks ? kMaxBlockTasks : task_bound);
@@ -1581,7 +1578,8 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     scan_chunks_kernel<<<1, 1024, 0, st>>>(b.chunk, nchunks, b.ctr);
     emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, b.counts, b.local, b.chunk, b.desc);
     const ChunkArgs args{jobs,   nb,     b.sel,  b.desc,     b.local, b.chunk, b.ctr,      b.state,
-                         b.arec, b.cont, b.cont_cap, b.keys, b.perm, rank.status, sm_count};
+                         b.arec, b.cont, b.cont_cap, b.keys, b.perm, rank.status, sm_count,
+                         tune.anneal_ctas_per_sm < 1 ? 1 : tune.anneal_ctas_per_sm, tune.yield_lanes};
     if (cls) {
       cudaError_t ce = cudaEventRecord(cls->fork[i & 1], st);
       const cudaStream_t *side = cls->side[i & 1];

@@ -115,10 +115,17 @@ void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t
 int block_task_bound(uint32_t modes);
 // sm_count: of the device that runs the launch (bounds the continuation lists).
 size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound, int sm_count);
+// Launch parameters the plan autotuner chooses (defaults: measured best on
+// the mixed-size texture set).
+struct PipelineTuning {
+  int anneal_ctas_per_sm = 5;  // persistent annealing CTAs per SM (capped by residency)
+  int yield_lanes = 12;        // a warp with at most this many lanes annealing hands its fits on
+};
+
 // `cls` null: every stage runs in order on `stream`. `task_bound`: the most
 // block_task_bound() of the jobs' masks.
 int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
                     void *scratch, int sm_count, int task_bound, const ClassStreams *cls,
-                    void *stream);
+                    const PipelineTuning &tune, void *stream);
 
 }  // namespace fastc

@@ -209,6 +209,17 @@ FASTC_BC7_API uint64_t fastc_bc7_plan_blocks(fastc_bc7_plan plan);
 /* Kernel launches one fastc_bc7_plan_launch makes (kernel nodes of the
  * captured graph). */
 FASTC_BC7_API uint64_t fastc_bc7_plan_kernels(fastc_bc7_plan plan);
+/* Autotuner (replaces FasTC's fixed thread-count choice): tries the
+ * pipeline's launch parameters -- persistent CTAs per SM of the annealing
+ * kernels, then the lane count below which a warp hands its unfinished fits
+ * on -- on the plan's own jobs, timing `launches` graph launches per
+ * candidate on `stream`, and keeps the fastest graph. The plan's outputs
+ * are rewritten with the same bytes (results do not depend on the launch
+ * parameters). Synchronises `stream`. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_autotune(fastc_bc7_plan plan, void *stream,
+                                         uint32_t launches);
+FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_tuning(fastc_bc7_plan plan, int *anneal_ctas_per_sm,
+                                       int *yield_lanes);
 FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_destroy(fastc_bc7_plan plan);
 
 /* --- Request server: continuous batching under a device-memory budget. ---

@@ -147,6 +147,34 @@ def test_device_api_and_plan_match_host_api(gpu):
     plan.close()
 
 
+def test_plan_autotune_keeps_the_bytes(gpu):
+    """The autotuner swaps launch parameters, never results."""
+    import torch
+
+    from fastc_gb300 import CompressionJob, CompressionSettings, Plan, compress_jobs
+
+    imgs = [make_image(f"tile_mix({90 + i}, {w}, {h})") for i, (w, h) in enumerate([(256, 128), (64, 64), (128, 512)])]
+    s = CompressionSettings(num_simulated_annealing_steps=16, seed=5)
+    din = [torch.from_numpy(im).cuda() for im in imgs]
+    dout = [torch.zeros(im.shape[0] * im.shape[1], dtype=torch.uint8, device="cuda") for im in imgs]
+    jobs = [CompressionJob(a, b, im.shape[1], im.shape[0]) for a, b, im in zip(din, dout, imgs)]
+    compress_jobs(jobs, s)
+    torch.cuda.synchronize()
+    want = [d.cpu().numpy().copy() for d in dout]
+    for d in dout:
+        d.zero_()
+    plan = Plan(jobs, s)
+    t = plan.autotune(launches=1)
+    assert t["anneal_ctas_per_sm"] in (3, 4, 5, 6, 7) and t["yield_lanes"] in (8, 12, 16)
+    for d in dout:
+        d.zero_()
+    plan.launch()
+    torch.cuda.synchronize()
+    for w, d in zip(want, dout):
+        assert np.array_equal(w, d.cpu().numpy())
+    plan.close()
+
+
 def test_sub_jobs_tile_the_image(gpu, port):
     """FasTC's ThreadGroup splits (Core/src/ThreadGroup.cpp:133-192), run one
     after another with the watermark counter continuing across calls like
