@@ -1,0 +1,159 @@
+"""Image files for the command-line tool: PNG (8-bit RGB/RGBA/grey, no
+interlace) read and written with zlib, raw RGBA8, numpy arrays, and the KTX
+container FasTC writes for compressed images.
+
+The KTX layout follows FasTC's ImageWriterKTX (IO/src/ImageWriterKTX.cpp:
+the 12-byte identifier, thirteen little-endian words, one key/value pair
+"KTXorientation" = "S=r,T=d" padded to four bytes with the key's leading
+bytes, the image size and the blocks), so files are byte-identical.
+"""
+from __future__ import annotations
+
+import struct
+import zlib
+
+import numpy as np
+
+KTX_IDENTIFIER = bytes([0xAB, 0x4B, 0x54, 0x58, 0x20, 0x31, 0x31, 0xBB, 0x0D, 0x0A, 0x1A, 0x0A])
+GL_RGBA = 0x1908
+GL_COMPRESSED_RGBA_BPTC_UNORM = 0x8E8C
+_ORIENT_KEY = b"KTXorientation"
+_ORIENT_VALUE = b"S=r,T=d"
+
+
+def ktx_bytes(blocks: np.ndarray, width: int, height: int) -> bytes:
+    """A KTX file holding BC7 blocks (width*height bytes), as FasTC writes it."""
+    data = np.ascontiguousarray(blocks, dtype=np.uint8).tobytes()
+    if len(data) != width * height:
+        raise ValueError("BC7 data must be width*height bytes")
+    kv = len(_ORIENT_KEY) + 1 + len(_ORIENT_VALUE) + 1
+    total_kv = (kv + 4 + 3) & ~3
+    head = KTX_IDENTIFIER + struct.pack(
+        "<13I", 0x04030201, 0, 1, 0, GL_COMPRESSED_RGBA_BPTC_UNORM, GL_RGBA, width, height, 0, 0, 1,
+        1, total_kv)
+    pad = (_ORIENT_KEY * 2)[: total_kv - kv - 4]
+    body = struct.pack("<I", kv) + _ORIENT_KEY + b"\0" + _ORIENT_VALUE + b"\0" + pad
+    return head + body + struct.pack("<I", len(data)) + data
+
+
+def read_ktx(raw: bytes):
+    """(blocks, width, height) of a BC7 KTX file."""
+    if raw[:12] != KTX_IDENTIFIER:
+        raise ValueError("not a KTX file")
+    words = struct.unpack("<13I", raw[12:64])
+    if words[0] != 0x04030201 or words[4] != GL_COMPRESSED_RGBA_BPTC_UNORM:
+        raise ValueError("not a little-endian BC7 KTX file")
+    width, height, kv = words[6], words[7], words[12]
+    off = 64 + kv
+    (size,) = struct.unpack("<I", raw[off:off + 4])
+    blocks = np.frombuffer(raw[off + 4:off + 4 + size], dtype=np.uint8).copy()
+    return blocks, width, height
+
+
+def _paeth(a, b, c):
+    p = a + b - c
+    pa, pb, pc = np.abs(p - a), np.abs(p - b), np.abs(p - c)
+    return np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
+
+
+def read_png(raw: bytes) -> np.ndarray:
+    """RGBA8 (h, w, 4) of an 8-bit, non-interlaced PNG."""
+    if raw[:8] != b"\x89PNG\r\n\x1a\n":
+        raise ValueError("not a PNG file")
+    pos, idat, hdr = 8, [], None
+    while pos < len(raw):
+        (ln,) = struct.unpack(">I", raw[pos:pos + 4])
+        kind = raw[pos + 4:pos + 8]
+        body = raw[pos + 8:pos + 8 + ln]
+        if kind == b"IHDR":
+            hdr = struct.unpack(">IIBBBBB", body)
+        elif kind == b"IDAT":
+            idat.append(body)
+        elif kind == b"IEND":
+            break
+        pos += 12 + ln
+    if hdr is None:
+        raise ValueError("PNG without IHDR")
+    w, h, depth, ctype, _, _, interlace = hdr
+    chans = {0: 1, 2: 3, 4: 2, 6: 4}.get(ctype)
+    if depth != 8 or chans is None or interlace:
+        raise ValueError("only 8-bit grey/RGB/RGBA non-interlaced PNGs are supported")
+    data = np.frombuffer(zlib.decompress(b"".join(idat)), dtype=np.uint8)
+    stride = w * chans
+    rows = data.reshape(h, stride + 1)
+    out = np.zeros((h, stride), dtype=np.int32)
+    prev = np.zeros(stride, dtype=np.int32)
+    for y in range(h):
+        f, line = rows[y, 0], rows[y, 1:].astype(np.int32)
+        if f == 0:
+            cur = line
+        elif f == 2:
+            cur = (line + prev) & 0xFF
+        else:
+            cur = np.zeros(stride, dtype=np.int32)
+            for x in range(stride):
+                a = cur[x - chans] if x >= chans else 0
+                b = prev[x]
+                c = prev[x - chans] if x >= chans else 0
+                if f == 1:
+                    pred = a
+                elif f == 3:
+                    pred = (a + b) >> 1
+                else:
+                    pred = int(_paeth(np.int32(a), np.int32(b), np.int32(c)))
+                cur[x] = (line[x] + pred) & 0xFF
+        out[y] = cur
+        prev = cur
+    img = out.astype(np.uint8).reshape(h, w, chans)
+    if chans == 4:
+        return img
+    rgba = np.full((h, w, 4), 255, dtype=np.uint8)
+    if chans == 3:
+        rgba[..., :3] = img
+    elif chans == 2:
+        rgba[..., :3] = img[..., :1]
+        rgba[..., 3] = img[..., 1]
+    else:
+        rgba[..., :3] = img
+    return rgba
+
+
+def png_bytes(rgba: np.ndarray) -> bytes:
+    """An RGBA8 PNG (filter 0 on every row)."""
+    rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
+    h, w = rgba.shape[:2]
+    rows = np.concatenate([np.zeros((h, 1), dtype=np.uint8), rgba.reshape(h, w * 4)], axis=1)
+
+    def chunk(kind: bytes, body: bytes) -> bytes:
+        return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body))
+
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(rows.tobytes(), 6)) + chunk(b"IEND", b""))
+
+
+def load_image(path: str, width: int = 0, height: int = 0) -> np.ndarray:
+    """RGBA8 (h, w, 4) from .png, .npy or raw RGBA (.rgba, needs width/height)."""
+    if path.endswith(".npy"):
+        img = np.load(path)
+    elif path.endswith(".rgba") or path.endswith(".raw"):
+        if not (width and height):
+            raise ValueError("raw RGBA input needs its size (-s WxH)")
+        img = np.fromfile(path, dtype=np.uint8).reshape(height, width, 4)
+    else:
+        with open(path, "rb") as f:
+            img = read_png(f.read())
+    if img.ndim != 3 or img.shape[2] != 4 or img.dtype != np.uint8:
+        raise ValueError("images must be RGBA8")
+    return img
+
+
+def pad_to_blocks(img: np.ndarray) -> np.ndarray:
+    """Zero-pad to multiples of 4, as FasTC's CompressImage does
+    (Core/src/TexComp.cpp:382-396)."""
+    h, w = img.shape[:2]
+    H, W = (h + 3) & ~3, (w + 3) & ~3
+    if (H, W) == (h, w):
+        return img
+    out = np.zeros((H, W, 4), dtype=np.uint8)
+    out[:h, :w] = img
+    return out

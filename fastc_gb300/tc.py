@@ -1,0 +1,114 @@
+"""tc-compatible command line: compress an image to BC7 on the GPU.
+
+    python -m fastc_gb300.tc [-q N] [-n N] [-d OUT] [-nd] [-s WxH] IMAGE
+
+Mirrors FasTC's CLTool (CLTool/src/tc.cpp): BPTC at quality -q (annealing
+steps, default 50), the image zero-padded to whole blocks, "PSNR: %.3f"
+computed as FasTC's Image::ComputePSNR (alpha-premultiplied RGB, peak
+3*255^2) on the decoded blocks, and the output written to -d (or
+<basename>-bptc.png): a .ktx name stores the compressed blocks in FasTC's KTX
+layout, a .png name the decoded image. -nd writes nothing; -n N repeats the
+compression and reports the time. Options that choose host threading (-t,
+-j, -a, -simd) are accepted and have no effect: the work is distributed on
+the GPU. -l (CompressWithStats) and formats other than BPTC are refused.
+Inputs: PNG (8-bit), .npy RGBA8 arrays, raw RGBA (.rgba/.raw with -s WxH).
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+
+def usage(out=sys.stderr) -> None:
+    print(__doc__.strip(), file=out)
+
+
+def psnr(src: np.ndarray, dec: np.ndarray) -> float:
+    """FasTC's Image::ComputePSNR (Base/src/Image.cpp:206-255)."""
+    a0 = src[..., 3:4].astype(np.float64) / 255.0
+    a1 = dec[..., 3:4].astype(np.float64) / 255.0
+    d = a0 * src[..., :3].astype(np.float64) - a1 * dec[..., :3].astype(np.float64)
+    mse = float((d * d).sum()) / (src.shape[0] * src.shape[1])
+    if mse == 0.0:
+        return float("inf")
+    return 10.0 * np.log10(3.0 * 255.0 * 255.0 / mse)
+
+
+def main(argv=None) -> int:
+    argv = list(sys.argv[1:] if argv is None else argv)
+    if not argv:
+        usage()
+        return 1
+    quality, repeats, out_name, write_out = 50, 1, "", True
+    width = height = 0
+    i = 0
+    while i < len(argv) and argv[i].startswith("-"):
+        opt = argv[i]
+        if opt in ("-h", "--help"):
+            usage(sys.stdout)
+            return 0
+        if opt in ("-q", "-n", "-t", "-j", "-s", "-d", "-f"):
+            if i + 1 >= len(argv):
+                usage()
+                return 1
+            val = argv[i + 1]
+            if opt == "-q":
+                quality = int(val)
+            elif opt == "-n":
+                repeats = max(1, int(val))
+            elif opt == "-s":
+                width, height = (int(x) for x in val.lower().split("x"))
+            elif opt == "-d":
+                out_name = val
+            elif opt == "-f" and val not in ("BPTC", "BPTCLib"):
+                print(f"format {val} is not supported: this build encodes BC7 (BPTC) only", file=sys.stderr)
+                return 1
+            i += 2
+            continue
+        if opt == "-nd":
+            write_out = False
+        elif opt == "-l":
+            print("-l (CompressWithStats) is not supported: its shape selection differs from "
+                  "BPTCC::Compress", file=sys.stderr)
+            return 1
+        elif opt not in ("-a", "-v", "-simd"):
+            usage()
+            return 1
+        i += 1
+    if i >= len(argv) or quality < 0:
+        usage()
+        return 1
+    path = argv[i]
+
+    from . import imageio
+    from .bptc import CompressionJob, CompressionSettings, compress, decompress
+
+    img = imageio.pad_to_blocks(imageio.load_image(path, width, height))
+    h, w = img.shape[:2]
+    blocks = np.zeros(w * h, dtype=np.uint8)
+    settings = CompressionSettings(num_simulated_annealing_steps=quality)
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        compress(CompressionJob(img, blocks, w, h), settings)
+    dt = (time.perf_counter() - t0) / repeats
+    if repeats > 1:
+        print(f"Compression time: {dt * 1e3:.3f} ms")
+    dec = decompress(blocks, w, h)
+    print(f"PSNR: {psnr(img, dec):.3f}")
+    if write_out:
+        if not out_name:
+            base = os.path.splitext(os.path.basename(path))[0]
+            out_name = base + "-bptc.png"
+        with open(out_name, "wb") as f:
+            if out_name.endswith(".ktx"):
+                f.write(imageio.ktx_bytes(blocks, w, h))
+            else:
+                f.write(imageio.png_bytes(dec))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

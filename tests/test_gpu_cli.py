@@ -1,0 +1,36 @@
+"""The tc-compatible command line on the GPU: PNG in, KTX out, the blocks
+those of the library call, PSNR printed as FasTC's tc prints it."""
+import numpy as np
+import pytest
+
+from conftest import make_image
+
+pytestmark = pytest.mark.gpu
+
+
+def test_tc_png_to_ktx(gpu, tmp_path, capsys):
+    from fastc_gb300 import CompressionJob, CompressionSettings, compress, imageio, tc
+
+    img = make_image("tile_mix(41, 40, 24)")
+    src = tmp_path / "in.png"
+    src.write_bytes(imageio.png_bytes(img))
+    out = tmp_path / "out.ktx"
+    assert tc.main(["-q", "8", "-t", "4", "-d", str(out), str(src)]) == 0
+    blocks, w, h = imageio.read_ktx(out.read_bytes())
+    want = np.zeros(40 * 24, np.uint8)
+    compress(CompressionJob(img, want, 40, 24), CompressionSettings(num_simulated_annealing_steps=8))
+    assert (w, h) == (40, 24) and np.array_equal(blocks, want)
+    line = [l for l in capsys.readouterr().out.splitlines() if l.startswith("PSNR: ")]
+    assert line and float(line[0].split()[1]) > 20.0
+
+
+def test_tc_pads_odd_sizes_and_writes_decoded_png(gpu, tmp_path):
+    from fastc_gb300 import imageio, tc
+
+    img = make_image("tile_mix(42, 16, 16)")[:14, :9].copy()
+    src = tmp_path / "odd.npy"
+    np.save(src, img)
+    out = tmp_path / "odd-bptc.png"
+    assert tc.main(["-q", "0", "-d", str(out), str(src)]) == 0
+    dec = imageio.read_png(out.read_bytes())
+    assert dec.shape == (16, 12, 4)
