@@ -215,6 +215,22 @@ def reference_impl(args):
     print(json.dumps(line))
 
 
+def max_over_ranks(seconds: float, dist, device: str) -> float:
+    """The job's time: the slowest replica's (all ranks take part)."""
+    if dist is None:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_mpix_s(texels_per_replica: int, world: int, steps: int, seconds: float) -> float:
+    """Whole-job throughput: every rank encodes its own replica of the set."""
+    return texels_per_replica * world * steps / seconds / 1e6
+
+
 SERVE_SEED = 11
 
 
@@ -352,11 +368,8 @@ def main():
         barrier()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     dt = sum(step_ms) / 1e3
-    t = torch.tensor([dt], device="cuda")
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    dt = float(t.item())
-    value = total_px * world * args.steps / dt / 1e6
+    dt = max_over_ranks(dt, dist, "cuda")
+    value = aggregate_mpix_s(total_px, world, args.steps, dt)
     flags = plan.flags()
 
     # --- plain: one encode call per texture ---
@@ -413,8 +426,8 @@ def main():
     for _ in range(e2e_steps):
         compress_jobs(hjobs, settings)
     barrier()
-    e2e_dt = time.perf_counter() - t0
-    e2e_value = total_px * world * e2e_steps / e2e_dt / 1e6
+    e2e_dt = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+    e2e_value = aggregate_mpix_s(total_px, world, e2e_steps, e2e_dt)
     e2e_identical = all(np.array_equal(h.numpy(), d.cpu().numpy()) for h, d in zip(hout, dout))
 
     # --- PSNR of the batched output (GPU decoder, reference semantics) ---
