@@ -1,10 +1,12 @@
 """GPU parity: the sm_103a encoder through the C ABI against FasTC's golden
 outputs and against the oracle. Integer/byte results are compared bit for
 bit; the only tolerance is the q>0 PSNR bar against the reference (0.05 dB)."""
+import os
+
 import numpy as np
 import pytest
 
-from conftest import golden_blocks, make_image
+from conftest import GOLDEN, golden_blocks, make_image
 
 pytestmark = pytest.mark.gpu
 
@@ -77,6 +79,23 @@ def test_q50_psnr_within_0p05db_of_reference(gpu, port, manifest, name):
     psnr = port.psnr(img, dec)
     ref = float(np.mean(case["psnr"]))
     assert abs(psnr - ref) <= 0.05, (psnr, case["psnr"])
+
+
+@pytest.mark.parametrize("name", ["tile_q50_psnr", "radial_q50_psnr"])
+def test_q50_per_block_error_within_reference_seed_spread(gpu, port, manifest, name):
+    """Per-block SSE (FasTC's premultiplied metric) against FasTC's own
+    blocks at three pinned seeds. Annealing draws differ per seed, so FasTC
+    against itself has about 7 % of blocks more than 1 % worse (16 SSE
+    floor); ours must stay within that spread, and the total within 0.5 %."""
+    case = manifest["quality"][name]
+    img = make_image(case["image"])
+    got = gpu_compress(img, case["steps"], seed=7)
+    sse = port.block_sse(img, port.decompress(got, img.shape[1], img.shape[0])).astype(np.float64)
+    ref = np.load(os.path.join(GOLDEN, name + "_sse.npy")).astype(np.float64)
+    spread = max(np.mean((ref[i] + 16) / (ref[j] + 16) > 1.01) for i in range(3) for j in range(3) if i != j)
+    for r in ref:
+        assert np.mean((sse + 16) / (r + 16) > 1.01) <= spread + 0.01
+        assert abs(sse.sum() / r.sum() - 1.0) <= 0.005
 
 
 @pytest.mark.parametrize("mask", [0x41, 0xF0, 0x02, 0x80, 0x0C])
