@@ -1,0 +1,54 @@
+"""The configurations at full size, through checks that do not need the
+reference to run at that size: config 2 (2048x2048 tile mix) bit-exact
+against the oracle at q0 and decoded identically by the GPU and the oracle
+decoder at q50; config 5's content (radial alpha, modes 4-7) at q100 the
+same alone and batched, and deterministic."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import make_image
+
+pytestmark = pytest.mark.gpu
+
+
+def _compress(img, steps, seed=1):
+    from fastc_gb300 import CompressionSettings, compress_image_data
+
+    return compress_image_data(img, img.shape[1], img.shape[0],
+                               CompressionSettings(num_simulated_annealing_steps=steps, seed=seed))
+
+
+def test_config2_q0_bit_exact_and_q50_decodes_alike(gpu, port):
+    from fastc_gb300 import decompress
+
+    img = make_image("tile_mix(2, 2048, 2048)")
+    got = _compress(img, 0)
+    want = port.compress_mt(img, steps=0, threads=os.cpu_count())
+    bad = np.nonzero((got.reshape(-1, 16) != want.reshape(-1, 16)).any(1))[0]
+    assert bad.size == 0, (bad.size, bad[:8])
+    q50 = _compress(img, 50)
+    dec = decompress(q50, 2048, 2048)
+    assert np.array_equal(dec, port.decompress(q50, 2048, 2048))
+    assert port.psnr(img, dec) >= port.psnr(img, port.decompress(got, 2048, 2048)) - 0.01
+
+
+def test_config5_content_q100_alone_equals_batched(gpu):
+    import torch
+
+    from fastc_gb300 import CompressionJob, CompressionSettings, compress_jobs
+
+    img = make_image("tile_mix_radial_alpha(9, 1024, 1024, 0, 0, 1024, 1024)")
+    small = make_image("tile_mix(10, 96, 64)")
+    alone = _compress(img, 100, seed=3)
+    assert np.array_equal(alone, _compress(img, 100, seed=3))
+    din = [torch.from_numpy(x).cuda() for x in (small, img)]
+    dout = [torch.zeros(x.shape[0] * x.shape[1], dtype=torch.uint8, device="cuda") for x in (small, img)]
+    compress_jobs([CompressionJob(a, b, x.shape[1], x.shape[0]) for a, b, x in zip(din, dout, (small, img))],
+                  CompressionSettings(num_simulated_annealing_steps=100, seed=3))
+    torch.cuda.synchronize()
+    assert np.array_equal(dout[1].cpu().numpy(), alone)
+    first = alone.reshape(-1, 16)[:, 0].astype(int)
+    modes = {(int(b) & -int(b)).bit_length() - 1 if b else 8 for b in np.unique(first)}
+    assert {4, 5} & modes  # the rotation / separate-alpha modes are in use
