@@ -127,13 +127,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic_per_block():
-    """DRAM bytes per block of the encode kernel from the committed ncu summary."""
+def profile_per_block():
+    """DRAM bytes and warp instructions per block of one encode launch, from
+    the committed ncu summary (profiles/bc7_encode_traffic.json)."""
     try:
         with open(os.path.join(ROOT, "profiles", "bc7_encode_traffic.json")) as f:
-            return float(json.load(f)["dram_bytes_per_block"])
+            d = json.load(f)
+        return float(d["dram_bytes_per_block"]), float(d["warp_instructions_per_block"])
     except Exception:
-        return None
+        return None, None
 
 
 def cpu_sample(imgs, budget_px: int):
@@ -361,11 +363,13 @@ def main():
     barrier()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     with ClockSampler(local_rank) as clocks:
+        torch.cuda.nvtx.range_push("timed_steps")  # lets ncu --nvtx-include pick these launches
         ev[0].record(stream)
         for k in range(args.steps):
             plan.launch()
             ev[k + 1].record(stream)
         barrier()
+        torch.cuda.nvtx.range_pop()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     dt = sum(step_ms) / 1e3
     dt = max_over_ranks(dt, dist, "cuda")
@@ -446,7 +450,7 @@ def main():
     step_s = dt / args.steps
     algo_bytes = 80.0 * total_blocks  # 64 B of texels in + 16 B of block out
     achieved = algo_bytes / step_s / 1e9
-    tpb = profile_traffic_per_block()
+    tpb, ipb = profile_per_block()
 
     line = {
         "metric": METRIC, "value": value, "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
@@ -471,6 +475,18 @@ def main():
                              "traffic counts the stages' fit state exchanged through HBM"},
         "clocks": clocks.summary(),
     }
+    if ipb:
+        # compute roofline of the issue-bound encoder: warp instructions per
+        # block (ncu, committed summary) x blocks/s (this run) against
+        # 4 schedulers x SMs x the SM clock seen during the timed region
+        cs = line["clocks"]
+        mhz = cs.get("sm_mhz") or cs.get("sm_max_mhz") or 2070.0
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        issued = ipb * total_blocks / step_s
+        peak_issue = 4.0 * sms * mhz * 1e6
+        line["issue_roofline"] = {"achieved": issued, "peak": peak_issue, "unit": "warp-inst/s",
+                                  "frac": issued / peak_issue,
+                                  "instructions_per_block": ipb, "sms": sms, "sm_mhz": mhz}
     if rank == 0 and not args.no_cpu_baseline:
         cb, sample, outs = run_cpu_baseline(imgs, args.cpu_budget_px)
         # same bytes as the GPU on the sample
