@@ -517,7 +517,7 @@ __device__ __forceinline__ uint32_t class_begin(const uint16_t *local, const uin
 // One launch per class (the mode is a compile-time constant, so each
 // kernel holds only its own mode's path).
 template <int C>
-__global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 2 : 4)) setup_kernel(
+__global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 3 : 6)) setup_kernel(
     const JobDev *__restrict__ jobs, uint32_t nb, const BlockSel *__restrict__ sel,
     const uint2 *__restrict__ desc, const uint16_t *__restrict__ local,
     const uint32_t *__restrict__ chunk, PipelineCounters *__restrict__ ctr,
