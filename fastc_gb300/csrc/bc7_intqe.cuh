@@ -116,6 +116,66 @@ __device__ __forceinline__ int pair_term(uint32_t e, const uint4 *pal, int j1, b
   return second ? t2 : t1;
 }
 
+// A lower bound on the uniform-metric QuantizedError of n texels against
+// ANY pair of endpoints, for pruning fits that cannot win their block.
+// Every palette colour is the exact interpolation rounded per channel (at
+// most half a unit), so it lies within one unit of the line through the
+// endpoints; a texel at distance d from that line has error at least
+// max(0, d - 1)^2 >= d^2 - 2d. Summed: S - 2 sqrt(n S) (Cauchy-Schwarz),
+// with S = sum d^2 >= R, the scatter left after the best-fitting line
+// (trace minus largest eigenvalue of the scatter matrix); the bound grows
+// with S for S >= n, so R - 2 sqrt(n R) holds whenever R >= n. The largest
+// eigenvalue of the scatter A scaled to unit trace is at most
+// sqrt(|A^2|_F) (the fourth root of the sum of the eigenvalues' fourth
+// powers). The scatter is exact in integers; the float steps after it are
+// covered by a margin of 1e-5 of the trace.
+__device__ __forceinline__ float qe_lower_bound(const uint32_t *pts, int stride, int n) {
+  int s[4] = {0, 0, 0, 0}, q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < n; k++) {
+    const uint32_t e = pts[k * stride];
+    int v[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      v[c] = (int)((e >> (8 * c)) & 0xFF);
+      s[c] += v[c];
+    }
+    int m = 0;
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int b = a; b < 4; b++) q[m++] += v[a] * v[b];
+  }
+  // n * scatter: entries below 16 * 16 * 255^2 < 2^24, exact in float
+  float A[4][4];
+  int tr = 0, m = 0;
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = a; b < 4; b++) {
+      const int v = n * q[m++] - s[a] * s[b];
+      if (a == b) tr += v;
+      A[a][b] = A[b][a] = (float)v;
+    }
+  if (tr <= 0) return 0.0f;
+  const float inv = 1.0f / (float)tr;
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) A[a][b] *= inv;
+  float f = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = a; b < 4; b++) {
+      const float v = A[a][0] * A[0][b] + A[a][1] * A[1][b] + A[a][2] * A[2][b] + A[a][3] * A[3][b];
+      f += (a == b ? 1.0f : 2.0f) * v * v;
+    }
+  const float lam = sqrtf(sqrtf(f));
+  const float R = fmaxf(0.0f, 1.0f - lam - 1e-5f) * ((float)tr / (float)n);
+  const float fn = (float)n;
+  return R >= fn ? fmaxf(0.0f, R - 2.0f * sqrtf(fn * R) - 1e-3f * R) : 0.0f;
+}
+
 // Sixteen texels in registers (one-subset modes; texel k is point k).
 // pr: the projected points of the rotation modes (the texel with the
 // rotated channel and alpha 255); for other modes the texels themselves.

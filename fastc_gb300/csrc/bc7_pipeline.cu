@@ -521,8 +521,7 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 3 : 6)) s
     const JobDev *__restrict__ jobs, uint32_t nb, const BlockSel *__restrict__ sel,
     const uint2 *__restrict__ desc, const uint16_t *__restrict__ local,
     const uint32_t *__restrict__ chunk, PipelineCounters *__restrict__ ctr,
-    TaskState *__restrict__ state, AnnealRec *__restrict__ arec, uint32_t *__restrict__ keys,
-    uint32_t *status) {
+    TaskState *__restrict__ state, AnnealRec *__restrict__ arec, uint32_t *status) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr kA = mode_attr(kMode);
   __shared__ uint32_t s_px[kSetupThreads * 17];
@@ -597,7 +596,6 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 3 : 6)) s
     o.steps = (uint16_t)jb.steps;
     o.pbit = (uint8_t)st.pbit;
     o.flags = (uint8_t)((st.anneal ? kTaskAnneal : 0u) | (jb.metric ? kTaskNonuniform : 0u));
-    state[t] = o;
     // append to the class's annealing list (warp-aggregated)
     const uint32_t peers = __ballot_sync(__activemask(), st.anneal);
     if (st.anneal) {
@@ -605,6 +603,10 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 3 : 6)) s
       uint32_t pos = 0;
       if (lane == leader) pos = atomicAdd(&ctr->anneal_count[C], (uint32_t)__popc(peers));
       pos = __shfl_sync(peers, pos, leader) + __popc(peers & ((1u << lane) - 1u));
+      // the bound stage reads the fit's error bound, list position and
+      // point count from idx (the re-index stage rewrites it)
+      const float lb = jb.metric ? 0.0f : qe_lower_bound(pts, kSetupThreads, c.n);
+      o.idx = (uint64_t)__float_as_uint(lb) | ((uint64_t)pos << 32) | ((uint64_t)c.n << 56);
       uint4 *r = reinterpret_cast<uint4 *>(arec + begin + pos);
 #pragma unroll
       for (int q = 0; q < 4; q++)
@@ -616,19 +618,110 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 3 : 6)) s
                         (uint32_t)o.steps | ((uint32_t)c.n << 16) | ((uint32_t)o.pbit << 24));
       r[6] = make_uint4((uint32_t)tk.rot | ((uint32_t)o.flags << 8), o.p1, o.p2, ef);
       r[7] = make_uint4((uint32_t)o.pbit, 0u, 0u, 0u);
-      if (kA.subsets > 1) {
-        // rank among the class's fits with as many points (sorted below)
-        const uint32_t rank = atomicAdd(&ctr->nhist[C][c.n], 1u);
-        keys[begin + pos] = ((uint32_t)c.n << 24) | rank;
+    }
+    state[t] = o;
+  }
+}
+
+// Per block, after every class's setup: FasTC keeps the candidate (mode and
+// shape slot) with the least total error, and annealing only lowers a fit's
+// error, so the winner's final total is at most U, the least total at the
+// setup errors. A candidate whose error lower bound exceeds U cannot win:
+// its fits skip the annealing and keep their setup errors, which are at
+// least the bound, so the arg-min of the choose stage is unchanged. The
+// bound of a multi-subset candidate is the sum over its subsets (a fit
+// that does not anneal counts with its error); a rotation fit competes on
+// its own (the mode keeps its best rotation), with its exact alpha error
+// added. The fits left to anneal get their rank among the class's fits
+// with as many points (point-count order for the annealing lanes), the
+// others a dead key.
+constexpr uint32_t kDeadKey = 0xFFFFFFFFu;
+
+__device__ __forceinline__ void keep_fit(PipelineCounters *ctr, uint32_t *keys, uint32_t base,
+                                         uint64_t info, bool alive, int c) {
+  const uint32_t pos = (uint32_t)(info >> 32) & 0xFFFFFFu;
+  const int n = (int)(info >> 56);
+  const int lane = threadIdx.x & 31;
+  const unsigned act = __activemask();
+  const unsigned grp = __match_any_sync(act, alive ? (unsigned)(c * 32 + n) : 0xFFFFFFFFu);
+  const int leader = __ffs(grp) - 1;
+  uint32_t r0 = 0;
+  if (alive && lane == leader) r0 = atomicAdd(&ctr->nhist[c][n], (uint32_t)__popc(grp));
+  r0 = __shfl_sync(act, r0, leader);
+  keys[base + pos] = alive ? ((uint32_t)n << 24) | (r0 + __popc(grp & ((1u << lane) - 1u))) : kDeadKey;
+}
+
+__device__ __forceinline__ float fit_bound(const TaskState &o) {
+  return (o.flags & kTaskAnneal) ? __uint_as_float((uint32_t)o.idx) : (float)o.err;
+}
+
+__global__ void __launch_bounds__(128) bound_kernel(uint32_t nb, const BlockSel *__restrict__ sel,
+                                                    const uint16_t *__restrict__ local,
+                                                    const uint32_t *__restrict__ chunk,
+                                                    const TaskState *__restrict__ state,
+                                                    PipelineCounters *__restrict__ ctr,
+                                                    uint32_t *__restrict__ keys) {
+  const uint32_t gl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gl >= nb) return;
+  const BlockSel bs = sel[gl];
+  if (bs.done) return;
+  const Selection s = sel_of(bs);
+  const uint32_t modes = bs.modes;
+  const uint32_t nshapes = s.nshapes < 5 ? s.nshapes : 5;
+  double U = DBL_MAX;
+  for (int pass = 0; pass < 2; pass++) {
+    for (int oi = 0; oi < 8; oi++) {
+      const int mode = mode_order(oi);
+      if (!(modes & (1u << mode))) continue;
+      const ModeAttr a = mode_attr(mode);
+      const int nim = mode == 4 ? 2 : 1;
+      uint32_t cbase[2];
+      for (int k = 0; k < nim; k++)
+        cbase[k] = scanned(local, chunk, (uint64_t)class_of(mode, k) * nb + gl);
+      uint32_t t = cbase[0];
+      int slot_rank = 0;
+      for (uint32_t sl = 0; sl < nshapes; sl++) {
+        if (a.subsets != 1 && (uint32_t)a.subsets != s.nparts[sl]) continue;
+        if (s.shape[sl] >= 16 && mode == 0) continue;
+        if (a.has_rotation) {
+          for (int r = 0; r < 4; r++)
+            for (int k = 0; k < nim; k++) {
+              const uint32_t tt = cbase[k] + (uint32_t)(slot_rank * 4 + r);
+              const TaskState &o = state[tt];
+              if (pass == 0) {
+                U = fmin(U, o.err + o.aerr);
+              } else if (o.flags & kTaskAnneal) {
+                const int c = class_of(mode, k);
+                const bool alive = !((double)fit_bound(o) + o.aerr > U + 1.0);
+                keep_fit(ctr, keys, scanned(local, chunk, (uint64_t)c * nb), o.idx, alive, c);
+              }
+            }
+        } else if (pass == 0) {
+          double total = 0.0;
+          for (int ci = 0; ci < a.subsets; ci++) total = total + state[t + ci].err;
+          U = fmin(U, total);
+        } else {
+          double lb = 0.0;
+          for (int ci = 0; ci < a.subsets; ci++) lb += (double)fit_bound(state[t + ci]);
+          const bool alive = !(lb > U + 1.0);
+          const int c = class_of(mode, 0);
+          const uint32_t base = scanned(local, chunk, (uint64_t)c * nb);
+          for (int ci = 0; ci < a.subsets; ci++) {
+            const TaskState &o = state[t + ci];
+            if (o.flags & kTaskAnneal) keep_fit(ctr, keys, base, o.idx, alive, c);
+          }
+        }
+        if (!a.has_rotation) t += (uint32_t)a.subsets;
+        slot_rank++;
       }
     }
   }
 }
 
-// Multi-subset classes: the order in which the annealing lanes take the
-// class's fits, by point count (most points first), so that the lanes of a
-// warp loop over the same number of texels. perm[k] = list index of the
-// k-th fit to take.
+// The order in which the annealing lanes take the class's fits that are
+// left after the bound stage, by point count (most points first), so that
+// the lanes of a warp loop over the same number of texels. perm[k] = list
+// index of the k-th fit to take.
 template <int C>
 __global__ void __launch_bounds__(128) order_kernel(uint32_t nb, const uint16_t *__restrict__ local,
                                                     const uint32_t *__restrict__ chunk,
@@ -649,7 +742,7 @@ __global__ void __launch_bounds__(128) order_kernel(uint32_t nb, const uint16_t 
   const uint32_t base = scanned(local, chunk, (uint64_t)C * nb);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
     const uint32_t key = keys[base + i];
-    perm[base + s_off[key >> 24] + (key & 0xFFFFFFu)] = i;
+    if (key != kDeadKey) perm[base + s_off[key >> 24] + (key & 0xFFFFFFu)] = i;
   }
 }
 
@@ -930,10 +1023,17 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   uint32_t *proj = kRot ? s_proj + threadIdx.x : pts;
   uint4 *pal = s_pal + threadIdx.x;
   uint32_t *palf = reinterpret_cast<uint32_t *>(s_pal) + threadIdx.x;  // float-metric palette
-  const uint32_t count = kCont ? ctr->cont_count[C] : ctr->anneal_count[C];
+  // the fits left after the bound stage, in the order of perm
+  uint32_t count = 0;
+  if (kCont) {
+    count = ctr->cont_count[C];
+  } else {
+#pragma unroll
+    for (int n = 0; n <= 16; n++) count += ctr->nhist[C][n];
+  }
   const uint32_t lbase = scanned(local, chunk, (uint64_t)C * nb);
   const AnnealRec *list = kCont ? clist : arec + lbase;
-  constexpr bool kOrdered = !kCont && a.subsets > 1;  // taken in point-count order
+  constexpr bool kOrdered = !kCont;
   unsigned long long *cursor = kCont ? &ctr->cont_next[C] : &ctr->anneal_next[C];
   Lane s;
   uint32_t ereg[16], preg[16];
@@ -1404,8 +1504,11 @@ cudaError_t class_streams_create(ClassStreams *cs) {
   cudaError_t e = cudaSuccess;
   for (int b = 0; b < 2 && e == cudaSuccess; b++) {
     e = cudaEventCreateWithFlags(&cs->fork[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&cs->bound[b], cudaEventDisableTiming);
     for (int c = 0; c < kClasses && e == cudaSuccess; c++)
       e = cudaEventCreateWithFlags(&cs->join[b][c], cudaEventDisableTiming);
+    for (int c = 0; c < kClasses && e == cudaSuccess; c++)
+      e = cudaEventCreateWithFlags(&cs->setup[b][c], cudaEventDisableTiming);
   }
   for (int b = 0; b < 2 && e == cudaSuccess; b++)
     for (int c = 0; c < kClasses && e == cudaSuccess; c++)
@@ -1420,8 +1523,11 @@ void class_streams_destroy(ClassStreams *cs) {
       if (cs->side[b][c]) cudaStreamDestroy(cs->side[b][c]);
   for (int b = 0; b < 2; b++) {
     if (cs->fork[b]) cudaEventDestroy(cs->fork[b]);
-    for (int c = 0; c < kClasses; c++)
+    if (cs->bound[b]) cudaEventDestroy(cs->bound[b]);
+    for (int c = 0; c < kClasses; c++) {
       if (cs->join[b][c]) cudaEventDestroy(cs->join[b][c]);
+      if (cs->setup[b][c]) cudaEventDestroy(cs->setup[b][c]);
+    }
   }
   *cs = ClassStreams{};
 }
@@ -1466,24 +1572,30 @@ constexpr int class_block_fits(int c) {
 }
 
 template <int C>
-void launch_class(const ChunkArgs &a, cudaStream_t s) {
-  // the annealing kernel is persistent: no more CTAs than can be resident
-  static const int anneal_res = resident_ctas(anneal_kernel<C, false>, kAnnealThreads);
-  // below the resident limit, so that setup and select CTAs of other
-  // chunks and classes share the SMs
-  const int anneal_per_sm = anneal_res < a.anneal_ctas ? anneal_res : a.anneal_ctas;
-  // setup: one thread per fit (latency-bound; threads past the class's
-  // fits return at once)
+void launch_setup(const ChunkArgs &a, cudaStream_t s) {
+  // one thread per fit (latency-bound; threads past the class's fits
+  // return at once)
   const uint64_t fits = (uint64_t)a.nb * class_block_fits(C);
   const uint64_t setup_ctas_max = (uint64_t)a.sm_count * 128;
   uint64_t setup_ctas = (fits + kSetupThreads - 1) / kSetupThreads;
   if (setup_ctas > setup_ctas_max) setup_ctas = setup_ctas_max;
   setup_kernel<C><<<(unsigned)setup_ctas, kSetupThreads, 0, s>>>(a.jobs, a.nb, a.sel, a.desc, a.local,
                                                            a.chunk, a.ctr, a.state, a.arec,
-                                                           a.keys, a.status);
-  if (mode_attr(class_mode(C)).subsets > 1)
-    order_kernel<C><<<(unsigned)setup_ctas, 128, 0, s>>>(a.nb, a.local, a.chunk, a.ctr, a.keys,
-                                                         a.perm);
+                                                           a.status);
+}
+
+template <int C>
+void launch_anneal(const ChunkArgs &a, cudaStream_t s) {
+  // the annealing kernel is persistent: no more CTAs than can be resident
+  static const int anneal_res = resident_ctas(anneal_kernel<C, false>, kAnnealThreads);
+  // below the resident limit, so that setup and select CTAs of other
+  // chunks and classes share the SMs
+  const int anneal_per_sm = anneal_res < a.anneal_ctas ? anneal_res : a.anneal_ctas;
+  const uint64_t fits = (uint64_t)a.nb * class_block_fits(C);
+  const uint64_t order_ctas_max = (uint64_t)a.sm_count * 16;
+  uint64_t order_ctas = (fits + 127) / 128;
+  if (order_ctas > order_ctas_max) order_ctas = order_ctas_max;
+  order_kernel<C><<<(unsigned)order_ctas, 128, 0, s>>>(a.nb, a.local, a.chunk, a.ctr, a.keys, a.perm);
   anneal_kernel<C, false><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
       a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.yield_lanes, a.state);
   if (mode_attr(class_mode(C)).has_rotation)
@@ -1491,18 +1603,26 @@ void launch_class(const ChunkArgs &a, cudaStream_t s) {
         a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.yield_lanes, a.state);
 }
 
-void launch_class_any(int c, const ChunkArgs &a, cudaStream_t s) {
+void launch_class_any(int c, bool anneal, const ChunkArgs &a, cudaStream_t s) {
   switch (c) {
-    case 0: launch_class<0>(a, s); break;
-    case 1: launch_class<1>(a, s); break;
-    case 2: launch_class<2>(a, s); break;
-    case 3: launch_class<3>(a, s); break;
-    case 4: launch_class<4>(a, s); break;
-    case 5: launch_class<5>(a, s); break;
-    case 6: launch_class<6>(a, s); break;
-    case 7: launch_class<7>(a, s); break;
-    default: launch_class<8>(a, s); break;
+#define FASTC_CLASS_CASE(k) \
+    case k: anneal ? launch_anneal<k>(a, s) : launch_setup<k>(a, s); break;
+    FASTC_CLASS_CASE(0)
+    FASTC_CLASS_CASE(1)
+    FASTC_CLASS_CASE(2)
+    FASTC_CLASS_CASE(3)
+    FASTC_CLASS_CASE(4)
+    FASTC_CLASS_CASE(5)
+    FASTC_CLASS_CASE(6)
+    FASTC_CLASS_CASE(7)
+    default: anneal ? launch_anneal<8>(a, s) : launch_setup<8>(a, s); break;
+#undef FASTC_CLASS_CASE
   }
+}
+
+void launch_bound(const ChunkArgs &a, cudaStream_t s) {
+  bound_kernel<<<(a.nb + 127) / 128, 128, 0, s>>>(a.nb, a.sel, a.local, a.chunk, a.state, a.ctr,
+                                                  a.keys);
 }
 
 // Classes in the order their work is enqueued: the longest first, so that
@@ -1581,21 +1701,39 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
                          b.arec, b.cont, b.cont_cap, b.keys, b.perm, rank.status, sm_count,
                          tune.anneal_ctas_per_sm < 1 ? 1 : tune.anneal_ctas_per_sm, tune.yield_lanes};
     if (cls) {
-      cudaError_t ce = cudaEventRecord(cls->fork[i & 1], st);
-      const cudaStream_t *side = cls->side[i & 1];
+      const int par = i & 1;
+      cudaError_t ce = cudaEventRecord(cls->fork[par], st);
+      const cudaStream_t *side = cls->side[par];
       for (int c = 0; c < kClasses && ce == cudaSuccess; c++)
-        ce = cudaStreamWaitEvent(side[c], cls->fork[i & 1], 0);
+        ce = cudaStreamWaitEvent(side[c], cls->fork[par], 0);
       if (ce != cudaSuccess) return (int)ce;
-      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], args, side[kClassOrder[k]]);
+      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], false, args, side[kClassOrder[k]]);
+      // the bound stage runs on the first class's stream once every
+      // class's setup is done; every class's annealing waits for it
+      const int lead = kClassOrder[0];
+      for (int c = 0; c < kClasses && ce == cudaSuccess; c++) {
+        if (c == lead) continue;
+        ce = cudaEventRecord(cls->setup[par][c], side[c]);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(side[lead], cls->setup[par][c], 0);
+      }
+      if (ce != cudaSuccess) return (int)ce;
+      launch_bound(args, side[lead]);
+      ce = cudaEventRecord(cls->bound[par], side[lead]);
       for (int c = 0; c < kClasses && ce == cudaSuccess; c++)
-        ce = cudaEventRecord(cls->join[i & 1][c], side[c]);
+        if (c != lead) ce = cudaStreamWaitEvent(side[c], cls->bound[par], 0);
+      if (ce != cudaSuccess) return (int)ce;
+      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], true, args, side[kClassOrder[k]]);
+      for (int c = 0; c < kClasses && ce == cudaSuccess; c++)
+        ce = cudaEventRecord(cls->join[par][c], side[c]);
       if (ce != cudaSuccess) return (int)ce;
       if (i > 0) {
         e = pack(bufs[(i - 1) & 1], prev_nb, (i - 1) & 1);
         if (e) return e;
       }
     } else {
-      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], args, st);
+      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], false, args, st);
+      launch_bound(args, st);
+      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], true, args, st);
       e = pack(b, nb, 0);
       if (e) return e;
     }

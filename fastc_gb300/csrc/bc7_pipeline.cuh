@@ -41,7 +41,11 @@ constexpr uint8_t kTaskNonuniform = 2u;  // nonuniform error metric
 struct __align__(16) TaskState {
   double err;     // CompressCluster's return value (colour part for modes 4/5)
   double aerr;    // alpha error (modes 4/5)
-  uint64_t idx;   // colour indices, 4 bits per texel
+  // colour indices, 4 bits per texel; for a fit that anneals, until the
+  // re-index stage writes its indices: the fit's error lower bound (float
+  // bits 0-31), its position in the class's annealing list (bits 32-55) and
+  // its point count (bits 56-63)
+  uint64_t idx;
   uint64_t aidx;  // alpha indices, 4 bits per texel (modes 4/5)
   uint32_t p1, p2;  // endpoints as bytes (grid values)
   float a1, a2;     // alpha endpoints (modes 4/5), as FasTC keeps them
@@ -91,7 +95,7 @@ struct PipelineCounters {
   unsigned long long cont_next[kClasses];    // refill cursors of the continuation lists
   uint32_t cont_count[kClasses];             // continuations of each class
   uint32_t reindex_count[kClasses];          // annealed winning fits of each class
-  uint32_t nhist[kClasses][17];              // annealing fits by point count (multi-subset classes)
+  uint32_t nhist[kClasses][17];              // fits left to anneal by point count
 };
 constexpr size_t kCountersSlot = 1024;
 static_assert(sizeof(PipelineCounters) <= kCountersSlot, "PipelineCounters fits its slot");
@@ -99,12 +103,16 @@ static_assert(sizeof(PipelineCounters) <= kCountersSlot, "PipelineCounters fits 
 // Side streams that run the classes' setup + annealing concurrently, forked
 // from and joined back into the caller's stream with events (both are
 // recorded into a CUDA graph when the caller's stream is being captured).
+// Between the two, the per-block bound stage waits for every class's setup
+// and the annealing of every class waits for it.
 // One set must not be enqueued on by two threads at once.
 // Chunks alternate between two sets, so that a class of chunk i + 1 starts
 // while the same class of chunk i drains.
 struct ClassStreams {
   cudaStream_t side[2][kClasses];
   cudaEvent_t fork[2];
+  cudaEvent_t setup[2][kClasses];  // a class's setup stage is done
+  cudaEvent_t bound[2];            // the block bounds are done
   cudaEvent_t join[2][kClasses];
 };
 cudaError_t class_streams_create(ClassStreams *cs);
