@@ -520,10 +520,16 @@ template <int C>
 __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 3 : 6)) setup_kernel(
     const JobDev *__restrict__ jobs, uint32_t nb, const BlockSel *__restrict__ sel,
     const uint2 *__restrict__ desc, const uint16_t *__restrict__ local,
-    const uint32_t *__restrict__ chunk, PipelineCounters *__restrict__ ctr,
-    TaskState *__restrict__ state, AnnealRec *__restrict__ arec, uint32_t *status) {
+    const uint32_t *__restrict__ chunk, const uint8_t *__restrict__ counts,
+    PipelineCounters *__restrict__ ctr, TaskState *__restrict__ state, AnnealRec *__restrict__ arec,
+    uint32_t *status) {
   constexpr int kMode = class_mode(C);
   constexpr ModeAttr kA = mode_attr(kMode);
+  // Mode 6 runs once per shape slot (CompressClusters searches the
+  // one-subset modes with every slot), on the same cluster: the setup is
+  // the same and only the annealing stream differs, so one thread per block
+  // sets it up and writes the fit of each slot.
+  constexpr bool kPerBlock = kMode == 6;
   __shared__ uint32_t s_px[kSetupThreads * 17];
   __shared__ uint32_t s_pts[16 * kSetupThreads];
   // palette of the integer QuantizedError (up to 8 entries; the 16-entry
@@ -534,11 +540,21 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 3 : 6)) s
   const uint32_t begin = class_begin(local, chunk, ctr, nb, C);
   const uint32_t end = class_begin(local, chunk, ctr, nb, C + 1);
   const int lane = threadIdx.x & 31;
-  for (uint32_t t = begin + blockIdx.x * blockDim.x + threadIdx.x; t < end;
-       t += gridDim.x * blockDim.x) {
-    const uint2 d = desc[t];
-    const uint32_t gl = d.x;
-    const int i = (int)(d.y >> 8);
+  const uint32_t items = kPerBlock ? nb : end - begin;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < items; k += gridDim.x * blockDim.x) {
+    uint32_t t, gl;
+    int i = 0, ndup = 1;
+    if (kPerBlock) {
+      gl = k;
+      ndup = (int)counts[(uint64_t)C * nb + gl];
+      if (ndup == 0) continue;
+      t = scanned(local, chunk, (uint64_t)C * nb + gl);
+    } else {
+      t = begin + k;
+      const uint2 d = desc[t];
+      gl = d.x;
+      i = (int)(d.y >> 8);
+    }
     const BlockSel bs = sel[gl];
     const JobDev &jb = jobs[bs.job];
     const Selection s = sel_of(bs);
@@ -588,38 +604,46 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 3 : 6)) s
     o.p2 = to_pixel(st.p2, 0xFFFFFFFFu, -1);
     o.gl = gl;
     o.mode = (uint8_t)kMode;
-    o.slot = (uint8_t)tk.slot;
     o.subset = (uint8_t)tk.subset;
     o.rotim = (uint8_t)((tk.rot << 1) | tk.im);
-    o.lcg = fit_seed(jb.seed, bx, by,
-                     (uint32_t)((kMode << 8) | (tk.slot << 7) | (tk.subset << 4) | (tk.rot << 1) | tk.im));
     o.steps = (uint16_t)jb.steps;
     o.pbit = (uint8_t)st.pbit;
     o.flags = (uint8_t)((st.anneal ? kTaskAnneal : 0u) | (jb.metric ? kTaskNonuniform : 0u));
-    // append to the class's annealing list (warp-aggregated)
-    const uint32_t peers = __ballot_sync(__activemask(), st.anneal);
-    if (st.anneal) {
-      const int leader = __ffs(peers) - 1;
-      uint32_t pos = 0;
-      if (lane == leader) pos = atomicAdd(&ctr->anneal_count[C], (uint32_t)__popc(peers));
-      pos = __shfl_sync(peers, pos, leader) + __popc(peers & ((1u << lane) - 1u));
-      // the bound stage reads the fit's error bound, list position and
-      // point count from idx (the re-index stage rewrites it)
-      const float lb = jb.metric ? 0.0f : qe_lower_bound(pts, kSetupThreads, c.n);
-      o.idx = (uint64_t)__float_as_uint(lb) | ((uint64_t)pos << 32) | ((uint64_t)c.n << 56);
-      uint4 *r = reinterpret_cast<uint4 *>(arec + begin + pos);
+    const float lb = st.anneal && !jb.metric ? qe_lower_bound(pts, kSetupThreads, c.n) : 0.0f;
+    const uint64_t idx0 = o.idx;
+#pragma unroll 1
+    for (int dup = 0; dup < (kPerBlock ? 2 : 1); dup++) {
+      const bool here = dup < ndup;
+      const int slot = kPerBlock ? class_task(s, C, dup).slot : tk.slot;
+      o.slot = (uint8_t)slot;
+      o.lcg = fit_seed(jb.seed, bx, by,
+                       (uint32_t)((kMode << 8) | (slot << 7) | (tk.subset << 4) | (tk.rot << 1) | tk.im));
+      o.idx = idx0;
+      // append to the class's annealing list (warp-aggregated)
+      const bool add = here && st.anneal;
+      const uint32_t peers = __ballot_sync(__activemask(), add);
+      if (add) {
+        const int leader = __ffs(peers) - 1;
+        uint32_t pos = 0;
+        if (lane == leader) pos = atomicAdd(&ctr->anneal_count[C], (uint32_t)__popc(peers));
+        pos = __shfl_sync(peers, pos, leader) + __popc(peers & ((1u << lane) - 1u));
+        // the bound stage reads the fit's error bound, list position and
+        // point count from idx (the re-index stage rewrites it)
+        o.idx = (uint64_t)__float_as_uint(lb) | ((uint64_t)pos << 32) | ((uint64_t)c.n << 56);
+        uint4 *r = reinterpret_cast<uint4 *>(arec + begin + pos);
 #pragma unroll
-      for (int q = 0; q < 4; q++)
-        r[q] = make_uint4(pts[(4 * q + 0) * kSetupThreads], pts[(4 * q + 1) * kSetupThreads],
-                          pts[(4 * q + 2) * kSetupThreads], pts[(4 * q + 3) * kSetupThreads]);
-      const uint32_t ef = __float_as_uint((float)o.err);
-      r[4] = make_uint4((uint32_t)c.tex, (uint32_t)(c.tex >> 32), o.p1, o.p2);
-      r[5] = make_uint4(ef, o.lcg, t,
-                        (uint32_t)o.steps | ((uint32_t)c.n << 16) | ((uint32_t)o.pbit << 24));
-      r[6] = make_uint4((uint32_t)tk.rot | ((uint32_t)o.flags << 8), o.p1, o.p2, ef);
-      r[7] = make_uint4((uint32_t)o.pbit, 0u, 0u, 0u);
+        for (int q = 0; q < 4; q++)
+          r[q] = make_uint4(pts[(4 * q + 0) * kSetupThreads], pts[(4 * q + 1) * kSetupThreads],
+                            pts[(4 * q + 2) * kSetupThreads], pts[(4 * q + 3) * kSetupThreads]);
+        const uint32_t ef = __float_as_uint((float)o.err);
+        r[4] = make_uint4((uint32_t)c.tex, (uint32_t)(c.tex >> 32), o.p1, o.p2);
+        r[5] = make_uint4(ef, o.lcg, t + (uint32_t)dup,
+                          (uint32_t)o.steps | ((uint32_t)c.n << 16) | ((uint32_t)o.pbit << 24));
+        r[6] = make_uint4((uint32_t)tk.rot | ((uint32_t)o.flags << 8), o.p1, o.p2, ef);
+        r[7] = make_uint4((uint32_t)o.pbit, 0u, 0u, 0u);
+      }
+      if (here) state[t + (uint32_t)dup] = o;
     }
-    state[t] = o;
   }
 }
 
@@ -1541,6 +1565,7 @@ struct ChunkArgs {
   const uint2 *desc;
   const uint16_t *local;
   const uint32_t *chunk;
+  const uint8_t *counts;
   PipelineCounters *ctr;
   TaskState *state;
   AnnealRec *arec;
@@ -1573,15 +1598,15 @@ constexpr int class_block_fits(int c) {
 
 template <int C>
 void launch_setup(const ChunkArgs &a, cudaStream_t s) {
-  // one thread per fit (latency-bound; threads past the class's fits
-  // return at once)
-  const uint64_t fits = (uint64_t)a.nb * class_block_fits(C);
+  // one thread per fit (per block for mode 6; latency-bound; threads past
+  // the class's fits return at once)
+  const uint64_t fits = (uint64_t)a.nb * (class_mode(C) == 6 ? 1 : class_block_fits(C));
   const uint64_t setup_ctas_max = (uint64_t)a.sm_count * 128;
   uint64_t setup_ctas = (fits + kSetupThreads - 1) / kSetupThreads;
   if (setup_ctas > setup_ctas_max) setup_ctas = setup_ctas_max;
   setup_kernel<C><<<(unsigned)setup_ctas, kSetupThreads, 0, s>>>(a.jobs, a.nb, a.sel, a.desc, a.local,
-                                                           a.chunk, a.ctr, a.state, a.arec,
-                                                           a.status);
+                                                           a.chunk, a.counts, a.ctr, a.state,
+                                                           a.arec, a.status);
 }
 
 template <int C>
@@ -1697,7 +1722,7 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     scan_local_u8_kernel<<<nchunks, kRankChunk, 0, st>>>(b.counts, n8, b.local, b.chunk);
     scan_chunks_kernel<<<1, 1024, 0, st>>>(b.chunk, nchunks, b.ctr);
     emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, b.counts, b.local, b.chunk, b.desc);
-    const ChunkArgs args{jobs,   nb,     b.sel,  b.desc,     b.local, b.chunk, b.ctr,      b.state,
+    const ChunkArgs args{jobs,   nb,     b.sel,  b.desc,     b.local, b.chunk, b.counts, b.ctr, b.state,
                          b.arec, b.cont, b.cont_cap, b.keys, b.perm, rank.status, sm_count,
                          tune.anneal_ctas_per_sm < 1 ? 1 : tune.anneal_ctas_per_sm, tune.yield_lanes};
     if (cls) {
