@@ -12,16 +12,25 @@
 //                   a mode and colour index width), so all fits of one class
 //                   are contiguous in the task arrays.
 //   emit_kernel     one thread per block writes its task descriptors.
-//   setup_kernel    one thread per cluster fit: PCA, k-means, least squares,
-//                   grid clamp, first QuantizedError (CP:921-1094, 632-919);
+//   setup_kernel    one thread per cluster fit (per block for mode 6, whose
+//                   two shape slots share the cluster): PCA, k-means, least
+//                   squares, grid clamp, first QuantizedError (CP:921-1094,
+//                   632-919), and an exact lower bound of the fit's error;
 //                   fits with annealing work go to their class's list.
+//   bound_kernel    one thread per block, after every class's setup: fits
+//                   of candidates whose lower bound exceeds the block's
+//                   least setup total cannot win and skip the annealing.
+//   order_kernel    the remaining fits of a class in point-count order.
 //   anneal_kernel   one persistent launch per class; one thread per fit,
 //                   refilled from the class list: the simulated annealing
-//                   (CP:538-630) on integer endpoints, with the error loop
-//                   on packed bytes (dp2a projection, a per-step palette of
-//                   interpolated colours, vabsdiff4 + dp4a squared error).
-//   pack_kernel     one thread per block: FasTC's arg-min over modes and the
-//                   128-bit packing (CP:1752-1817, 1096-1298).
+//                   (CP:538-630) on integer endpoints with an exact integer
+//                   QuantizedError (dp2a projection, paired palette, dp4a);
+//                   the rotation classes hand sparse warps' fits on to two
+//                   generations of continuation launches.
+//   choose_kernel   one thread per block: FasTC's arg-min over modes
+//                   (CP:1752-1817); reindex_kernel: indices of the winning
+//                   annealed fits; pack_kernel: the 128-bit packing
+//                   (CP:1096-1298).
 //
 // Blocks are processed in chunks so that the task arrays fit a fixed
 // scratch size; every stage is asynchronous and graph-capturable.
@@ -1014,12 +1023,19 @@ __device__ __forceinline__ bool anneal_step(Lane &s, const uint32_t (&ereg)[16],
   return false;
 }
 
-// kCont = false: the class's list of fits from the setup stage. When that
-// list is empty, a warp with at most yield_lanes lanes still annealing
-// writes their fits, mid-flight, to the class's continuation list and
-// exits, instead of running on with most lanes idle (fit lengths vary about
-// threefold). kCont = true: the continuation list, run to completion.
-template <int C, bool kCont>
+// Continuation lists: two generations for each rotation class (modes 4
+// and 5, classes 4-6), list (generation - 1) * 3 + class - 4.
+constexpr int kContLists = 6;
+__host__ __device__ constexpr int cont_list(int c, int gen) { return (gen - 1) * 3 + (c - 4); }
+
+// kPhase 0: the class's list of fits from the setup stage. When that list
+// is empty, a warp with at most yield_lanes lanes still annealing writes
+// their fits, mid-flight, to the class's first continuation list and
+// exits, instead of running on with most lanes idle (fit lengths vary
+// more than tenfold). kPhase 1: that list, handing on to the second list
+// the same way; kPhase 2: the second list, run to completion. Only the
+// rotation classes, whose fits are long, hand fits on.
+template <int C, int kPhase>
 __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
     uint32_t nb, const uint16_t *__restrict__ local, const uint32_t *__restrict__ chunk,
     PipelineCounters *__restrict__ ctr, const AnnealRec *__restrict__ arec,
@@ -1030,12 +1046,14 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   constexpr int kBits = class_im(C) ? a.alpha_idx_bits : a.idx_bits;
   constexpr bool kRot = a.has_rotation != 0;
   constexpr int T = kAnnealThreads;
-  // only classes with long fits (the rotation modes) hand fits on; short
-  // fits drain quickly
-  constexpr bool kYields = kRot;
+  constexpr bool kCont = kPhase > 0;
+  constexpr bool kYields = kRot && kPhase < 2;
   constexpr int kRefillBatch = kRot || kCont ? 1 : 4;
-  AnnealRec *clist = cont + (size_t)C * cont_cap;
-  if (kCont && blockIdx.x * (uint32_t)T >= ctr->cont_count[C]) return;
+  constexpr int kIn = kCont ? cont_list(C, kPhase) : 0;        // list read by a continuation phase
+  constexpr int kOut = kYields ? cont_list(C, kPhase + 1) : 0;  // list fits are handed on to
+  AnnealRec *clist = cont + (size_t)kIn * cont_cap;
+  AnnealRec *olist = cont + (size_t)kOut * cont_cap;
+  if (kCont && blockIdx.x * (uint32_t)T >= ctr->cont_count[kIn]) return;
   __shared__ uint8_t s_lut[8 * 3 * 256];
   __shared__ uint32_t s_pts[16 * T];
   __shared__ uint32_t s_proj[kRot ? 16 * T : 1];
@@ -1050,7 +1068,7 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   // the fits left after the bound stage, in the order of perm
   uint32_t count = 0;
   if (kCont) {
-    count = ctr->cont_count[C];
+    count = ctr->cont_count[kIn];
   } else {
 #pragma unroll
     for (int n = 0; n <= 16; n++) count += ctr->nhist[C][n];
@@ -1058,7 +1076,7 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
   const uint32_t lbase = scanned(local, chunk, (uint64_t)C * nb);
   const AnnealRec *list = kCont ? clist : arec + lbase;
   constexpr bool kOrdered = !kCont;
-  unsigned long long *cursor = kCont ? &ctr->cont_next[C] : &ctr->anneal_next[C];
+  unsigned long long *cursor = kCont ? &ctr->cont_next[kIn] : &ctr->anneal_next[C];
   Lane s;
   uint32_t ereg[16], preg[16];
   bool active = false, exhausted = false;
@@ -1132,17 +1150,17 @@ __global__ void __launch_bounds__(kAnnealThreads) anneal_kernel(
     }
     if (__all_sync(0xFFFFFFFFu, exhausted && !active)) break;
     // a lane finished (nmask != 0): with the list empty, maybe retire
-    if (!kCont && kYields && nmask) {
+    if (kYields && nmask) {
       const uint32_t act = __ballot_sync(0xFFFFFFFFu, active);
       if (__any_sync(0xFFFFFFFFu, exhausted) && __popc(act) <= yield_lanes) {
         // hand the unfinished fits on and retire the warp
         const int leader = __ffs(act) - 1;
         uint32_t pos = 0;
-        if (lane == leader) pos = atomicAdd(&ctr->cont_count[C], (uint32_t)__popc(act));
+        if (lane == leader) pos = atomicAdd(&ctr->cont_count[kOut], (uint32_t)__popc(act));
         pos = __shfl_sync(0xFFFFFFFFu, pos, leader) + __popc(act & ((1u << lane) - 1u));
         if (active) {
           // the list holds one record per lane of the grid, so pos < cont_cap
-          uint4 *w = reinterpret_cast<uint4 *>(clist + pos);
+          uint4 *w = reinterpret_cast<uint4 *>(olist + pos);
 #pragma unroll
           for (int q = 0; q < 4; q++)
             w[q] = make_uint4(pts[(4 * q + 0) * T], pts[(4 * q + 1) * T], pts[(4 * q + 2) * T],
@@ -1431,7 +1449,7 @@ size_t chunk_buffer_bytes(uint64_t nb, int tb, int sm_count) {
   b += (tmax * sizeof(uint2) + 255) & ~255ull;
   b += (tmax * sizeof(TaskState) + 255) & ~255ull;
   b += (tmax * sizeof(AnnealRec) + 255) & ~255ull;
-  b += (kClasses * cont_capacity(nb, tb, sm_count) * sizeof(AnnealRec) + 255) & ~255ull;
+  b += (kContLists * cont_capacity(nb, tb, sm_count) * sizeof(AnnealRec) + 255) & ~255ull;
   b += (nb * sizeof(uint2) + 255) & ~255ull;                      // winners
   b += ((uint64_t)kClasses * 3 * nb * sizeof(uint32_t) + 255) & ~255ull;  // re-index lists
   b += 2 * ((tmax * sizeof(uint32_t) + 255) & ~255ull);           // point-count keys, order
@@ -1475,7 +1493,7 @@ ChunkBuf carve_chunk(uint8_t *p, uint64_t nb, int tb, int sm_count) {
   p += ((uint64_t)tb * nb * sizeof(AnnealRec) + 255) & ~255ull;
   c.cont = reinterpret_cast<AnnealRec *>(p);
   c.cont_cap = (uint32_t)cont_capacity(nb, tb, sm_count);
-  p += ((uint64_t)kClasses * c.cont_cap * sizeof(AnnealRec) + 255) & ~255ull;
+  p += ((uint64_t)kContLists * c.cont_cap * sizeof(AnnealRec) + 255) & ~255ull;
   c.win = reinterpret_cast<uint2 *>(p);
   p += (nb * sizeof(uint2) + 255) & ~255ull;
   c.rlist = reinterpret_cast<uint32_t *>(p);
@@ -1612,7 +1630,7 @@ void launch_setup(const ChunkArgs &a, cudaStream_t s) {
 template <int C>
 void launch_anneal(const ChunkArgs &a, cudaStream_t s) {
   // the annealing kernel is persistent: no more CTAs than can be resident
-  static const int anneal_res = resident_ctas(anneal_kernel<C, false>, kAnnealThreads);
+  static const int anneal_res = resident_ctas(anneal_kernel<C, 0>, kAnnealThreads);
   // below the resident limit, so that setup and select CTAs of other
   // chunks and classes share the SMs
   const int anneal_per_sm = anneal_res < a.anneal_ctas ? anneal_res : a.anneal_ctas;
@@ -1621,11 +1639,14 @@ void launch_anneal(const ChunkArgs &a, cudaStream_t s) {
   uint64_t order_ctas = (fits + 127) / 128;
   if (order_ctas > order_ctas_max) order_ctas = order_ctas_max;
   order_kernel<C><<<(unsigned)order_ctas, 128, 0, s>>>(a.nb, a.local, a.chunk, a.ctr, a.keys, a.perm);
-  anneal_kernel<C, false><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
+  anneal_kernel<C, 0><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
       a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.yield_lanes, a.state);
-  if (mode_attr(class_mode(C)).has_rotation)
-    anneal_kernel<C, true><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
+  if (mode_attr(class_mode(C)).has_rotation) {
+    anneal_kernel<C, 1><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
         a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.yield_lanes, a.state);
+    anneal_kernel<C, 2><<<a.sm_count * anneal_per_sm, kAnnealThreads, 0, s>>>(
+        a.nb, a.local, a.chunk, a.ctr, a.arec, a.perm, a.cont, a.cont_cap, a.yield_lanes, a.state);
+  }
 }
 
 void launch_class_any(int c, bool anneal, const ChunkArgs &a, cudaStream_t s) {

@@ -93,7 +93,7 @@ struct PipelineCounters {
   uint32_t anneal_count[kClasses];           // fits of each class that anneal
   uint32_t tasks;                            // tasks in the current chunk
   unsigned long long cont_next[kClasses];    // refill cursors of the continuation lists
-  uint32_t cont_count[kClasses];             // continuations of each class
+  uint32_t cont_count[kClasses];             // records in each continuation list (six used)
   uint32_t reindex_count[kClasses];          // annealed winning fits of each class
   uint32_t nhist[kClasses][17];              // fits left to anneal by point count
 };
