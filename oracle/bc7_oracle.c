@@ -1382,6 +1382,40 @@ static void write_transparent(uint8_t out[16]) {
   put_bits(&w, 0, 121);
 }
 
+/* CompressClusters (CP:1752-1817): every selected mode over the searched
+ * shapes in the order {0,2,1,3,7,4,5,6}, strict-< arg-min, Pack. Returns the
+ * packed mode (8 when no mode applied: a transparent block is written). */
+static int compress_clusters(const uint32_t px[16], const selection *sel, uint32_t modes,
+                             const block_ctx *b, uint8_t out[16]) {
+  static const int order[8] = {0, 2, 1, 3, 7, 4, 5, 6};
+  double best = DBL_MAX;
+  int best_mode = 8;
+  params best_p, p;
+  memset(&best_p, 0, sizeof(best_p));
+  uint32_t nshapes = sel->nshapes < 5 ? sel->nshapes : 5;
+  for (int oi = 0; oi < 8; oi++) {
+    const int mode = order[oi];
+    if (!(modes & (1u << mode))) continue;
+    for (uint32_t si = 0; si < nshapes; si++) {
+      const int np = kMode[mode].subsets;
+      if (np != 1 && (uint32_t)np != sel->nparts[si]) continue;
+      if (sel->shape[si] >= 16 && mode == 0) continue;
+      const double e = compress_mode(mode, (int)sel->shape[si], (int)si, px, b, &p);
+      if (e < best) {
+        best = e;
+        best_mode = mode;
+        best_p = p;
+      }
+    }
+  }
+  if (best_mode == 8) { /* no mode applies to any searched shape */
+    write_transparent(out);
+    return 8;
+  }
+  pack(best_mode, &best_p, out);
+  return best_mode;
+}
+
 void bc7o_compress_block(const uint32_t px[16], const bc7o_settings *s,
                          uint32_t bx, uint32_t by, uint32_t *wm, uint32_t *lcg,
                          uint8_t out[16]) {
@@ -1408,32 +1442,142 @@ void bc7o_compress_block(const uint32_t px[16], const bc7o_settings *s,
   if (modes == 0) modes = s->block_modes & 0xFF;
 
   block_ctx b = {s, bx, by, lcg};
-  static const int order[8] = {0, 2, 1, 3, 7, 4, 5, 6};
+  compress_clusters(px, &sel, modes, &b, out);
+}
+
+/* ------------------------------------------------------------------------ */
+/* CompressWithStats: the logging block encoder (CP:1862-2183)               */
+/* ------------------------------------------------------------------------ */
+
+/* UpdateErrorEstimate (CP:1930-1936). */
+static void update_estimate(double *est, int mode, double e) {
+  if (est[mode] == -1.0 || e < est[mode]) est[mode] = e;
+}
+
+/* EstimateTwoClusterErrorStats / EstimateThreeClusterErrorStats
+ * (CP:1862-1928): the subset's bounding box quantised with two grids (the
+ * colour precisions of modes 1 and 3, or 0 and 2), each error recorded as
+ * the candidate mode's estimate; the shape error takes the smaller. */
+static double estimate_stats(const cluster *c, int three, uint32_t metric, double est[2]) {
+  float v[4];
+  for (int k = 0; k < 4; k++) v[k] = c->mx[k] - c->mn[k];
+  if (dot4(v, v) == 0) {
+    est[0] = est[1] = 0.0;
+    return 0.0;
+  }
+  const int nb = three ? 4 : 8;
+  const uint32_t m0 = three ? 0xFFF0F0F0u : 0xFFFCFCFCu;
+  const uint32_t m1 = three ? 0xFFF8F8F8u : 0xFFFEFEFEu;
+  const double bias = three ? 0.0001 : 0.0;
+  const double e0 = bias + (double)quantized_error(c, c->mn, c->mx, nb, m0, gMetricW[metric], NULL, NULL);
+  const double e1 = bias + (double)quantized_error(c, c->mn, c->mx, nb, m1, gMetricW[metric], NULL, NULL);
+  est[0] = e0; /* never negative, so the reference's min() branch is dead */
+  est[1] = e1;
+  double err = 0.0001;
+  err += e0 < e1 ? e0 : e1;
+  return err;
+}
+
+/* One shape loop of the logging encoder: nsub 2 (CP:2066-2114) or 3
+ * (CP:2118-2166). Returns 1 when a shape's estimate is below 1e-9. */
+static int stats_shapes(const uint32_t px[16], int nsub, uint32_t metric, selection *sel,
+                        bc7o_block_stats *st) {
+  const int three = nsub == 3;
+  const int slot = three ? 1 : 0;
   double best = DBL_MAX;
-  int best_mode = 8;
-  params best_p, p;
-  memset(&best_p, 0, sizeof(best_p));
-  uint32_t nshapes = sel.nshapes < 5 ? sel.nshapes : 5;
-  for (int oi = 0; oi < 8; oi++) {
-    const int mode = order[oi];
-    if (!(modes & (1u << mode))) continue;
-    for (uint32_t si = 0; si < nshapes; si++) {
-      const int np = kMode[mode].subsets;
-      if (np != 1 && (uint32_t)np != sel.nparts[si]) continue;
-      if (sel.shape[si] >= 16 && mode == 0) continue;
-      const double e = compress_mode(mode, (int)sel.shape[si], (int)si, px, &b, &p);
-      if (e < best) {
-        best = e;
-        best_mode = mode;
-        best_p = p;
-      }
+  for (int i = 0; i < 64; i++) {
+    double err = 0.0;
+    double acc[2] = {-1.0, -1.0};
+    for (int ci = 0; ci < nsub; ci++) {
+      cluster c;
+      make_cluster(px, i, nsub, ci, &c);
+      double e[2] = {-1.0, -1.0};
+      err += estimate_stats(&c, three, metric, e);
+      for (int k = 0; k < 2; k++)
+        if (e[k] >= 0.0) acc[k] = acc[k] == -1.0 ? e[k] : acc[k] + e[k];
+    }
+    if (acc[0] != -1.0) update_estimate(st->estimate, three ? 0 : 1, acc[0]);
+    if (acc[1] != -1.0) update_estimate(st->estimate, three ? 2 : 3, acc[1]);
+    if (err < best) {
+      if (three) st->three_shape[st->n_three++] = err;
+      else st->two_shape[st->n_two++] = err;
+      best = err;
+      sel->shape[slot] = (uint32_t)i;
+      sel->nparts[slot] = (uint32_t)nsub;
+    }
+    if (err < 1e-9) {
+      sel->modes = three ? MODES_THREE : MODES_TWO;
+      return 1;
     }
   }
-  if (best_mode == 8) { /* no mode applies to any searched shape */
-    write_transparent(out);
+  return 0;
+}
+
+/* CompressBC7Block with a BlockLogger (CP:1938-2183). Its shape selection
+ * differs from BoxSelection: opaque means every alpha is exactly 255, the
+ * modes are not narrowed by opacity (modes 4 and 5 stay on for opaque
+ * blocks, 1, 3 and 6 for the others), the 3-subset shapes are searched
+ * for opaque blocks even after an exact 2-subset shape, and the bounding
+ * boxes are quantised before their QuantizedError. The per-mode errors it
+ * logs stay -1: CompressClusters keeps min(error, -1) (CP:1801). */
+void bc7o_compress_block_stats(const uint32_t px[16], const bc7o_settings *s, uint32_t bx,
+                               uint32_t by, uint32_t *wm, uint32_t *lcg, uint8_t out[16],
+                               bc7o_block_stats *st) {
+  pthread_once(&gTablesOnce, build_tables);
+  pthread_once(&gMetricOnce, build_metric);
+  memset(st, 0, sizeof(*st));
+  for (int i = 0; i < 8; i++) st->estimate[i] = st->error[i] = -1.0;
+  int same = 1;
+  for (int i = 1; i < 16; i++) same = same && px[i] == px[0];
+  if (same) {
+    write_single_color(px[0], *wm, out);
+    (*wm)++;
+    st->mode = 5;
+    st->path = 0;
     return;
   }
-  pack(best_mode, &best_p, out);
+  int opaque = 1, transparent = 1;
+  for (int i = 0; i < 16; i++) {
+    const uint32_t a = px[i] >> 24;
+    if (a != 255) opaque = 0;
+    if (a != 0) transparent = 0;
+  }
+  if (transparent) {
+    write_transparent(out);
+    st->mode = 6;
+    st->path = 1;
+    return;
+  }
+  { /* mode 6's estimate: the whole block's box, 4 buckets (CP:2046-2058) */
+    cluster c;
+    make_cluster(px, 0, 1, 0, &c);
+    float v[4];
+    for (int k = 0; k < 4; k++) v[k] = c.mx[k] - c.mn[k];
+    if (dot4(v, v) == 0) {
+      st->estimate[6] = 0.0;
+    } else {
+      const double e = 0.0001 + (double)quantized_error(&c, c.mn, c.mx, 4, 0xFEFEFEFEu,
+                                                         gMetricW[s->metric], NULL, NULL);
+      update_estimate(st->estimate, 6, e);
+    }
+  }
+  selection sel;
+  sel.nshapes = 1;
+  sel.shape[0] = sel.shape[1] = 0;
+  sel.nparts[0] = sel.nparts[1] = 0;
+  sel.modes = 0xFF;
+  int path = 0;
+  if (stats_shapes(px, 2, s->metric, &sel, st)) path = 2;
+  if (opaque) {
+    sel.nshapes++;
+    if (stats_shapes(px, 3, s->metric, &sel, st)) path = 2;
+  }
+  if (path == 0) path = 3;
+  st->path = path;
+  uint32_t modes = sel.modes & s->block_modes;
+  if (modes == 0) modes = s->block_modes & 0xFF; /* as in bc7o_compress_block */
+  block_ctx b = {s, bx, by, lcg};
+  st->mode = compress_clusters(px, &sel, modes, &b, out);
 }
 
 /* ------------------------------------------------------------------------ */

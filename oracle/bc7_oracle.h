@@ -66,6 +66,23 @@ void bc7o_compress_block(const uint32_t px[16], const bc7o_settings *s,
                          uint32_t bx, uint32_t by, uint32_t *wm, uint32_t *lcg,
                          uint8_t out[16]);
 
+/* What CompressWithStats logs for one block (Compressor.cpp:1938-2183):
+ * the path (0 single colour, 1 transparent, 2 an exact shape, 3 searched),
+ * the packed mode, each mode's error estimate and logged error (-1 when
+ * unset), and every improving 2- and 3-subset shape estimate in order. */
+typedef struct {
+  int32_t path, mode;
+  double estimate[8], error[8];
+  int32_t n_two, n_three;
+  double two_shape[64], three_shape[64];
+} bc7o_block_stats;
+
+/* One block through the logging encoder (its own shape selection). */
+void bc7o_compress_block_stats(const uint32_t px[16], const bc7o_settings *s,
+                               uint32_t bx, uint32_t by, uint32_t *wm,
+                               uint32_t *lcg, uint8_t out[16],
+                               bc7o_block_stats *st);
+
 void bc7o_decompress(const uint8_t *blocks, uint8_t *rgba, uint32_t w,
                      uint32_t h);
 

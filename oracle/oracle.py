@@ -36,6 +36,39 @@ class Settings(C.Structure):
                 ("rng_mode", C.c_uint32), ("seed", C.c_uint32), ("exp_mode", C.c_uint32)]
 
 
+class BlockStats(C.Structure):
+    """bc7o_block_stats: what CompressWithStats logs for one block."""
+    _fields_ = [("path", C.c_int32), ("mode", C.c_int32), ("estimate", C.c_double * 8),
+                ("error", C.c_double * 8), ("n_two", C.c_int32), ("n_three", C.c_int32),
+                ("two_shape", C.c_double * 64), ("three_shape", C.c_double * 64)]
+
+
+_MODE_NAMES = ["Zero", "One", "Two", "Three", "Four", "Five", "Six", "Seven"]
+
+
+def stats_log(blocks) -> str:
+    """The text CompressWithStats writes to its log stream for (block index,
+    BlockStats) pairs in encode order: one "<index>: BlockStat_<name> --
+    <value>" line per statistic (Compressor.cpp:1373-1389, 1951-1993), the
+    improving shape estimates first, then the path, then (on return) the
+    mode and each mode's estimate and error. Doubles print as an ostream's
+    default 6 significant digits, i.e. printf's %g."""
+    lines = []
+    for idx, st in blocks:
+        def put(name, v):
+            lines.append(f"{idx}: BlockStat_{name} -- {v}\n")
+        for k in range(st.n_two):
+            put("TwoShapeEstimate", "%g" % st.two_shape[k])
+        for k in range(st.n_three):
+            put("ThreeShapeEstimate", "%g" % st.three_shape[k])
+        put("Path", st.path)
+        put("Mode", st.mode)
+        for m in range(8):
+            put(f"Mode{_MODE_NAMES[m]}Estimate", "%g" % st.estimate[m])
+            put(f"Mode{_MODE_NAMES[m]}Error", "%g" % st.error[m])
+    return "".join(lines)
+
+
 def _ptr(a: np.ndarray, t=_u8p):
     assert a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(t)
@@ -76,7 +109,38 @@ class Port:
         lib.bc7o_fit_seed.restype = C.c_uint32
         lib.bc7o_expf.argtypes = [C.c_float]
         lib.bc7o_expf.restype = C.c_float
+        lib.bc7o_compress_block_stats.argtypes = [_u32p, C.POINTER(Settings), C.c_uint32,
+                                                  C.c_uint32, _u32p, _u32p, _u8p,
+                                                  C.POINTER(BlockStats)]
         self.lib = lib
+
+    def compress_stats(self, img: np.ndarray, steps=0, modes=0xFF, metric=0,
+                       rng_mode=RNG_PER_FIT, seed=0, exp_mode=EXP_PORTABLE, state=None):
+        """The logging encoder (CompressWithStats with a log stream) over a
+        whole image in raster block order: (blocks, [(block index,
+        BlockStats)]). state = [LCG state, watermark counter], updated."""
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape[:2]
+        out = np.zeros(w * h, dtype=np.uint8)
+        st = np.zeros(2, dtype=np.uint32) if state is None else state
+        s = self.settings(steps, modes, metric, rng_mode, seed, exp_mode)
+        lcg = st[0:1]
+        wm = st[1:2]
+        blocks = []
+        bw = w // 4
+        for by in range(h // 4):
+            for bx in range(bw):
+                px = np.ascontiguousarray(
+                    img[4 * by:4 * by + 4, 4 * bx:4 * bx + 4].reshape(16, 4)).view(np.uint32).reshape(16)
+                dst = np.zeros(16, dtype=np.uint8)
+                bs = BlockStats()
+                self.lib.bc7o_compress_block_stats(_ptr(px, _u32p), C.byref(s), bx, by,
+                                                   _ptr(wm, _u32p), _ptr(lcg, _u32p), _ptr(dst),
+                                                   C.byref(bs))
+                i = by * bw + bx
+                out[16 * i:16 * i + 16] = dst
+                blocks.append((i, bs))
+        return out, blocks
 
     @staticmethod
     def settings(steps=0, modes=0xFF, metric=0, rng_mode=RNG_PER_FIT, seed=0,
@@ -158,7 +222,34 @@ class Reference:
         lib.ref_decompress.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32]
         lib.ref_box_selection.argtypes = [_u32p, C.c_int, _u32p]
         lib.ref_tables.argtypes = [_u8p, _u8p]
+        lib.ref_compress_stats.argtypes = [_u8p, _u8p] + [C.c_uint32] * 8 + [C.c_int, C.c_char_p,
+                                                                          C.c_size_t]
+        lib.ref_compress_stats.restype = C.c_size_t
         self.lib = lib
+
+    def compress_stats(self, img: np.ndarray, steps=0, modes=0xFF, metric=0, seed=None, wm=0):
+        """BPTCC::CompressWithStats with a log stream: (blocks, log text).
+        Its block loop runs while the row is <= YEnd without Compress's clamp
+        to height - 4 (Compressor.cpp:1583-1584), so a whole-image job
+        (YEnd = height) reads and writes one block row past the buffers; the
+        job here ends at the last block row (YEnd = height - 4)."""
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape[:2]
+        out = np.zeros(w * h, dtype=np.uint8)
+        if seed is not None:
+            self.lib.ref_set_seed(seed)
+        self.lib.ref_set_wm((wm - 1) & 0xFFFFFFFF if wm else 0xFFFFFFFF)
+        cap = 1 << 16
+        while True:
+            buf = C.create_string_buffer(cap)
+            n = self.lib.ref_compress_stats(_ptr(img), _ptr(out), w, h, 0, 0, w, h - 4, steps,
+                                            modes, metric, buf, cap)
+            if n < cap:
+                return out, buf.value.decode()
+            cap = n + 1
+            if seed is not None:
+                self.lib.ref_set_seed(seed)
+            self.lib.ref_set_wm((wm - 1) & 0xFFFFFFFF if wm else 0xFFFFFFFF)
 
     def compress(self, img: np.ndarray, steps=0, modes=0xFF, metric=0, seed=None, wm=0,
                  rect=None) -> np.ndarray:

@@ -8,6 +8,8 @@
 //   * ref_decompress      -> BPTCC::Decompress          (Decompressor.cpp:345)
 //   * ref_box_selection   -> BoxSelection               (Compressor.cpp:1670)
 //   * ref_compress_block  -> CompressBC7Block           (Compressor.cpp:1819)
+//   * ref_compress_stats  -> BPTCC::CompressWithStats   (Compressor.cpp:1577),
+//                            with its per-block log captured as text
 //   * ref_{get,set}_seed  -> g_seed, the annealing LCG  (Compressor.cpp:358)
 //   * ref_{get,set}_wm    -> gWMVal, the single-colour watermark counter
 //                            (Compressor.cpp:140)
@@ -80,6 +82,25 @@ double ref_compress_mode(const uint32_t px[16], int mode, int shape,
   cluster.SetShapeIndex(shape, nparts);
   BPTCC::CompressionMode::Params params;
   return BPTCC::CompressionMode(mode, s).Compress(params, shape, cluster);
+}
+
+// CompressWithStats over a job rectangle with a log stream: returns the
+// log's length and copies at most cap - 1 bytes of it, NUL-terminated.
+size_t ref_compress_stats(const uint8_t *rgba, uint8_t *out, uint32_t w, uint32_t h,
+                          uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
+                          uint32_t steps, uint32_t modes, int metric, char *log,
+                          size_t cap) {
+  FasTC::CompressionJob cj(FasTC::eCompressionFormat_BPTC, rgba, out, w, h,
+                           x0, y0, x1, y1);
+  std::stringstream ss;
+  BPTCC::CompressWithStats(cj, &ss, MakeSettings(steps, modes, metric));
+  const std::string text = ss.str();
+  if (cap > 0) {
+    const size_t n = text.size() < cap - 1 ? text.size() : cap - 1;
+    memcpy(log, text.data(), n);
+    log[n] = 0;
+  }
+  return text.size();
 }
 
 void ref_tables(uint8_t opt7[512], uint8_t opt6[1536]) {

@@ -37,6 +37,13 @@ CASES = {
     "radial_q16_seed": ("tile_mix_radial_alpha(5, 64, 64, 3000, 3000)", 16, 0, 0xC0FFEE),
 }
 
+# CompressWithStats with a log stream: name -> (generator call, steps, pinned
+# LCG seed or None); the blocks, the log's hash and the parsed statistics
+STATS = {
+    "tile_stats_q0": ("tile_mix(3, 64, 64)", 0, None),
+    "radial_stats_q16_seed": ("tile_mix_radial_alpha(4, 64, 64, 800, 1200)", 16, 0xACE1),
+}
+
 # PSNR reference points at q50: the reference with several pinned seeds
 QUALITY = {
     "tile_q50_psnr": ("tile_mix(21, 512, 512)", 50, [11, 22, 33]),
@@ -52,13 +59,66 @@ def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
+def parse_stats_log(text: str, nblocks: int):
+    """The per-block statistics of a CompressWithStats log, as arrays."""
+    path = np.full(nblocks, -1, np.int8)
+    mode = np.full(nblocks, -1, np.int8)
+    est = np.full((nblocks, 8), np.nan)
+    err = np.full((nblocks, 8), np.nan)
+    shapes = {2: ([], []), 3: ([], [])}  # (block index, estimate) of each improving shape
+    names = ["Zero", "One", "Two", "Three", "Four", "Five", "Six", "Seven"]
+    for line in text.splitlines():
+        idx, rest = line.split(": ", 1)
+        stat, val = rest.split(" -- ")
+        i, stat = int(idx), stat[len("BlockStat_"):]
+        if stat == "Path":
+            path[i] = int(val)
+        elif stat == "Mode":
+            mode[i] = int(val)
+        elif stat in ("TwoShapeEstimate", "ThreeShapeEstimate"):
+            k = 2 if stat.startswith("Two") else 3
+            shapes[k][0].append(i)
+            shapes[k][1].append(float(val))
+        else:
+            m = names.index(stat[4:-8] if stat.endswith("Estimate") else stat[4:-5])
+            (est if stat.endswith("Estimate") else err)[i, m] = float(val)
+    return dict(path=path, mode=mode, estimate=est, error=err,
+                two_block=np.array(shapes[2][0], np.int32), two=np.array(shapes[2][1]),
+                three_block=np.array(shapes[3][0], np.int32), three=np.array(shapes[3][1]))
+
+
+def make_stats(ref, manifest):
+    manifest["stats"] = {}
+    for name, (expr, steps, seed) in STATS.items():
+        img = make(expr)
+        blocks, log = ref.compress_stats(img, steps=steps, seed=seed)
+        blocks.tofile(os.path.join(HERE, name + ".bin"))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                            **parse_stats_log(log, len(blocks) // 16))
+        manifest["stats"][name] = {
+            "image": expr, "steps": steps, "lcg_seed": seed, "input_sha256": sha(img),
+            "blocks_sha256": sha(blocks),
+            "log_sha256": hashlib.sha256(log.encode()).hexdigest(), "log_bytes": len(log),
+        }
+        print(name, len(blocks) // 16, "blocks,", len(log), "log bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=O.DEFAULT_REFERENCE)
+    ap.add_argument("--stats-only", action="store_true",
+                    help="only (re)write the CompressWithStats fixtures")
     args = ap.parse_args()
     if not O.build_ref(args.reference):
         sys.exit("FasTC checkout not found; cannot regenerate fixtures")
     ref = O.Reference()
+    if args.stats_only:
+        with open(os.path.join(HERE, "manifest.json")) as f:
+            manifest = json.load(f)
+        make_stats(ref, manifest)
+        with open(os.path.join(HERE, "manifest.json"), "w") as f:
+            json.dump(manifest, f, indent=1, sort_keys=True)
+        return
     manifest = {"cases": {}, "quality": {}}
     for name, (expr, steps, metric, seed) in CASES.items():
         img = make(expr)
@@ -89,6 +149,7 @@ def main():
     manifest["box_selection"] = {"image": "tile_mix(11, 128, 128)", "input_sha256": sha(sel_img)}
     o7, o6 = ref.tables()
     np.savez(os.path.join(HERE, "endpoint_tables.npz"), opt7=o7, opt6=o6)
+    make_stats(ref, manifest)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
 
