@@ -766,6 +766,18 @@ static void pick_neighbor(const mode_ctx *m, const float *p1, const float *p2,
 }
 
 /* OptimizeEndpointsForCluster (CP:538-630). Indices are in point order. */
+/* Diagnostic trace of one block's cluster fits (bc7o_trace_block only):
+ * where the fit being computed records its setup error (the QuantizedError
+ * the annealing starts from) and, for the rotation modes, its alpha error.
+ * Set only while bc7o_trace_block runs, on its own thread. */
+typedef struct {
+  double init, aerr;
+  int annealed; /* reached the QuantizedError path (not a single-colour shortcut) */
+} fit_note;
+static __thread fit_note *g_note;
+static __thread bc7o_fit_trace *g_trace;
+static __thread int g_ntrace, g_trace_cap;
+
 static float optimize_endpoints(const mode_ctx *m, const cluster *c, float *p1,
                                 float *p2, uint8_t *best_idx,
                                 uint8_t *best_pbit) {
@@ -775,6 +787,10 @@ static float optimize_endpoints(const mode_ctx *m, const cluster *c, float *p1,
   metric_of(m, metric);
   float cur_err = quantized_error(c, p1, p2, nb, qm, metric,
                                   pbit_combo(m, *best_pbit), best_idx);
+  if (g_note) {
+    g_note->init = cur_err;
+    g_note->annealed = 1;
+  }
   int cur_pbit = *best_pbit;
   float best_err = cur_err;
   uint32_t q1, q2;
@@ -1073,6 +1089,7 @@ static double fit_alpha(const mode_ctx *m, const cluster *c, float *p1,
   }
   p1[3] = a1;
   p2[3] = a2;
+  if (g_note) g_note->aerr = aerr;
   return rgb_err + aerr;
 }
 
@@ -1104,6 +1121,72 @@ static void init_ctx(mode_ctx *m, int mode, const block_ctx *b) {
   m->idx_mode = 0;
   m->exp_mode = (int)b->s->exp_mode;
   m->lcg = b->lcg;
+}
+
+/* The GPU pipeline's error lower bound for a fit of n texels (qe_lower_bound
+ * in fastc_gb300/csrc/bc7_intqe.cuh), in the same float steps: the scatter
+ * left after the best line, from an upper bound on the largest eigenvalue,
+ * less the palette's rounding slack. */
+static float fit_lower_bound(const uint32_t *px, int n) {
+  int sm[4] = {0, 0, 0, 0}, q[10] = {0};
+  for (int k = 0; k < n; k++) {
+    int v[4];
+    for (int c = 0; c < 4; c++) {
+      v[c] = (int)((px[k] >> (8 * c)) & 0xFF);
+      sm[c] += v[c];
+    }
+    int j = 0;
+    for (int a = 0; a < 4; a++)
+      for (int b = a; b < 4; b++) q[j++] += v[a] * v[b];
+  }
+  float A[4][4];
+  int tr = 0, j = 0;
+  for (int a = 0; a < 4; a++)
+    for (int b = a; b < 4; b++) {
+      const int v = n * q[j++] - sm[a] * sm[b];
+      if (a == b) tr += v;
+      A[a][b] = A[b][a] = (float)v;
+    }
+  if (tr <= 0) return 0.0f;
+  const float inv = 1.0f / (float)tr;
+  for (int a = 0; a < 4; a++)
+    for (int b = 0; b < 4; b++) A[a][b] *= inv;
+  float f = 0.0f;
+  for (int a = 0; a < 4; a++)
+    for (int b = a; b < 4; b++) {
+      const float v = A[a][0] * A[0][b] + A[a][1] * A[1][b] + A[a][2] * A[2][b] + A[a][3] * A[3][b];
+      f += (a == b ? 1.0f : 2.0f) * v * v;
+    }
+  const float lam = sqrtf(sqrtf(f));
+  float one = 1.0f - lam - 1e-5f;
+  if (one < 0.0f) one = 0.0f;
+  const float R = one * ((float)tr / (float)n);
+  const float fn = (float)n;
+  if (R < fn) return 0.0f;
+  const float lb = R - 2.0f * sqrtf(fn * R) - 1e-3f * R;
+  return lb > 0.0f ? lb : 0.0f;
+}
+
+/* Records one fit of the traced block. For a fit that took FasTC's
+ * single-colour shortcut the setup error and bound are its error. */
+static void trace_fit(const mode_ctx *m, const cluster *c, int slot, int subset, int rot_im,
+                      const fit_note *note, double final_err) {
+  g_note = NULL;
+  if (g_ntrace >= g_trace_cap) return;
+  bc7o_fit_trace *t = &g_trace[g_ntrace++];
+  t->mode = m->mode;
+  t->slot = slot;
+  t->subset = subset;
+  t->rot_im = rot_im;
+  t->n = c->n;
+  t->annealed = note->annealed;
+  t->final_err = final_err;
+  if (note->annealed) {
+    t->init_err = note->init + note->aerr;
+    t->lower_bound = (m->metric ? 0.0 : (double)fit_lower_bound(c->px, c->n)) + note->aerr;
+  } else {
+    t->init_err = t->lower_bound = final_err;
+  }
 }
 
 /* CompressionMode::Compress (CP:1300-1371). `slot` is the position of the
@@ -1142,7 +1225,10 @@ static double compress_mode(int mode, int shape, int slot,
             m.lcg = &fit_lcg;
           }
           float v1[4], v2[4];
+          fit_note note = {0.0, 0.0, 0};
+          if (g_trace) g_note = &note;
           const double e = fit_alpha(&m, &c, v1, v2, idx, aidx);
+          if (g_trace) trace_fit(&m, &c, slot, ci, (rot << 1) | im, &note, e);
           if (e < best) {
             best = e;
             memcpy(pr->idx[ci], idx, 16);
@@ -1162,7 +1248,11 @@ static double compress_mode(int mode, int shape, int slot,
                                 (uint32_t)((mode << 8) | (slot << 7) | (ci << 4)));
         m.lcg = &fit_lcg;
       }
-      total += fit_rgb(&m, &c, pr->p1[ci], pr->p2[ci], idx, &pr->pbit[ci]);
+      fit_note note = {0.0, 0.0, 0};
+      if (g_trace) g_note = &note;
+      const double e = fit_rgb(&m, &c, pr->p1[ci], pr->p2[ci], idx, &pr->pbit[ci]);
+      if (g_trace) trace_fit(&m, &c, slot, ci, -1, &note, e);
+      total += e;
       int k = 0;
       for (int i = 0; i < 16; i++)
         if (subset_of(i, shape, nsub) == ci) pr->idx[ci][i] = idx[k++];
@@ -1443,6 +1533,18 @@ void bc7o_compress_block(const uint32_t px[16], const bc7o_settings *s,
 
   block_ctx b = {s, bx, by, lcg};
   compress_clusters(px, &sel, modes, &b, out);
+}
+
+int bc7o_trace_block(const uint32_t px[16], const bc7o_settings *s, uint32_t bx,
+                     uint32_t by, uint32_t *wm, uint32_t *lcg, uint8_t out[16],
+                     bc7o_fit_trace *fits, int cap) {
+  g_trace = fits;
+  g_trace_cap = cap;
+  g_ntrace = 0;
+  bc7o_compress_block(px, s, bx, by, wm, lcg, out);
+  g_trace = NULL;
+  g_note = NULL;
+  return g_ntrace;
 }
 
 /* ------------------------------------------------------------------------ */

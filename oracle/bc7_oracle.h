@@ -66,6 +66,24 @@ void bc7o_compress_block(const uint32_t px[16], const bc7o_settings *s,
                          uint32_t bx, uint32_t by, uint32_t *wm, uint32_t *lcg,
                          uint8_t out[16]);
 
+/* One cluster fit of a traced block, in CompressClusters' order. */
+typedef struct {
+  int32_t mode, slot, subset;
+  int32_t rot_im;      /* rotation << 1 | index mode (modes 4, 5), else -1 */
+  int32_t n, annealed; /* point count; 1 when the fit took the QuantizedError
+                          path (not FasTC's single-colour shortcut) */
+  double init_err;     /* its error before the annealing (alpha error included) */
+  double final_err;    /* CompressCluster's return value */
+  double lower_bound;  /* the GPU pipeline's bound (its error when not annealed) */
+} bc7o_fit_trace;
+
+/* bc7o_compress_block, also listing the block's cluster fits (at most cap;
+ * returns how many were recorded). Diagnostic: checks the pipeline's
+ * pruning rule against the whole algorithm. */
+int bc7o_trace_block(const uint32_t px[16], const bc7o_settings *s, uint32_t bx,
+                     uint32_t by, uint32_t *wm, uint32_t *lcg, uint8_t out[16],
+                     bc7o_fit_trace *fits, int cap);
+
 /* What CompressWithStats logs for one block (Compressor.cpp:1938-2183):
  * the path (0 single colour, 1 transparent, 2 an exact shape, 3 searched),
  * the packed mode, each mode's error estimate and logged error (-1 when

@@ -43,6 +43,13 @@ class BlockStats(C.Structure):
                 ("two_shape", C.c_double * 64), ("three_shape", C.c_double * 64)]
 
 
+class FitTrace(C.Structure):
+    """bc7o_fit_trace: one cluster fit of a traced block."""
+    _fields_ = [("mode", C.c_int32), ("slot", C.c_int32), ("subset", C.c_int32),
+                ("rot_im", C.c_int32), ("n", C.c_int32), ("annealed", C.c_int32),
+                ("init_err", C.c_double), ("final_err", C.c_double), ("lower_bound", C.c_double)]
+
+
 _MODE_NAMES = ["Zero", "One", "Two", "Three", "Four", "Five", "Six", "Seven"]
 
 
@@ -109,10 +116,37 @@ class Port:
         lib.bc7o_fit_seed.restype = C.c_uint32
         lib.bc7o_expf.argtypes = [C.c_float]
         lib.bc7o_expf.restype = C.c_float
+        lib.bc7o_trace_block.argtypes = [_u32p, C.POINTER(Settings), C.c_uint32, C.c_uint32,
+                                          _u32p, _u32p, _u8p, C.POINTER(FitTrace), C.c_int]
+        lib.bc7o_trace_block.restype = C.c_int
         lib.bc7o_compress_block_stats.argtypes = [_u32p, C.POINTER(Settings), C.c_uint32,
                                                   C.c_uint32, _u32p, _u32p, _u8p,
                                                   C.POINTER(BlockStats)]
         self.lib = lib
+
+    def trace(self, img: np.ndarray, steps=0, modes=0xFF, metric=0, seed=0):
+        """Every block's cluster fits (per-fit RNG), in raster block order:
+        (blocks, [list of FitTrace per block])."""
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape[:2]
+        out = np.zeros(w * h, dtype=np.uint8)
+        s = self.settings(steps, modes, metric, RNG_PER_FIT, seed, EXP_PORTABLE)
+        st = np.zeros(2, dtype=np.uint32)
+        fits = (FitTrace * 64)()
+        per_block = []
+        bw = w // 4
+        for by in range(h // 4):
+            for bx in range(bw):
+                px = np.ascontiguousarray(
+                    img[4 * by:4 * by + 4, 4 * bx:4 * bx + 4].reshape(16, 4)).view(np.uint32).reshape(16)
+                dst = np.zeros(16, dtype=np.uint8)
+                n = self.lib.bc7o_trace_block(_ptr(px, _u32p), C.byref(s), bx, by,
+                                              _ptr(st[1:2], _u32p), _ptr(st[0:1], _u32p), _ptr(dst),
+                                              fits, 64)
+                i = by * bw + bx
+                out[16 * i:16 * i + 16] = dst
+                per_block.append([FitTrace.from_buffer_copy(fits[k]) for k in range(n)])
+        return out, per_block
 
     def compress_stats(self, img: np.ndarray, steps=0, modes=0xFF, metric=0,
                        rng_mode=RNG_PER_FIT, seed=0, exp_mode=EXP_PORTABLE, state=None):
