@@ -471,8 +471,9 @@ def main():
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": (tpb * total_blocks) if tpb else None,
                      "note": "issue-bound integer/FP32 search: the annealing and select kernels keep "
-                             "the ALU pipe 62-65 % busy while HBM traffic stays under 1 % of peak; "
-                             "traffic counts the stages' fit state exchanged through HBM"},
+                             "the ALU pipe 60-69 % busy and the setup kernels are latency-bound, "
+                             "while HBM traffic stays under 1 % of peak; traffic counts the stages' "
+                             "fit state exchanged through HBM and the setup kernels' spills"},
         "clocks": clocks.summary(),
     }
     if ipb:
