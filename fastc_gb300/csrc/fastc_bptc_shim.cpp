@@ -65,9 +65,16 @@ void Compress(const FasTC::CompressionJob &cj, CompressionSettings settings) {
   if (st != FASTC_BC7_OK) Die("BPTCC::Compress", st);
 }
 
-// BPTCCompressor.h:173. The per-block statistics log selects shapes
-// differently from Compress (Compressor.cpp:1862-2183) and is not provided.
-void CompressWithStats(const FasTC::CompressionJob &, std::ostream *, CompressionSettings) {
+// BPTCCompressor.h:173. Without a log stream FasTC encodes exactly as
+// Compress does, block for block (Compressor.cpp:1591-1596); with one it
+// runs a logging encoder that selects shapes differently
+// (Compressor.cpp:1862-2183), which is not provided.
+void CompressWithStats(const FasTC::CompressionJob &cj, std::ostream *logStream,
+                       CompressionSettings settings) {
+  if (!logStream) {
+    Compress(cj, settings);
+    return;
+  }
   Die("BPTCC::CompressWithStats", FASTC_BC7_ERR_UNSUPPORTED);
 }
 
