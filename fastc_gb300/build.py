@@ -25,7 +25,17 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
           "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
-SOURCES = ["bc7_kernels.cu", "bc7_pipeline.cu", "bc7_api.cu", "bc7_server.cu", "bc7_static.cu"]
+# (source, object name, extra flags). bc7_kernels.cu is compiled once per warp
+# count of the warp-per-block encoder, one encode_kernel instantiation each,
+# so that the four long compiles run in parallel.
+SOURCES = [("bc7_kernels.cu", "bc7_kernels", []),
+           ("bc7_kernels.cu", "bc7_wpb_w1", ["-DFASTC_WPB_WARPS=1"]),
+           ("bc7_kernels.cu", "bc7_wpb_w2", ["-DFASTC_WPB_WARPS=2"]),
+           ("bc7_kernels.cu", "bc7_wpb_w8", ["-DFASTC_WPB_WARPS=8"]),
+           ("bc7_pipeline.cu", "bc7_pipeline", []),
+           ("bc7_api.cu", "bc7_api", []),
+           ("bc7_server.cu", "bc7_server", []),
+           ("bc7_static.cu", "bc7_static", [])]
 
 
 def nvcc() -> str:
@@ -35,9 +45,10 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build fastc_gb300")
 
 
-def _compile(src: str, extra) -> str:
-    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+def _compile(item, extra) -> str:
+    src, name, flags = item
+    obj = os.path.join(BUILD, name + ".o")
+    cmd = [nvcc(), *ARCH, *COMMON, *flags, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

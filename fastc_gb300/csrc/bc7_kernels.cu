@@ -15,6 +15,12 @@
 //                        shapes two per lane, runs one cluster fit
 //                        (mode x subset x rotation x index mode) per lane,
 //                        then lane 0 picks the winner and packs 128 bits.
+//
+// The file is compiled once per warp count of the encoder
+// (FASTC_WPB_WARPS = 1, 2, 4 or 8), each object holding one instantiation
+// of encode_kernel so that the four compile in parallel; the object built
+// with FASTC_WPB_WARPS == 4 (the default) also holds the rest of the file.
+// The tables below have internal linkage, one copy per object.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -27,17 +33,41 @@
 #include "bc7_block.cuh"
 #include "bc7_pipeline.cuh"
 
+#ifndef FASTC_WPB_WARPS
+#define FASTC_WPB_WARPS 4
+#endif
+#define FASTC_WPB_MAIN (FASTC_WPB_WARPS == 4)
+#define FASTC_CAT2(a, b) a##b
+#define FASTC_CAT(a, b) FASTC_CAT2(a, b)
+
 namespace fastc {
 
-__constant__ uint32_t c_part2[64] = {FASTC_PART2_WORDS};
-__constant__ uint32_t c_part3[64] = {FASTC_PART3_WORDS};
-__constant__ uint8_t c_anchor2[64] = {FASTC_ANCHOR2_BYTES};
-__constant__ uint8_t c_anchor3[64] = {FASTC_ANCHOR3_BYTES};
-__constant__ uint32_t c_watermark[9] = {FASTC_WATERMARK_WORDS};
+static __constant__ uint32_t c_part2[64] = {FASTC_PART2_WORDS};
+static __constant__ uint32_t c_part3[64] = {FASTC_PART3_WORDS};
+static __constant__ uint8_t c_anchor2[64] = {FASTC_ANCHOR2_BYTES};
+static __constant__ uint8_t c_anchor3[64] = {FASTC_ANCHOR3_BYTES};
+static __constant__ uint32_t c_watermark[9] = {FASTC_WATERMARK_WORDS};
 // Single-colour mode-5 endpoints: byte 0 = 7-bit first, byte 1 = 7-bit second.
-__constant__ uint32_t c_opt7[256];
+static __constant__ uint32_t c_opt7[256];
 // Mode-4 constant-alpha endpoints: byte 0 = a1, byte 1 = a2.
-__constant__ uint32_t c_opt6[256];
+static __constant__ uint32_t c_opt6[256];
+
+// The per-warp-count objects: launch, occupancy and table upload of their
+// encode_kernel instantiation.
+int wpb_launch_w1(const JobDev *, int, uint64_t, const EncodeScratch &, int, cudaStream_t);
+int wpb_launch_w2(const JobDev *, int, uint64_t, const EncodeScratch &, int, cudaStream_t);
+int wpb_launch_w4(const JobDev *, int, uint64_t, const EncodeScratch &, int, cudaStream_t);
+int wpb_launch_w8(const JobDev *, int, uint64_t, const EncodeScratch &, int, cudaStream_t);
+int wpb_occupancy_w1();
+int wpb_occupancy_w2();
+int wpb_occupancy_w4();
+int wpb_occupancy_w8();
+void wpb_upload_w1(const uint32_t *opt7, const uint32_t *opt6);
+void wpb_upload_w2(const uint32_t *opt7, const uint32_t *opt6);
+void wpb_upload_w4(const uint32_t *opt7, const uint32_t *opt6);
+void wpb_upload_w8(const uint32_t *opt7, const uint32_t *opt6);
+
+#if FASTC_WPB_MAIN
 
 
 // ---------------------------------------------------------------------------
@@ -115,8 +145,10 @@ void upload_tables(int device) {
   if (device < 0 || device >= 64 || done[device]) return;
   uint32_t opt7[256], opt6[256];
   build_endpoint_tables(opt7, opt6);
-  cudaMemcpyToSymbol(c_opt7, opt7, sizeof(opt7));
-  cudaMemcpyToSymbol(c_opt6, opt6, sizeof(opt6));
+  wpb_upload_w1(opt7, opt6);
+  wpb_upload_w2(opt7, opt6);
+  wpb_upload_w4(opt7, opt6);
+  wpb_upload_w8(opt7, opt6);
   upload_pipeline_tables(device, opt7, opt6);
   done[device] = true;
 }
@@ -126,6 +158,7 @@ int device_sm_count(int device) {
   cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device);
   return n > 0 ? n : 1;
 }
+#endif  // FASTC_WPB_MAIN
 
 // ---------------------------------------------------------------------------
 // Job lookup and block loads
@@ -166,6 +199,7 @@ __device__ __forceinline__ void store_block(const JobDev &jb, uint32_t lin, cons
   }
 }
 
+#if FASTC_WPB_MAIN
 // ---------------------------------------------------------------------------
 // 1+2. Single-colour watermark ranks
 // ---------------------------------------------------------------------------
@@ -251,6 +285,8 @@ __global__ void __launch_bounds__(1024) scan_kernel(uint32_t *chunk, uint32_t nc
   }
   if (threadIdx.x == 0) *singles = s_carry;
 }
+
+#endif  // FASTC_WPB_MAIN
 
 // ---------------------------------------------------------------------------
 // 3. Encoder
@@ -388,16 +424,33 @@ __global__ void __launch_bounds__(kWarps * 32) encode_kernel(
   }
 }
 
-int encode_ctas_per_sm(int warps) {
+int FASTC_CAT(wpb_launch_w, FASTC_WPB_WARPS)(const JobDev *jobs_dev, int njobs, uint64_t total,
+                                              const EncodeScratch &sc, int ctas, cudaStream_t st) {
+  encode_kernel<FASTC_WPB_WARPS><<<ctas, FASTC_WPB_WARPS * 32, 0, st>>>(
+      jobs_dev, njobs, total, sc.rank_local, sc.chunk_prefix, sc.counter, sc.status);
+  return (int)cudaPeekAtLastError();
+}
+
+int FASTC_CAT(wpb_occupancy_w, FASTC_WPB_WARPS)() {
   int n = 0;
-  cudaError_t e;
-  switch (warps) {
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, encode_kernel<1>, 32, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, encode_kernel<2>, 64, 0); break;
-    case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, encode_kernel<8>, 256, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, encode_kernel<4>, 128, 0); break;
-  }
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &n, encode_kernel<FASTC_WPB_WARPS>, FASTC_WPB_WARPS * 32, 0);
   return (e == cudaSuccess && n > 0) ? n : 1;
+}
+
+void FASTC_CAT(wpb_upload_w, FASTC_WPB_WARPS)(const uint32_t *opt7, const uint32_t *opt6) {
+  cudaMemcpyToSymbol(c_opt7, opt7, 256 * sizeof(uint32_t));
+  cudaMemcpyToSymbol(c_opt6, opt6, 256 * sizeof(uint32_t));
+}
+
+#if FASTC_WPB_MAIN
+int encode_ctas_per_sm(int warps) {
+  switch (warps) {
+    case 1: return wpb_occupancy_w1();
+    case 2: return wpb_occupancy_w2();
+    case 8: return wpb_occupancy_w8();
+    default: return wpb_occupancy_w4();
+  }
 }
 
 int launch_rank_prepass(const JobDev *jobs_dev, int njobs, uint64_t total,
@@ -422,24 +475,11 @@ int launch_encode(const JobDev *jobs_dev, int njobs, uint64_t total, const Encod
   }
   const int ctas = shape.ctas > 0 ? shape.ctas : 1;
   switch (shape.warps_per_cta) {
-    case 1:
-      encode_kernel<1><<<ctas, 32, 0, st>>>(jobs_dev, njobs, total, sc.rank_local,
-                                            sc.chunk_prefix, sc.counter, sc.status);
-      break;
-    case 2:
-      encode_kernel<2><<<ctas, 64, 0, st>>>(jobs_dev, njobs, total, sc.rank_local,
-                                            sc.chunk_prefix, sc.counter, sc.status);
-      break;
-    case 8:
-      encode_kernel<8><<<ctas, 256, 0, st>>>(jobs_dev, njobs, total, sc.rank_local,
-                                             sc.chunk_prefix, sc.counter, sc.status);
-      break;
-    default:
-      encode_kernel<4><<<ctas, 128, 0, st>>>(jobs_dev, njobs, total, sc.rank_local,
-                                             sc.chunk_prefix, sc.counter, sc.status);
-      break;
+    case 1: return wpb_launch_w1(jobs_dev, njobs, total, sc, ctas, st);
+    case 2: return wpb_launch_w2(jobs_dev, njobs, total, sc, ctas, st);
+    case 8: return wpb_launch_w8(jobs_dev, njobs, total, sc, ctas, st);
+    default: return wpb_launch_w4(jobs_dev, njobs, total, sc, ctas, st);
   }
-  return (int)cudaPeekAtLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -587,5 +627,6 @@ int launch_decode(const uint8_t *blocks, uint8_t *rgba, uint32_t width, uint32_t
       blocks, rgba, width, height, spec);
   return (int)cudaPeekAtLastError();
 }
+#endif  // FASTC_WPB_MAIN
 
 }  // namespace fastc
