@@ -41,14 +41,29 @@ constexpr size_t kRankBytes =
 
 // Nothing here has to start at zero: the rank pre-pass writes every chunk
 // count and block rank and resets the work counter and status before the
-// encoder reads them, and the job table is copied in by each call.
+// encoder reads them, and the job table is written by each call.
 __device__ __align__(256) uint8_t g_noalloc_scratch[kJobBytes + kRankBytes];
+
+// The job table travels to the device inside kernel parameters, in pieces of
+// kJobsPerCopy entries (2,304 bytes of parameters each): the launch keeps
+// its own copy of the entries, so nothing refers to the caller's host stack
+// once the call has returned.
+constexpr uint32_t kJobsPerCopy = 32;
+struct JobPiece {
+  JobDev j[kJobsPerCopy];
+};
+
+__global__ void put_jobs_kernel(JobPiece piece, uint32_t count, JobDev *dst) {
+  if (threadIdx.x < count) dst[threadIdx.x] = piece.j[threadIdx.x];
+}
 
 constexpr int kMaxDevices = 64;
 void *g_base[kMaxDevices];  // address of the array on each device (guarded by g_mu)
 
 // One-time set-up per device, with that device current: the array's address
 // and the encoder's constant tables (this synchronises the device once).
+// The address is the one in the runtime's primary context of the device,
+// the context every runtime-API caller shares.
 fastc_bc7_status device_base(int dev, void **out) {
   std::lock_guard<std::mutex> lk(fastc::host::g_mu);
   if (dev < 0 || dev >= kMaxDevices) return FASTC_BC7_ERR_NO_DEVICE;
@@ -81,6 +96,7 @@ fastc_bc7_status fastc_bc7_compress_device_noalloc(const fastc_bc7_job *jobs, ui
   fastc_bc7_settings dflt;
   fastc_bc7_settings_default(&dflt);
   JobDev tab[kMaxJobs];  // on the stack: the host side allocates nothing either
+  static_assert(kMaxJobs % kJobsPerCopy == 0, "job table pieces");
   uint64_t total = 0;
   for (uint32_t i = 0; i < n; i++) {
     const fastc_bc7_settings &st = settings ? (per_job_settings ? settings[i] : settings[0]) : dflt;
@@ -115,7 +131,13 @@ fastc_bc7_status fastc_bc7_compress_device_noalloc(const fastc_bc7_job *jobs, ui
   }
   cudaStream_t cs = static_cast<cudaStream_t>(stream);
   uint8_t *p = static_cast<uint8_t *>(base);
-  CK(cudaMemcpyAsync(p, tab, n * sizeof(JobDev), cudaMemcpyHostToDevice, cs));
+  for (uint32_t k = 0; k < n; k += kJobsPerCopy) {
+    JobPiece piece{};
+    const uint32_t cnt = n - k < kJobsPerCopy ? n - k : kJobsPerCopy;
+    for (uint32_t i = 0; i < cnt; i++) piece.j[i] = tab[k + i];
+    put_jobs_kernel<<<1, kJobsPerCopy, 0, cs>>>(piece, cnt, reinterpret_cast<JobDev *>(p) + k);
+    CK(cudaPeekAtLastError());
+  }
   const fastc::EncodeScratch sc = carve_scratch(p + kJobBytes, total);
   const int le = fastc::launch_encode(reinterpret_cast<const JobDev *>(p), (int)n, total, sc,
                                       shape, cs);

@@ -65,10 +65,14 @@ void Compress(const FasTC::CompressionJob &cj, CompressionSettings settings) {
   if (st != FASTC_BC7_OK) Die("BPTCC::Compress", st);
 }
 
-// BPTCCompressor.h:173. Without a log stream FasTC encodes exactly as
-// Compress does, block for block (Compressor.cpp:1591-1596); with one it
-// runs a logging encoder that selects shapes differently
-// (Compressor.cpp:1862-2183), which is not provided.
+// BPTCCompressor.h:173. Without a log stream FasTC encodes each block as
+// Compress does (Compressor.cpp:1591-1596); with one it runs a logging
+// encoder that selects shapes differently (Compressor.cpp:1862-2183), which
+// is not provided. Its block loop runs to y <= YEnd with no clamp to
+// Height - 4 (Compressor.cpp:1583-1584, unlike Compress at :1478), so for a
+// job whose YEnd equals Height FasTC reads and writes one block row past
+// the buffers; here the range is clamped as Compress clamps it, and the
+// blocks written are those of Compress.
 void CompressWithStats(const FasTC::CompressionJob &cj, std::ostream *logStream,
                        CompressionSettings settings) {
   if (!logStream) {

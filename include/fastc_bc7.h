@@ -179,7 +179,11 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_decompress_device(const uint8_t *blocks
  *   - every call reuses the one array, so calls that overlap on the device
  *     (different streams, or threads without ordering) race and corrupt
  *     each other's output; calls in order on one stream are safe;
- *   - it always runs the warp-per-block engine. */
+ *   - the array is addressed in the runtime's primary context of the
+ *     current device; a caller that makes its own driver-API context current
+ *     instead (cuCtxCreate + cuCtxSetCurrent) must not use this entry point;
+ *   - it always runs the warp-per-block engine, whose bytes equal the
+ *     pipeline engine's (both are checked against the oracle bit for bit). */
 #define FASTC_BC7_NOALLOC_MAX_BLOCKS (1u << 20)
 #define FASTC_BC7_NOALLOC_MAX_JOBS 256u
 FASTC_BC7_API fastc_bc7_status fastc_bc7_compress_device_noalloc(const fastc_bc7_job *jobs,
