@@ -7,6 +7,12 @@ encoded at 50 annealing steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
     python bench.py --serve [--serve-rates 20,60,120] [--serve-seconds 4]
+    python bench.py --profile-case [--case-kind tile_mix|radial|gradient]
+        [--case-size 4096] [--case-steps 50] [--case-repeat 1]
+
+--profile-case encodes one seeded texture through the device-memory C ABI
+`--case-repeat` times and prints each encode's wall time: the small,
+self-contained command that the ncu captures under profiles/ run.
 
 A step is one pass of the encoder over the whole texture set:
   * value       -- batched: one graph launch of the captured plan over all
@@ -304,6 +310,39 @@ def serve_bench(args):
                       "sweep": results}))
 
 
+def profile_case(args):
+    """One seeded texture encoded `case_repeat` times (for ncu captures)."""
+    n = args.case_size
+    from fastc_gb300 import synth
+
+    if args.case_kind == "tile_mix":
+        img = synth.tile_mix(21, n, n)
+    elif args.case_kind == "radial":
+        img = synth.tile_mix_radial_alpha(5, n, n, 0, 0, n, n)
+    else:
+        img = synth.gradient_noise_alpha_ramp(1, n, n)
+    import torch
+
+    from fastc_gb300 import CompressionJob, CompressionSettings, compress, set_launch_shape
+
+    from fastc_gb300 import set_engine
+
+    set_engine(args.case_engine)
+    set_launch_shape(args.case_warps, 0)
+    din = torch.from_numpy(img).cuda()
+    dout = torch.zeros(n * n, dtype=torch.uint8, device="cuda")
+    s = CompressionSettings(num_simulated_annealing_steps=args.case_steps, seed=1)
+    job = CompressionJob(din, dout, n, n)
+    for _ in range(args.case_repeat):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        compress(job, s)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        print(f"{args.case_kind} {n}x{n} q{args.case_steps}: {dt * 1e3:.2f} ms, "
+              f"{n * n / dt / 1e6:.2f} MPix/s")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -315,7 +354,20 @@ def main():
     ap.add_argument("--serve", action="store_true", help="run the serving sweep instead")
     ap.add_argument("--serve-rates", default="20,60,120")
     ap.add_argument("--serve-seconds", type=float, default=4.0)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="encode one texture --case-repeat times (for ncu captures)")
+    ap.add_argument("--case-kind", default="tile_mix", choices=["tile_mix", "radial", "gradient"])
+    ap.add_argument("--case-size", type=int, default=4096)
+    ap.add_argument("--case-steps", type=int, default=50)
+    ap.add_argument("--case-repeat", type=int, default=1)
+    ap.add_argument("--case-engine", type=int, default=0,
+                    help="0: pipeline engine, 1: warp-per-block engine")
+    ap.add_argument("--case-warps", type=int, default=0,
+                    help="warps per CTA of the warp-per-block engine (0: keep)")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args)
+        return
     if args.impl == "reference":
         reference_impl(args)
         return

@@ -51,6 +51,18 @@ QUALITY = {
 }
 
 
+# The full-size configurations, FasTC at three pinned seeds each: PSNR and
+# per-block SSE (premultiplied metric, float32, compressed). The 2048x2048
+# tile mix at q50 is the single-launch configuration; the q100 radial-alpha
+# case is the 8192x512 stripe of rows 3840..4351 (through the centre band
+# of the radial gradient) of the 8192x8192 image, since FasTC takes about
+# 20 minutes per seed on that stripe alone.
+FULL_SIZE = {
+    "c2_tile2048_q50": ("tile_mix(2, 2048, 2048)", 50, [11, 22, 33]),
+    "c5_stripe8192x512_q100": ("tile_mix_radial_alpha(5, 8192, 512, 0, 3840)", 100, [11, 22, 33]),
+}
+
+
 def make(expr: str) -> np.ndarray:
     return eval("synth." + expr, {"synth": synth})
 
@@ -103,19 +115,53 @@ def make_stats(ref, manifest):
         print(name, len(blocks) // 16, "blocks,", len(log), "log bytes")
 
 
+def _full_size_one(args):
+    """One (case, seed) of the full-size fixtures, in a worker process (the
+    reference's LCG seed is process-global, so each seed gets its own)."""
+    name, expr, steps, seed = args
+    ref, port = O.Reference(), O.Port()
+    img = make(expr)
+    blocks = ref.compress(img, steps=steps, seed=seed)
+    dec = ref.decompress(blocks, img.shape[1], img.shape[0])
+    return name, seed, port.psnr(img, dec), port.block_sse(img, dec).astype(np.float32)
+
+
+def make_full_size(manifest, workers):
+    import multiprocessing as mp
+
+    work = [(name, expr, steps, s) for name, (expr, steps, seeds) in FULL_SIZE.items() for s in seeds]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        res = pool.map(_full_size_one, work, chunksize=1)
+    manifest["full_size"] = {}
+    for name, (expr, steps, seeds) in FULL_SIZE.items():
+        rows = sorted((r for r in res if r[0] == name), key=lambda r: seeds.index(r[1]))
+        np.savez_compressed(os.path.join(HERE, name + "_sse.npz"),
+                            sse=np.stack([r[3] for r in rows]))
+        manifest["full_size"][name] = {"image": expr, "steps": steps, "lcg_seeds": seeds,
+                                       "input_sha256": sha(make(expr)),
+                                       "psnr": [r[2] for r in rows]}
+        print(name, [r[2] for r in rows])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=O.DEFAULT_REFERENCE)
     ap.add_argument("--stats-only", action="store_true",
                     help="only (re)write the CompressWithStats fixtures")
+    ap.add_argument("--full-size-only", action="store_true",
+                    help="only (re)write the full-size PSNR / per-block SSE fixtures")
+    ap.add_argument("--workers", type=int, default=6)
     args = ap.parse_args()
     if not O.build_ref(args.reference):
         sys.exit("FasTC checkout not found; cannot regenerate fixtures")
     ref = O.Reference()
-    if args.stats_only:
+    if args.stats_only or args.full_size_only:
         with open(os.path.join(HERE, "manifest.json")) as f:
             manifest = json.load(f)
-        make_stats(ref, manifest)
+        if args.stats_only:
+            make_stats(ref, manifest)
+        else:
+            make_full_size(manifest, args.workers)
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
             json.dump(manifest, f, indent=1, sort_keys=True)
         return
@@ -150,6 +196,7 @@ def main():
     o7, o6 = ref.tables()
     np.savez(os.path.join(HERE, "endpoint_tables.npz"), opt7=o7, opt6=o6)
     make_stats(ref, manifest)
+    make_full_size(manifest, args.workers)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
 
