@@ -114,6 +114,10 @@ SIGNATURES = {
     "fastc_bc7_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fastc_bc7_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
     "fastc_bc7_server_destroy": (C.c_int, [C.c_void_p]),
+    "fastc_bc7_psnr": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                 C.POINTER(C.c_double), C.c_void_p]),
+    "fastc_bc7_block_error_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                               C.c_void_p, C.c_void_p, C.c_void_p]),
     "fastc_bc7_set_engine": (C.c_int, [C.c_int]),
     "fastc_bc7_get_engine": (C.c_int, []),
     "fastc_bc7_set_launch_shape": (C.c_int, [C.c_int, C.c_int]),

@@ -255,6 +255,39 @@ def decompress(blocks, width: int, height: int, spec_semantics: bool = False, ou
     return out
 
 
+def psnr(blocks, rgba, width: int, height: int, block_sse: bool = False, stream=None):
+    """Image::ComputePSNR (Base/src/Image.cpp:206-255) of encoded `blocks`
+    against the original `rgba`, computed on the GPU: the PSNR in dB, or
+    (psnr, per-block SSE) with ``block_sse``. Host arrays go through
+    fastc_bc7_psnr; CUDA tensors through fastc_bc7_block_error_device on
+    `stream` (the result is read back, which synchronises that stream)."""
+    import math
+
+    lib = load()
+    nb = ((width + 3) // 4) * ((height + 3) // 4)
+    if _is_cuda(blocks):
+        import torch
+
+        sse = torch.empty(nb + 1, dtype=torch.float64, device=blocks.device)
+        check(lib.fastc_bc7_block_error_device(
+            C.c_void_p(blocks.data_ptr()), C.c_void_p(rgba.data_ptr()), width, height,
+            C.c_void_p(sse.data_ptr() + 8), C.c_void_p(sse.data_ptr()),
+            C.c_void_p(_stream_handle(stream))), "fastc_bc7_block_error_device")
+        host = sse.cpu().numpy()
+        total, per = float(host[0]), host[1:]
+        db = 10.0 * math.log10(3.0 * 255.0 * 255.0 / (total / (width * height))) if total > 0 else math.inf
+        return (db, per) if block_sse else db
+    blocks = np.ascontiguousarray(np.asarray(blocks, dtype=np.uint8))
+    rgba = np.ascontiguousarray(np.asarray(rgba, dtype=np.uint8))
+    if blocks.size < nb * 16 or rgba.size < width * height * 4:
+        raise BC7Error(_lib.ERR_INVALID_ARGUMENT, "psnr: buffers smaller than the image")
+    out = C.c_double()
+    per = np.zeros(nb, dtype=np.float64) if block_sse else None
+    check(lib.fastc_bc7_psnr(blocks.ctypes.data, rgba.ctypes.data, width, height, C.byref(out),
+                             per.ctypes.data if per is not None else None), "fastc_bc7_psnr")
+    return (out.value, per) if block_sse else out.value
+
+
 class Plan:
     """A fixed set of device jobs captured once into a CUDA graph; each
     :meth:`launch` re-encodes the whole set with one graph launch."""

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <utility>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -468,6 +469,43 @@ fastc_bc7_status fastc_bc7_decompress(const uint8_t *blocks, uint8_t *rgba, uint
   if (le) return fail_cuda((cudaError_t)le);
   CK(cudaMemcpyAsync(rgba, g_host.out.p, img, cudaMemcpyDeviceToHost, cs));
   CK(cudaStreamSynchronize(cs));
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_block_error_device(const uint8_t *blocks, const uint8_t *rgba,
+                                              uint32_t width, uint32_t height, double *block_sse,
+                                              double *sse_total, void *stream) {
+  if (!blocks || !rgba || !block_sse || width == 0 || height == 0)
+    return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  const int le = fastc::launch_block_error(blocks, rgba, width, height, block_sse, sse_total, stream);
+  if (le) return fail_cuda((cudaError_t)le);
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_psnr(const uint8_t *blocks, const uint8_t *rgba, uint32_t width,
+                                uint32_t height, double *psnr, double *block_sse) {
+  if (!blocks || !rgba || width == 0 || height == 0) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(g_mu);
+  fastc_bc7_status st = host_ctx_init();
+  if (st != FASTC_BC7_OK) return st;
+  const size_t nb = (size_t)((width + 3) / 4) * ((height + 3) / 4);
+  const size_t img = (size_t)width * height * 4;
+  CK(g_host.in.ensure(img + nb * 16));
+  CK(g_host.out.ensure((nb + 1) * sizeof(double)));
+  cudaStream_t cs = g_host.stream;
+  uint8_t *dimg = static_cast<uint8_t *>(g_host.in.p);
+  uint8_t *dblk = dimg + img;  // byte loads only, so no alignment is needed
+  double *dsse = static_cast<double *>(g_host.out.p);
+  CK(cudaMemcpyAsync(dimg, rgba, img, cudaMemcpyHostToDevice, cs));
+  CK(cudaMemcpyAsync(dblk, blocks, nb * 16, cudaMemcpyHostToDevice, cs));
+  const int le = fastc::launch_block_error(dblk, dimg, width, height, dsse + 1, dsse, cs);
+  if (le) return fail_cuda((cudaError_t)le);
+  double total = 0.0;
+  CK(cudaMemcpyAsync(&total, dsse, sizeof(double), cudaMemcpyDeviceToHost, cs));
+  if (block_sse)
+    CK(cudaMemcpyAsync(block_sse, dsse + 1, nb * sizeof(double), cudaMemcpyDeviceToHost, cs));
+  CK(cudaStreamSynchronize(cs));
+  if (psnr) *psnr = 10.0 * std::log10((3.0 * 255.0 * 255.0) / (total / ((double)width * height)));
   return FASTC_BC7_OK;
 }
 

@@ -353,7 +353,9 @@ __device__ inline void power_method(const float m[4][4], float *out) {
       nb[j] = s;
     }
     const float len = length4(nb);
-    if ((double)len < 1e-10) {
+    // (double)len < 1e-10: 1e-10f is the least float above 1e-10, so for a
+    // float the test is the same in single precision
+    if (len < 1e-10f) {
       if (bad) break;
       b[0] = b[1] = 1.0f;
       normalize4(b);
@@ -361,7 +363,9 @@ __device__ inline void power_method(const float m[4][4], float *out) {
       continue;
     }
     normalize4(nb);
-    if (fabs((double)__fsub_rn(1.0f, dot4(b, nb))) < 1e-8) fixed = true;
+    // fabs((double)x) < 1e-8 for a float x: 1e-8f is the greatest float
+    // below 1e-8, so the test is |x| <= 1e-8f
+    if (fabsf(__fsub_rn(1.0f, dot4(b, nb))) <= 1e-8f) fixed = true;
 #pragma unroll
     for (int k = 0; k < 4; k++) b[k] = nb[k];
   }
@@ -372,22 +376,26 @@ __device__ inline void power_method(const float m[4][4], float *out) {
 __device__ __forceinline__ uint32_t cl_packed(const Cluster &c, int k);
 
 // The unique points are kept packed (they are bytes) in the cluster's
-// scratch words instead of a float array.
+// scratch words instead of a float array, and found only as far as the
+// tests below read them: the collinearity test usually stops at the third
+// unique point, so the whole list is rarely needed. The list, where read,
+// is FasTC's (points in cluster order, first occurrences).
 __device__ inline void principal_axis(const Cluster &c, float *axis) {
-  // unique points, in order; slots past the unique count read (-1,-1,-1,-1)
   uint32_t *up = c.aux;
   const int us = c.aux_stride;
-  int nu = 0;
-  for (int i = 0; i < c.n; i++) {
-    const uint32_t q = cl_packed(c, i);
-    bool has = false;
-    for (int j = 0; j < nu; j++)
-      if (up[j * us] == q) has = true;
-    if (!has) {
-      up[nu * us] = q;
-      nu++;
+  int nu = 0, scan = 0;  // unique points found, next point to look at
+  auto find_unique = [&](int want) {
+    while (nu < want && scan < c.n) {
+      const uint32_t q = cl_packed(c, scan++);
+      bool has = false;
+      for (int j = 0; j < nu; j++) has = has || up[j * us] == q;
+      if (!has) {
+        up[nu * us] = q;
+        nu++;
+      }
     }
-  }
+  };
+  find_unique(2);
   if (nu == 1) {
     axis[0] = axis[1] = axis[2] = axis[3] = 0.0f;
     return;
@@ -399,13 +407,19 @@ __device__ inline void principal_axis(const Cluster &c, float *axis) {
   for (int k = 0; k < 4; k++) dir[k] = __fsub_rn(u1[k], u0[k]);
   normalize4(dir);
   bool collinear = true;
-  for (int i = 2; i < c.n; i++) {  // bounded by the point count, not nu
+  for (int i = 2; i < c.n; i++) {  // bounded by the point count; slots past the
+                                   // unique count read (-1,-1,-1,-1)
+    find_unique(i + 1);
     float ui[4] = {-1.0f, -1.0f, -1.0f, -1.0f};
     if (i < nu) unpack4(up[i * us], ui);
     float v[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) v[k] = __fsub_rn(ui[k], u0[k]);
-    if (fabs(fabs((double)dot4(v, dir)) - (double)length4(v)) > 1e-7) {
+    // fabs(fabs((double)a) - (double)b) > 1e-7 in single precision: b is 0
+    // (then a is 0 too) or the root of an integer >= 1; where |a - b| is
+    // below b / 2 the float difference is exact (Sterbenz), elsewhere it is
+    // at least 0.5 either way. 1e-7f is the least float above 1e-7.
+    if (fabsf(__fsub_rn(fabsf(dot4(v, dir)), length4(v))) >= 1e-7f) {
       collinear = false;
       break;
     }
@@ -415,18 +429,29 @@ __device__ inline void principal_axis(const Cluster &c, float *axis) {
     for (int k = 0; k < 4; k++) axis[k] = dir[k];
     return;
   }
+  // The ten sums of the covariance in one pass over the points; each sum
+  // adds the same products in the same order as one pass per entry.
+  float cs[10];
+#pragma unroll
+  for (int m = 0; m < 10; m++) cs[m] = 0.0f;
+  for (int t = 0; t < c.n; t++) {
+    float p[4], d[4];
+    cl_point(c, t, p);
+#pragma unroll
+    for (int k = 0; k < 4; k++) d[k] = __fsub_rn(p[k], c.avg[k]);
+    int m = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j <= i; j++, m++) cs[m] = __fadd_rn(cs[m], __fmul_rn(d[i], d[j]));
+  }
   float cov[4][4];
+  int m = 0;
 #pragma unroll
   for (int i = 0; i < 4; i++)
 #pragma unroll
-    for (int j = 0; j <= i; j++) {
-      float s = 0.0f;
-      for (int t = 0; t < c.n; t++) {
-        float p[4];
-        cl_point(c, t, p);
-        s = __fadd_rn(s, __fmul_rn(__fsub_rn(p[i], c.avg[i]), __fsub_rn(p[j], c.avg[j])));
-      }
-      cov[i][j] = __fdiv_rn(s, 3.0f);
+    for (int j = 0; j <= i; j++, m++) {
+      cov[i][j] = __fdiv_rn(cs[m], 3.0f);
       cov[j][i] = cov[i][j];
     }
   power_method(cov, axis);
@@ -1158,23 +1183,47 @@ __device__ inline void alpha_fit_t(const ModeCtx &m, const Cluster &c, uint32_t 
     const uint32_t a1b = quantize_channel((uint32_t)a1 & 0xFF, amask, -1);
     const uint32_t a2b = quantize_channel((uint32_t)a2 & 0xFF, amask, -1);
     aerr = 0.0;
-    for (int i = 0; i < 16; i++) {
-      const uint32_t val = (cl_pixel(c, i) >> (8 * ch)) & 0xFF;
-      float me = FLT_MAX;
-      uint32_t bb = 0;
+    if (wa == 1.0f) {
+      // Uniform weight: each texel's error is the square of an integer below
+      // 256, exact in float, and sixteen of them sum exactly in double, so
+      // the integer sum is the same number without double arithmetic.
+      uint32_t ie = 0;
+      for (int i = 0; i < 16; i++) {
+        const uint32_t val = (cl_pixel(c, i) >> (8 * ch)) & 0xFF;
+        uint32_t me = 0xFFFFFFFFu, bb = 0;
 #pragma unroll
-      for (int j = 0; j < nb; j++) {
-        const uint32_t w1 = weight1(abits, (uint32_t)j), w0 = 64u - w1;
-        const uint32_t ip = ((a1b * w0 + a2b * w1 + 32u) >> 6) & 0xFF;
-        float pe = __fmul_rn(wa, (float)(val > ip ? val - ip : ip - val));
-        pe = __fmul_rn(pe, pe);
-        if (pe < me) {
-          me = pe;
-          bb = (uint32_t)j;
+        for (int j = 0; j < nb; j++) {
+          const uint32_t w1 = weight1(abits, (uint32_t)j), w0 = 64u - w1;
+          const uint32_t ip = ((a1b * w0 + a2b * w1 + 32u) >> 6) & 0xFF;
+          const uint32_t d = val > ip ? val - ip : ip - val;
+          if (d * d < me) {
+            me = d * d;
+            bb = (uint32_t)j;
+          }
         }
+        ie += me;
+        set_nib(aidx, i, bb);
       }
-      aerr = aerr + (double)me;
-      set_nib(aidx, i, bb);
+      aerr = (double)ie;
+    } else {
+      for (int i = 0; i < 16; i++) {
+        const uint32_t val = (cl_pixel(c, i) >> (8 * ch)) & 0xFF;
+        float me = FLT_MAX;
+        uint32_t bb = 0;
+#pragma unroll
+        for (int j = 0; j < nb; j++) {
+          const uint32_t w1 = weight1(abits, (uint32_t)j), w0 = 64u - w1;
+          const uint32_t ip = ((a1b * w0 + a2b * w1 + 32u) >> 6) & 0xFF;
+          float pe = __fmul_rn(wa, (float)(val > ip ? val - ip : ip - val));
+          pe = __fmul_rn(pe, pe);
+          if (pe < me) {
+            me = pe;
+            bb = (uint32_t)j;
+          }
+        }
+        aerr = aerr + (double)me;
+        set_nib(aidx, i, bb);
+      }
     }
   }
   a1_out = a1;

@@ -504,18 +504,8 @@ __device__ __forceinline__ void weights_padded(int bits, uint32_t j, uint32_t &w
   w0 = 64u - w1;
 }
 
-__global__ void decode_kernel(const uint8_t *__restrict__ blocks, uint8_t *__restrict__ rgba,
-                              uint32_t width, uint32_t height, int spec) {
-  const uint32_t bw = (width + 3) / 4, bh = (height + 3) / 4;
-  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= (uint64_t)bw * bh) return;
-  const uint32_t bx = (uint32_t)(b % bw), by = (uint32_t)(b / bw);
-  uint32_t w[4];
-  const uint8_t *src = blocks + b * 16;
-  for (int i = 0; i < 4; i++)
-    w[i] = (uint32_t)src[4 * i] | ((uint32_t)src[4 * i + 1] << 8) |
-           ((uint32_t)src[4 * i + 2] << 16) | ((uint32_t)src[4 * i + 3] << 24);
-  uint32_t outpx[16];
+// The 16 texels (RGBA8, R in the low byte) of one 128-bit block.
+__device__ void decode_block(const uint32_t w[4], int spec, uint32_t outpx[16]) {
   int pos = 0, mode = 0;
   while (mode < 8 && !get_bits(w, pos, 1)) mode++;
   if (mode >= 8) {
@@ -606,6 +596,24 @@ __global__ void decode_kernel(const uint8_t *__restrict__ blocks, uint8_t *__res
       outpx[i] = p;
     }
   }
+}
+
+__device__ __forceinline__ void load_block_words(const uint8_t *src, uint32_t w[4]) {
+  for (int i = 0; i < 4; i++)
+    w[i] = (uint32_t)src[4 * i] | ((uint32_t)src[4 * i + 1] << 8) |
+           ((uint32_t)src[4 * i + 2] << 16) | ((uint32_t)src[4 * i + 3] << 24);
+}
+
+__global__ void decode_kernel(const uint8_t *__restrict__ blocks, uint8_t *__restrict__ rgba,
+                              uint32_t width, uint32_t height, int spec) {
+  const uint32_t bw = (width + 3) / 4, bh = (height + 3) / 4;
+  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= (uint64_t)bw * bh) return;
+  const uint32_t bx = (uint32_t)(b % bw), by = (uint32_t)(b / bw);
+  uint32_t w[4];
+  load_block_words(blocks + b * 16, w);
+  uint32_t outpx[16];
+  decode_block(w, spec, outpx);
   for (int r = 0; r < 4; r++) {
     const uint32_t y = by * 4 + r;
     if (y >= height) break;
@@ -615,6 +623,81 @@ __global__ void decode_kernel(const uint8_t *__restrict__ blocks, uint8_t *__res
       *reinterpret_cast<uint32_t *>(rgba + ((size_t)y * width + x) * 4) = outpx[4 * r + c];
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Quality: FasTC's Image::ComputePSNR metric (Base/src/Image.cpp:206-255),
+// per 4x4 block. Per texel, RGB premultiplied by alpha / 255 in double,
+// the three squared differences summed in channel order; per block, the
+// texels in row order (texels outside the image are skipped). One thread
+// decodes its block (FasTC's decoder semantics) and compares it with the
+// original texels, so no decoded image is written.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double texel_sse(uint32_t a, uint32_t b) {
+  const double ra = (double)(a >> 24) / 255.0, ua = (double)(b >> 24) / 255.0;
+  double s = 0.0;
+  for (int c = 0; c < 3; c++) {
+    const double d = ra * (double)((a >> (8 * c)) & 0xFF) - ua * (double)((b >> (8 * c)) & 0xFF);
+    s += d * d;
+  }
+  return s;
+}
+
+__global__ void block_error_kernel(const uint8_t *__restrict__ blocks,
+                                   const uint8_t *__restrict__ rgba, uint32_t width,
+                                   uint32_t height, double *__restrict__ sse) {
+  const uint32_t bw = (width + 3) / 4, bh = (height + 3) / 4;
+  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= (uint64_t)bw * bh) return;
+  const uint32_t bx = (uint32_t)(b % bw), by = (uint32_t)(b / bw);
+  uint32_t w[4];
+  load_block_words(blocks + b * 16, w);
+  uint32_t dec[16];
+  decode_block(w, 0, dec);
+  double s = 0.0;
+  for (int r = 0; r < 4; r++) {
+    const uint32_t y = by * 4 + r;
+    if (y >= height) break;
+    for (int c = 0; c < 4; c++) {
+      const uint32_t x = bx * 4 + c;
+      if (x >= width) break;
+      const uint8_t *p = rgba + ((size_t)y * width + x) * 4;
+      const uint32_t orig = (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) |
+                            ((uint32_t)p[3] << 24);
+      s += texel_sse(orig, dec[4 * r + c]);
+    }
+  }
+  sse[b] = s;
+}
+
+// Sum of n doubles in a fixed order (one CTA): thread t adds entries t,
+// t + 1024, ... in sequence, then a pairwise tree over the threads. The
+// result does not depend on scheduling, so it repeats bit for bit.
+__global__ void __launch_bounds__(1024) sum_kernel(const double *__restrict__ v, uint64_t n,
+                                                   double *__restrict__ out) {
+  __shared__ double s[1024];
+  double acc = 0.0;
+  for (uint64_t i = threadIdx.x; i < n; i += 1024) acc += v[i];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = 512; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) s[threadIdx.x] += s[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = s[0];
+}
+
+int launch_block_error(const uint8_t *blocks, const uint8_t *rgba, uint32_t width,
+                       uint32_t height, double *block_sse, double *total, void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const uint64_t nb = (uint64_t)((width + 3) / 4) * ((height + 3) / 4);
+  if (nb == 0) return 0;
+  const int threads = 128;
+  block_error_kernel<<<(unsigned)((nb + threads - 1) / threads), threads, 0, st>>>(
+      blocks, rgba, width, height, block_sse);
+  if (total) sum_kernel<<<1, 1024, 0, st>>>(block_sse, nb, total);
+  return (int)cudaPeekAtLastError();
 }
 
 int launch_decode(const uint8_t *blocks, uint8_t *rgba, uint32_t width, uint32_t height,

@@ -51,6 +51,11 @@ int launch_encode(const JobDev *jobs_dev, int njobs, uint64_t total_blocks,
 int launch_decode(const uint8_t *blocks, uint8_t *rgba, uint32_t width, uint32_t height,
                   int spec_semantics, void *stream);
 int device_sm_count(int device);
+// Per-block squared error of decoded `blocks` against the original `rgba`
+// (FasTC's PSNR metric) into block_sse, and their sum into *total when
+// total is not null.
+int launch_block_error(const uint8_t *blocks, const uint8_t *rgba, uint32_t width,
+                       uint32_t height, double *block_sse, double *total, void *stream);
 // The single-colour rank pre-pass (classify + scan); also resets the work
 // counter and status of `scratch`.
 int launch_rank_prepass(const JobDev *jobs_dev, int njobs, uint64_t total_blocks,

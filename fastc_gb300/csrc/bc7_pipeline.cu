@@ -38,6 +38,8 @@
 
 #include <cfloat>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 
 #include "bc7_block.cuh"
 #include "bc7_encode.cuh"
@@ -60,6 +62,17 @@ __constant__ uint32_t q_opt6[256];
 __constant__ uint8_t q_qlut[8][3][256];
 // single_channel_search() for every row and value, built once per device.
 __device__ uint32_t g_sct[kSctRows * 256];
+// The shape estimate's subsets as tasks (select stage): the member masks of
+// the 128 subsets of the two-subset shapes and of the 140 distinct subsets
+// of the three-subset shapes (192 less the repeats), each list sorted by
+// member count, most first, so that the 32 lanes of a round loop over the
+// same number of texels; and for subset k of shape s, the position of its
+// mask in the list ([s * 2 + k], [s * 3 + k]).
+constexpr int kSub2 = 128, kSub3 = 160;  // list lengths (the second padded to 5 rounds)
+__constant__ uint16_t q_sub2_mask[kSub2];
+__constant__ uint8_t q_sub2_pos[64 * 2];
+__constant__ uint16_t q_sub3_mask[kSub3];
+__constant__ uint8_t q_sub3_pos[64 * 3];
 
 __global__ void build_sct_kernel() {
   const int row = blockIdx.x, val = threadIdx.x;
@@ -96,9 +109,55 @@ static uint8_t host_quantize(uint32_t val, uint32_t mask, int pbit) {
   return (uint8_t)(dl < dh ? l8 : h8);
 }
 
+// Member masks of (shape, subset), distinct ones once, sorted by member
+// count (most first; ties in shape and subset order); pos[s * nsub + k] =
+// position of the mask of subset k of shape s. Returns the list length.
+static int build_subset_list(const uint32_t part[64], int nsub, uint16_t *list, uint8_t *pos) {
+  uint16_t masks[64 * 3];
+  int n = 0;
+  for (int sh = 0; sh < 64; sh++)
+    for (int k = 0; k < nsub; k++) {
+      uint16_t m = 0;
+      for (int i = 0; i < 16; i++)
+        if ((int)((part[sh] >> (2 * i)) & 3u) == k) m |= (uint16_t)(1u << i);
+      bool seen = false;
+      for (int j = 0; j < n; j++) seen = seen || masks[j] == m;
+      if (!seen) masks[n++] = m;
+    }
+  int len = 0;
+  for (int cnt = 16; cnt >= 1; cnt--)
+    for (int j = 0; j < n; j++)
+      if (__builtin_popcount(masks[j]) == cnt) list[len++] = masks[j];
+  for (int sh = 0; sh < 64; sh++)
+    for (int k = 0; k < nsub; k++) {
+      uint16_t m = 0;
+      for (int i = 0; i < 16; i++)
+        if ((int)((part[sh] >> (2 * i)) & 3u) == k) m |= (uint16_t)(1u << i);
+      for (int j = 0; j < len; j++)
+        if (list[j] == m) pos[sh * nsub + k] = (uint8_t)j;
+    }
+  return len;
+}
+
 void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t opt6[256]) {
   static bool done[64] = {false};
   if (device < 0 || device >= 64 || done[device]) return;
+  {
+    static const uint32_t part2[64] = {FASTC_PART2_WORDS};
+    static const uint32_t part3[64] = {FASTC_PART3_WORDS};
+    uint16_t l2[kSub2] = {0}, l3[kSub3] = {0};
+    uint8_t p2[128] = {0}, p3[192] = {0};
+    const int n2 = build_subset_list(part2, 2, l2, p2);
+    const int n3 = build_subset_list(part3, 3, l3, p3);
+    if (n2 != kSub2 || n3 > kSub3) {  // fixed by the BC7 partition tables
+      fprintf(stderr, "fastc_bc7: unexpected partition subset counts %d, %d\n", n2, n3);
+      abort();
+    }
+    cudaMemcpyToSymbol(q_sub2_mask, l2, sizeof(l2));
+    cudaMemcpyToSymbol(q_sub2_pos, p2, sizeof(p2));
+    cudaMemcpyToSymbol(q_sub3_mask, l3, sizeof(l3));
+    cudaMemcpyToSymbol(q_sub3_pos, p3, sizeof(p3));
+  }
   static uint8_t lut[8][3][256];
   for (int p = 1; p <= 8; p++)
     for (int b = -1; b <= 1; b++)
@@ -248,6 +307,130 @@ __device__ __forceinline__ double estimate_shape_int(const uint32_t *px, uint32_
   return err;
 }
 
+// One subset of the shape estimate as a task: the subset's members (mask of
+// texel positions) of the block's texels `px`, their bounding-box corners
+// as the endpoints of an unquantized QuantizedError (CP:1626-1655). A shape
+// adds for this subset 0 for a one-point box, else 0.0001 + the error; the
+// error is an integer below 2^23, returned with bit 31 set when the box has
+// more than one point.
+template <int kBits>
+__device__ __forceinline__ uint32_t estimate_subset_int(const uint32_t *px, uint32_t mask,
+                                                        uint4 *pal) {
+  uint32_t mn = 0xFFFFFFFFu, mx = 0u;
+  int se = 0;
+#pragma unroll 1
+  for (uint32_t m = mask; m; m &= m - 1) {
+    const uint32_t e = px[__ffs(m) - 1];
+    mn = __vminu4(mn, e);
+    mx = __vmaxu4(mx, e);
+    se += (int)__dp4a(e, e, 0u);
+  }
+  if (mn == mx) return 0u;
+  const Proj pj = make_proj(mn, mx);
+  palette_sq<kBits>(mn, mx, pal);
+  int acc = 0;
+#pragma unroll 1
+  for (uint32_t m = mask; m; m &= m - 1) {
+    const uint32_t e = px[__ffs(m) - 1];
+    bool two;
+    const int j1 = nearest_pair<kBits>(pj, e, two);
+    int bj;
+    acc += pair_term(e, pal, j1, two, bj);
+  }
+  return 0x80000000u | (uint32_t)(se + acc);
+}
+
+// A shape's estimate as FasTC sums it in double: per subset, in order, 0
+// or 0.0001 + the error.
+template <int kNSub>
+__device__ __forceinline__ double shape_estimate_double(const uint32_t *est, const uint8_t *pos,
+                                                        int sh) {
+  double err = 0.0;
+#pragma unroll
+  for (int k = 0; k < kNSub; k++) {
+    const uint32_t v = est[pos[sh * kNSub + k]];
+    double e = 0.0;
+    if (v) {
+      e = 0.0001;
+      e = e + (double)(float)(int)(v & 0x7FFFFFFFu);
+    }
+    err = err + e;
+  }
+  return err;
+}
+
+// One pass of BoxSelection (CP:1670-1750) for the uniform metric: every
+// distinct subset estimated once, in rounds of 32 lanes over the
+// member-count-sorted list, into the warp's `est`; each lane then sums the
+// subsets of shapes `lane` and `lane + 32`. The choice is made on integers:
+// a shape's double estimate is its integer total plus at most three times
+// 0.0001 (and rounding far below that), so the first shape with estimate 0
+// is the first with no multi-point box, and the least estimate is among the
+// shapes of least integer total; only when several shapes share that total
+// are their double estimates formed and compared (strict <, first index
+// wins, as FasTC's loop). Returns the chosen shape; `zero` is set when it
+// is FasTC's early exit (estimate below 1e-9).
+template <int kNSub>
+__device__ __forceinline__ int select_shape_int(const uint32_t *px, int lane, uint32_t *est,
+                                                uint4 *pal, bool &zero) {
+  constexpr int kBits = kNSub == 2 ? 3 : 2;
+  constexpr int kLen = kNSub == 2 ? kSub2 : kSub3;
+  const uint16_t *list = kNSub == 2 ? q_sub2_mask : q_sub3_mask;
+  const uint8_t *pos = kNSub == 2 ? q_sub2_pos : q_sub3_pos;
+#pragma unroll 1
+  for (int r = lane; r < kLen; r += 32) {
+    const uint32_t m = list[r];
+    est[r] = m ? estimate_subset_int<kBits>(px, m, pal) : 0u;
+  }
+  __syncwarp();
+  uint32_t tot[2];
+  bool any[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int sh = lane + 32 * h;
+    uint32_t t = 0, f = 0;
+#pragma unroll
+    for (int k = 0; k < kNSub; k++) {
+      const uint32_t v = est[pos[sh * kNSub + k]];
+      t += v & 0x7FFFFFFFu;
+      f |= v;
+    }
+    tot[h] = t;
+    any[h] = (f >> 31) != 0;
+  }
+  const uint64_t z = (uint64_t)__ballot_sync(0xFFFFFFFFu, !any[0]) |
+                     ((uint64_t)__ballot_sync(0xFFFFFFFFu, !any[1]) << 32);
+  int chosen;
+  if (z) {
+    zero = true;
+    chosen = __ffsll((long long)z) - 1;
+  } else {
+    zero = false;
+    uint32_t mt = min(tot[0], tot[1]);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) mt = min(mt, __shfl_xor_sync(0xFFFFFFFFu, mt, o));
+    const uint64_t cand = (uint64_t)__ballot_sync(0xFFFFFFFFu, tot[0] == mt) |
+                          ((uint64_t)__ballot_sync(0xFFFFFFFFu, tot[1] == mt) << 32);
+    if (__popcll(cand) == 1) {
+      chosen = __ffsll((long long)cand) - 1;
+    } else {
+      double be = tot[0] == mt ? shape_estimate_double<kNSub>(est, pos, lane) : DBL_MAX;
+      const double e1 = tot[1] == mt ? shape_estimate_double<kNSub>(est, pos, lane + 32) : DBL_MAX;
+      int bi = lane;
+      argmin_pair(be, bi, e1, lane + 32);
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        const double oe = __shfl_xor_sync(0xFFFFFFFFu, be, o);
+        const int oi = __shfl_xor_sync(0xFFFFFFFFu, bi, o);
+        argmin_pair(be, bi, oe, oi);
+      }
+      chosen = bi;
+    }
+  }
+  __syncwarp();
+  return chosen;
+}
+
 // The float-metric estimate, kept out of line.
 __device__ __noinline__ double estimate_shape_float(const uint32_t *px, uint32_t part, int nsub,
                                                     int bits, int metric) {
@@ -278,7 +461,8 @@ __device__ __forceinline__ void estimate_pair(const uint32_t *px, const uint32_t
 __device__ __forceinline__ Selection box_selection_pipe(const uint32_t *px,
                                                         const uint32_t *part2,
                                                         const uint32_t *part3, int metric,
-                                                        int lane, uint32_t *buf, uint4 *pal) {
+                                                        int lane, uint32_t *buf, uint4 *pal,
+                                                        uint32_t *est) {
   Selection r;
   r.nshapes = 1;
   r.shape[0] = r.shape[1] = 0;
@@ -290,6 +474,26 @@ __device__ __forceinline__ Selection box_selection_pipe(const uint32_t *px,
 #pragma unroll
   for (int pass = 0; pass < 2; pass++) {
     const int nsub = pass ? 3 : 2;
+    if (metric == 0) {
+      bool zero;
+      const int sh = pass ? select_shape_int<3>(px, lane, est, pal, zero)
+                          : select_shape_int<2>(px, lane, est, pal, zero);
+      r.shape[pass] = (uint32_t)sh;
+      r.nparts[pass] = (uint32_t)nsub;
+      if (zero) {
+        r.modes = pass ? kModesThree : kModesTwo;
+        return r;
+      }
+      if (pass == 0) {
+        if (!opaque) {
+          r.modes &= kModesAlpha;
+          return r;
+        }
+        r.modes &= ~((1u << 4) | (1u << 5));
+        r.nshapes = 2;
+      }
+      continue;
+    }
     double e0, e1;
     if (pass) estimate_pair<3>(px, part3, metric, lane, buf, pal, e0, e1);
     else estimate_pair<2>(px, part2, metric, lane, buf, pal, e0, e1);
@@ -334,6 +538,7 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
   __shared__ uint32_t s_px[kWarps][16];
   __shared__ uint32_t s_buf[16 * kLaneStride];
   __shared__ uint4 s_pal[8 * kLaneStride];
+  __shared__ uint32_t s_est[kWarps][kSub3];
   for (int i = threadIdx.x; i < 64; i += blockDim.x) {
     s_part2[i] = q_part2[i];
     s_part3[i] = q_part3[i];
@@ -388,7 +593,7 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
       continue;
     }
     const Selection s = box_selection_pipe(px, s_part2, s_part3, (int)jb.metric, lane,
-                                           s_buf + threadIdx.x, s_pal + threadIdx.x);
+                                           s_buf + threadIdx.x, s_pal + threadIdx.x, s_est[wid]);
     uint32_t modes = s.modes & jb.modes;
     if (modes == 0) modes = jb.modes & 0xFF;  // FasTC: undefined behaviour
     const int c = lane < kClasses ? class_task_count(s, modes, lane) : 0;

@@ -133,6 +133,31 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_compress_image(const uint8_t *rgba, uin
 FASTC_BC7_API fastc_bc7_status fastc_bc7_decompress(const uint8_t *blocks, uint8_t *rgba, uint32_t width,
                                       uint32_t height, int spec_semantics);
 
+/* Image quality of encoded blocks against the original texels, by FasTC's
+ * Image::ComputePSNR metric (Base/src/Image.cpp:206-255): per texel the RGB
+ * channels premultiplied by alpha / 255, squared differences summed over
+ * R, G, B; PSNR = 10 log10(3 * 255^2 / (sum / (width * height))). The
+ * blocks are decoded with FasTC's decoder semantics on the GPU and never
+ * written out as an image.
+ *
+ * fastc_bc7_psnr: host buffers (blocks: width*height bytes for multiples of
+ * 4; rgba: width*height*4 bytes). *psnr receives the PSNR (may be NULL);
+ * block_sse, if not NULL, receives one double per 4x4 block in raster
+ * order (the texels of the block in row order; texels outside the image
+ * skipped). The PSNR equals FasTC's up to the order of the double sum
+ * (per block, then a fixed tree over the blocks, instead of one pass over
+ * the texels). */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_psnr(const uint8_t *blocks, const uint8_t *rgba,
+                                              uint32_t width, uint32_t height, double *psnr,
+                                              double *block_sse);
+/* The same on device pointers, asynchronous on `stream`: block_sse (one
+ * double per block, required) and, if sse_total is not NULL, their sum in
+ * one device double (the same value on every run). Allocates nothing. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_block_error_device(const uint8_t *blocks,
+                                                            const uint8_t *rgba, uint32_t width,
+                                                            uint32_t height, double *block_sse,
+                                                            double *sse_total, void *stream);
+
 /* BPTCC::LogicalBlock (BPTCCompressor.h:203-209): the stored fields of one
  * block. Endpoints are at their stored precision (p-bit appended as the
  * lowest bit), depth[] gives that precision per channel (0: channel absent,

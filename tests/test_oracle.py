@@ -133,3 +133,27 @@ def test_exact_projection_rounds_to_the_integer_index():
         for j in range(1, k):
             sc = (np.float32(j) / np.float32(k)) * np.float32(k)
             assert sc.dtype == np.float32 and float(sc) == j, (k, j, sc)
+
+
+def test_float_thresholds_equal_the_double_comparisons():
+    """The PCA's tests against 1e-7, 1e-8 and 1e-10, which FasTC makes on
+    floats widened to double, are made in single precision on the GPU with
+    the float literals: 1e-7f and 1e-10f are the least floats above their
+    doubles (x > 1e-7 iff x >= 1e-7f; x < 1e-10 iff x < 1e-10f), 1e-8f the
+    greatest float below 1e-8 (x < 1e-8 iff x <= 1e-8f)."""
+    def neighbours(c):
+        f = np.float32(c)
+        return float(np.nextafter(f, np.float32(0))), float(f), float(np.nextafter(f, np.float32(1)))
+
+    for c in (1e-7, 1e-10):
+        below, f, _ = neighbours(c)
+        assert below < c < f
+    below, f, above = neighbours(1e-8)
+    assert f < 1e-8 < above
+    # the comparisons themselves on the floats around each threshold
+    for x in neighbours(1e-7):
+        assert (x > 1e-7) == (np.float32(x) >= np.float32(1e-7))
+    for x in neighbours(1e-10):
+        assert (x < 1e-10) == (np.float32(x) < np.float32(1e-10))
+    for x in neighbours(1e-8):
+        assert (x < 1e-8) == (np.float32(x) <= np.float32(1e-8))
