@@ -271,42 +271,6 @@ __device__ __forceinline__ uint32_t scanned(const uint16_t *local, const uint32_
 // select
 // ---------------------------------------------------------------------------
 
-// BoxSelection's shape estimate (CP:1626-1655) for the uniform metric in
-// exact integers: the corners of each subset's bounding box are the
-// endpoints of an unquantized QuantizedError over the subset's texels.
-// Loops stay rolled: the select kernel is instruction-fetch bound when the
-// estimate is unrolled.
-template <int kNSub, int kBits>
-__device__ __forceinline__ double estimate_shape_int(const uint32_t *px, uint32_t part,
-                                                     uint32_t *buf, uint4 *pal) {
-  constexpr int T = kLaneStride;
-  double err = 0.0;
-#pragma unroll 1
-  for (int s = 0; s < kNSub; s++) {
-    uint32_t mn = 0xFFFFFFFFu, mx = 0u;
-    int n = 0, se = 0;
-#pragma unroll 4
-    for (int i = 0; i < 16; i++) {
-      const uint32_t e = px[i];
-      if ((int)((part >> (2 * i)) & 3u) == s) {
-        buf[n * T] = e;
-        n++;
-        mn = __vminu4(mn, e);
-        mx = __vmaxu4(mx, e);
-        se += (int)__dp4a(e, e, 0u);
-      }
-    }
-    double e = 0.0;
-    if (mn != mx) {
-      e = 0.0001;
-      uint64_t unused = 0;
-      e = e + (double)qe_smem<kBits, false>(buf, n, 0, se, pal, mn, mx, unused);
-    }
-    err = err + e;
-  }
-  return err;
-}
-
 // One subset of the shape estimate as a task: the subset's members (mask of
 // texel positions) of the block's texels `px`, their bounding-box corners
 // as the endpoints of an unquantized QuantizedError (CP:1626-1655). A shape
@@ -440,18 +404,17 @@ __device__ __noinline__ double estimate_shape_float(const uint32_t *px, uint32_t
   return estimate_shape(px, part, nsub, bits, w);
 }
 
-// One pass of BoxSelection (CP:1670-1750) over the 64 shapes with kNSub
-// subsets, two shapes per lane: the estimates of this lane's shapes.
+// One pass of BoxSelection (CP:1670-1750) for the nonuniform metric over
+// the 64 shapes with kNSub subsets, two shapes per lane: the estimates of
+// this lane's shapes.
 template <int kNSub>
 __device__ __forceinline__ void estimate_pair(const uint32_t *px, const uint32_t *part, int metric,
-                                              int lane, uint32_t *buf, uint4 *pal, double &e0,
-                                              double &e1) {
+                                              int lane, double &e0, double &e1) {
   constexpr int kBits = kNSub == 2 ? 3 : 2;
 #pragma unroll 1
   for (int h = 0; h < 2; h++) {
     const uint32_t pw = part[lane + 32 * h];
-    const double v = metric == 0 ? estimate_shape_int<kNSub, kBits>(px, pw, buf, pal)
-                                 : estimate_shape_float(px, pw, kNSub, kBits, metric);
+    const double v = estimate_shape_float(px, pw, kNSub, kBits, metric);
     if (h == 0) e0 = v;
     else e1 = v;
   }
@@ -461,8 +424,7 @@ __device__ __forceinline__ void estimate_pair(const uint32_t *px, const uint32_t
 __device__ __forceinline__ Selection box_selection_pipe(const uint32_t *px,
                                                         const uint32_t *part2,
                                                         const uint32_t *part3, int metric,
-                                                        int lane, uint32_t *buf, uint4 *pal,
-                                                        uint32_t *est) {
+                                                        int lane, uint4 *pal, uint32_t *est) {
   Selection r;
   r.nshapes = 1;
   r.shape[0] = r.shape[1] = 0;
@@ -495,8 +457,8 @@ __device__ __forceinline__ Selection box_selection_pipe(const uint32_t *px,
       continue;
     }
     double e0, e1;
-    if (pass) estimate_pair<3>(px, part3, metric, lane, buf, pal, e0, e1);
-    else estimate_pair<2>(px, part2, metric, lane, buf, pal, e0, e1);
+    if (pass) estimate_pair<3>(px, part3, metric, lane, e0, e1);
+    else estimate_pair<2>(px, part2, metric, lane, e0, e1);
     const uint64_t zero = (uint64_t)__ballot_sync(0xFFFFFFFFu, e0 < 1e-9) |
                           ((uint64_t)__ballot_sync(0xFFFFFFFFu, e1 < 1e-9) << 32);
     if (zero) {
@@ -536,7 +498,6 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
   static_assert(kWarps * 32 == kLaneStride, "shared arrays use the lane stride");
   __shared__ uint32_t s_part2[64], s_part3[64];
   __shared__ uint32_t s_px[kWarps][16];
-  __shared__ uint32_t s_buf[16 * kLaneStride];
   __shared__ uint4 s_pal[8 * kLaneStride];
   __shared__ uint32_t s_est[kWarps][kSub3];
   for (int i = threadIdx.x; i < 64; i += blockDim.x) {
@@ -593,7 +554,7 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
       continue;
     }
     const Selection s = box_selection_pipe(px, s_part2, s_part3, (int)jb.metric, lane,
-                                           s_buf + threadIdx.x, s_pal + threadIdx.x, s_est[wid]);
+                                           s_pal + threadIdx.x, s_est[wid]);
     uint32_t modes = s.modes & jb.modes;
     if (modes == 0) modes = jb.modes & 0xFF;  // FasTC: undefined behaviour
     const int c = lane < kClasses ? class_task_count(s, modes, lane) : 0;
