@@ -144,30 +144,95 @@ def profile_per_block():
         return None, None
 
 
-def cpu_sample(imgs, budget_px: int):
-    """Deterministic sample: textures in set order until the pixel budget."""
-    out, px = [], 0
-    for im in imgs:
-        if px + im.shape[0] * im.shape[1] > budget_px and out:
-            continue
-        out.append(im)
-        px += im.shape[0] * im.shape[1]
-        if px >= budget_px:
-            break
-    return out, px
+# The CPU legs encode a uniform sample of the set's blocks: every
+# BAND_STRIDE-th block row of the 512 textures, rows counted across the set
+# in texture order (89 rows, 9,368 blocks, 149,888 texels). A block's
+# cost depends only on its texels, so this is the set's content mix at
+# 1/720 of its size.
+BAND_STRIDE = 720
 
 
-def run_cpu_baseline(imgs, budget_px: int):
+def band_sample(stride: int = BAND_STRIDE):
+    """[(texture index, first texel row, the 4-row band as RGBA8)] of every
+    stride-th block row of the texture set."""
+    from fastc_gb300 import synth
+
+    out, g = [], 0
+    for i, (w, h) in enumerate(synth.texture_sides(SET_SEED, SET_COUNT)):
+        for r in range(h // 4):
+            if g % stride == stride // 2:
+                out.append((i, 4 * r, synth.tile_mix(SET_SEED * 1000 + i, w, 4, 0, 4 * r)))
+            g += 1
+    return out
+
+
+def _single_colour_blocks_before(tex, y0: int) -> int:
+    """Single-colour blocks of `tex` in the block rows above texel row y0."""
+    import numpy as np
+
+    top = tex[:y0].view("<u4")[..., 0]
+    if top.size == 0:
+        return 0
+    h, w = top.shape
+    blk = top.reshape(h // 4, 4, w // 4, 4).transpose(0, 2, 1, 3).reshape(h // 4, w // 4, 16)
+    return int((blk == blk[..., :1]).all(-1).sum())
+
+
+def encode_bands(bands, threads: int, kind: str, textures=None):
+    """One pass over the bands on `threads` host threads (each thread takes
+    every threads-th band): FasTC's own encoder (kind "reference", the
+    in-place build; its global RNG is shared by the threads, as under
+    tc -t N) or the oracle port (kind "port", per-fit streams). With the
+    whole `textures` the port encodes each band as that row of its texture
+    (the texture's block coordinates seed the annealing, the watermark
+    counter continues from the rows above), giving the GPU's bytes. Returns
+    (seconds, the band's blocks for each band)."""
+    import concurrent.futures as cf
+
+    import numpy as np
+
     from oracle import oracle as O
 
-    port = O.Port()
-    cores = os.cpu_count() or 1
-    sample, px = cpu_sample(imgs, budget_px)
+    enc = O.Reference() if kind == "reference" else O.Port()
+    if kind == "reference":
+        enc.lib.ref_set_seed(ANNEAL_SEED)
+    prior = [_single_colour_blocks_before(textures[i], y0) for i, y0, _ in bands] if textures else None
+    outs = [None] * len(bands)
+
+    def work(t):
+        for k in range(t, len(bands), threads):
+            i, y0, band = bands[k]
+            img = np.ascontiguousarray(band)
+            h, w = img.shape[:2]
+            if kind == "reference":
+                o = np.zeros(w * h, dtype=np.uint8)
+                enc.lib.ref_compress(O._ptr(img), O._ptr(o), w, h, 0, 0, w, h, STEPS_Q, 0xFF, 0)
+                outs[k] = o
+            elif textures is None or y0 == 0:
+                outs[k] = enc.compress(img, steps=STEPS_Q, seed=ANNEAL_SEED)
+            else:
+                o = enc.compress(textures[i], steps=STEPS_Q, seed=ANNEAL_SEED, rect=(0, y0, w, y0),
+                                 state=np.array([0, prior[k]], np.uint32))
+                outs[k] = o[y0 * w:(y0 + 4) * w]
+
     t0 = time.perf_counter()
-    outs = [port.compress_mt(im, steps=STEPS_Q, seed=ANNEAL_SEED, threads=cores) for im in sample]
-    dt = time.perf_counter() - t0
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(work, range(threads)))
+    return time.perf_counter() - t0, outs
+
+
+def band_texels(bands) -> int:
+    return sum(b[2].shape[0] * b[2].shape[1] for b in bands)
+
+
+def run_cpu_baseline(textures=None):
+    cores = os.cpu_count() or 1
+    bands = band_sample()
+    px = band_texels(bands)
+    dt, outs = encode_bands(bands, cores, "port", textures)
     return {"value": px / dt / 1e6, "unit": "MPix/s", "cores": cores, "kind": "port",
-            "sample": f"{len(sample)} textures of the set, {px} texels, q50, one pass"}, sample, outs
+            "sample": f"every {BAND_STRIDE}th block row of the set: {len(bands)} rows, {px} texels, "
+                      f"q50, one pass"}, bands, outs
 
 
 def reference_impl(args):
@@ -176,51 +241,61 @@ def reference_impl(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from fastc_gb300 import synth
     from oracle import oracle as O
 
-    sides = synth.texture_sides(SET_SEED, SET_COUNT)
-    imgs = [synth.tile_mix(SET_SEED * 1000 + i, w, h) for i, (w, h) in enumerate(sides[:64])]
-    sample, px = cpu_sample(imgs, 160_000)
+    bands = band_sample()
+    px = band_texels(bands)
     cores = os.cpu_count() or 1
     kind = "port"
-    ref = None
     if os.path.exists(O.REF_SO):
         try:
-            ref = O.Reference()
+            O.Reference()
             kind = "reference"
         except OSError:
-            ref = None
-    port = O.Port()
-
-    def one_pass():
-        if ref is not None:
-            # tc -t N: N threads on disjoint block ranges of each image
-            for im in sample:
-                ref.compress_threads(im, steps=STEPS_Q, threads=cores, seed=ANNEAL_SEED)
-        else:
-            for im in sample:
-                port.compress_mt(im, steps=STEPS_Q, seed=ANNEAL_SEED, threads=cores)
-
+            kind = "port"
     for _ in range(args.warmup):
-        one_pass()
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        one_pass()
-        times.append(time.perf_counter() - t0)
+        encode_bands(bands, cores, kind)
+    times = [encode_bands(bands, cores, kind)[0] for _ in range(args.steps)]
     dt = sum(times) / len(times)
     v = px / dt / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "MPix/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": "texture_set_512_q50", "textures": len(sample), "texels": px, "steps_q": STEPS_Q},
+        "config": {"workload": "texture_set_512_q50", "sample_rows": len(bands), "texels": px,
+                   "steps_q": STEPS_Q},
         "cpu_baseline": {"value": v, "unit": "MPix/s", "cores": cores, "kind": kind,
-                         "sample": f"{len(sample)} textures of the set, {px} texels per step"},
+                         "sample": f"every {BAND_STRIDE}th block row of the set: {len(bands)} rows, "
+                                   f"{px} texels per step"},
         "e2e": {"value": v, "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def calibrate_cpu(args):
+    """--calibrate-cpu (where FasTC's encoder is built in place, oracle/_ref):
+    FasTC's own encoder and the oracle port on the same sampled rows and
+    thread count, `--steps` passes each after `--warmup`; prints both rates
+    and their ratio, which says how far the port's speed stands for
+    FasTC's on the GPU machine, where only the port exists."""
+    from oracle import oracle as O
+
+    if not os.path.exists(O.REF_SO):
+        print(json.dumps({"calibrate_cpu": "unavailable", "why": "oracle/_ref not built here"}))
+        return
+    bands = band_sample()
+    px = band_texels(bands)
+    threads = args.threads or (os.cpu_count() or 1)
+    res = {}
+    for kind in ("reference", "port"):
+        for _ in range(args.warmup):
+            encode_bands(bands, threads, kind)
+        ts = [encode_bands(bands, threads, kind)[0] for _ in range(args.steps)]
+        res[kind] = px / statistics.median(ts) / 1e6
+    print(json.dumps({"calibrate_cpu": {"reference_mpix_s": res["reference"], "port_mpix_s": res["port"],
+                                        "port_over_reference": res["port"] / res["reference"],
+                                        "threads": threads, "passes": args.steps, "texels": px,
+                                        "rows": len(bands), "steps_q": STEPS_Q}}))
 
 
 def max_over_ranks(seconds: float, dist, device: str) -> float:
@@ -249,38 +324,38 @@ def _gen_serve(args):
     return synth.tile_mix(SERVE_SEED * 1000 + i, w, h)
 
 
-def serve_bench(args):
-    """--serve: the request server under a Poisson stream of requests (sides
-    log-uniform in 32..4096 rounded to multiples of 4, q drawn from
-    {0, 16, 50} with probabilities {0.3, 0.4, 0.3}, 8 GB device budget) at a
-    sweep of arrival rates. Prints one JSON line with p50/p99 latency and
-    MP/s per rate. Textures come from a pool of seeded images that requests
-    draw from."""
+def serve_pool(npool: int = 48):
+    """The seeded texture pool the serving requests draw from (sides
+    log-uniform in 32..4096, multiples of 4), generated on host processes."""
     import numpy as np
 
     rng = np.random.default_rng(SERVE_SEED)
-    npool = 48
     sides = [(int(4 * round(32 * (128 ** rng.random()) / 4)), int(4 * round(32 * (128 ** rng.random()) / 4)))
              for _ in range(npool)]
     ctx = mp.get_context("spawn")
     with ctx.Pool(max(1, min(16, os.cpu_count() or 1))) as pool:
-        imgs = pool.map(_gen_serve, [(i, w, h) for i, (w, h) in enumerate(sides)], chunksize=1)
+        return pool.map(_gen_serve, [(i, w, h) for i, (w, h) in enumerate(sides)], chunksize=1)
 
-    import torch
 
-    torch.cuda.init()
+def serve_sweep(imgs, rates, seconds: float):
+    """The request server under Poisson arrivals at each rate for `seconds`
+    (q from {0, 16, 50} w.p. {0.3, 0.4, 0.3}, 8 GB budget, 3 batches in
+    flight): per rate the offered and the served MPix/s (texels over the
+    time from the first arrival to the last completion), p50/p99 latency."""
+    import numpy as np
+
     from fastc_gb300 import CompressionSettings
     from fastc_gb300.serve import Server
 
+    rng = np.random.default_rng(SERVE_SEED + 1)
     qs = [0, 16, 50]
-    rates = [float(r) for r in args.serve_rates.split(",")]
-    results = []
-    # warm the device (tables, allocator)
-    with Server(memory_budget=8 << 30) as srv:
+    with Server(memory_budget=8 << 30) as srv:  # warm the device (tables, allocator)
         srv.wait(srv.submit(imgs[0], CompressionSettings(num_simulated_annealing_steps=0)))
+    mean_px = float(np.mean([im.shape[0] * im.shape[1] for im in imgs]))
+    results = []
     for rate in rates:
-        n = max(8, int(rate * args.serve_seconds))
-        picks = rng.integers(0, npool, n)
+        n = max(8, int(rate * seconds))
+        picks = rng.integers(0, len(imgs), n)
         qsel = rng.choice(qs, size=n, p=[0.3, 0.4, 0.3])
         gaps = rng.exponential(1.0 / rate, n)
         with Server(memory_budget=8 << 30, max_inflight=3) as srv:
@@ -295,19 +370,88 @@ def serve_bench(args):
                 reqs.append(srv.submit(imgs[picks[k]],
                                        CompressionSettings(num_simulated_annealing_steps=int(qsel[k]),
                                                            seed=k)))
+            t_sub = time.perf_counter() - t0
             for r in reqs:
                 srv.wait(r)
             dt = time.perf_counter() - t0
             st = srv.stats()
         px = sum(imgs[i].shape[0] * imgs[i].shape[1] for i in picks)
-        results.append({"rate_per_s": rate, "requests": n, "mpix": px / 1e6, "mpix_s": px / dt / 1e6,
+        results.append({"rate_per_s": rate, "requests": n, "offered_mpix_s": rate * mean_px / 1e6,
+                        "submitted_in_s": t_sub, "mpix_s": px / dt / 1e6,
                         "p50_ms": st["p50_latency_ms"], "p99_ms": st["p99_latency_ms"],
                         "batches": st["batches"], "peak_bytes": st["peak_bytes"]})
+    return results
+
+
+def serve_bench(args):
+    """--serve: the request server under a Poisson stream of requests (sides
+    log-uniform in 32..4096 rounded to multiples of 4, q drawn from
+    {0, 16, 50} with probabilities {0.3, 0.4, 0.3}, 8 GB device budget) at a
+    sweep of arrival rates. Prints one JSON line with p50/p99 latency and
+    MP/s per rate. Textures come from a pool of seeded images that requests
+    draw from."""
+    imgs = serve_pool()
+    import torch
+
+    torch.cuda.init()
+    results = serve_sweep(imgs, [float(r) for r in args.serve_rates.split(",")], args.serve_seconds)
     print(json.dumps({"metric": "BC7 serving: p50/p99 latency and MPix/s under Poisson arrivals",
                       "config": {"workload": "poisson_mixed_q_8gb", "sides": "log-uniform 32..4096",
                                  "q": "{0,16,50} w.p. {0.3,0.4,0.3}", "budget_bytes": 8 << 30,
-                                 "texture_pool": npool},
+                                 "texture_pool": len(imgs)},
                       "sweep": results}))
+
+
+def _gen_stripe(args):
+    from fastc_gb300 import synth
+
+    y0, rows = args
+    return synth.tile_mix_radial_alpha(5, 8192, rows, 0, y0)
+
+
+def config5_image():
+    """The 8192x8192 radial-alpha image of the large q100 configuration,
+    generated as 16 stripes on host processes."""
+    import numpy as np
+
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(max(1, min(8, os.cpu_count() or 1))) as pool:
+        parts = pool.map(_gen_stripe, [(512 * k, 512) for k in range(16)], chunksize=1)
+    return np.concatenate(parts, axis=0)
+
+
+def single_launch(img, steps: int, warmup: int, reps: int):
+    """One texture encoded by one device-memory call per launch (inputs
+    resident): MPix/s by CUDA events over `reps` launches, the blocks, and
+    their PSNR computed on the GPU."""
+    import torch
+
+    from fastc_gb300 import CompressionJob, CompressionSettings, compress_jobs, psnr
+
+    h, w = img.shape[:2]
+    din = torch.from_numpy(img).cuda()
+    dout = torch.zeros(w * h, dtype=torch.uint8, device="cuda")
+    job = CompressionJob(din, dout, w, h)
+    st = CompressionSettings(num_simulated_annealing_steps=steps, seed=ANNEAL_SEED)
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        compress_jobs([job], st)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        compress_jobs([job], st)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dt = e0.elapsed_time(e1) / 1e3 / reps
+    return w * h / dt / 1e6, dt, din, dout, psnr(dout, din, w, h)
+
+
+def fasTC_full_size_psnr(name: str):
+    """FasTC's mean PSNR over its pinned seeds for a full-size fixture."""
+    with open(os.path.join(ROOT, "tests", "golden", "manifest.json")) as f:
+        case = json.load(f)["full_size"][name]
+    return sum(case["psnr"]) / len(case["psnr"])
 
 
 def profile_case(args):
@@ -349,8 +493,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cpu-budget-px", type=int, default=400_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the config-2, config-5 and serving measurements")
+    ap.add_argument("--calibrate-cpu", action="store_true",
+                    help="time FasTC's own encoder (oracle/_ref) against the port on the CPU sample")
+    ap.add_argument("--threads", type=int, default=0, help="host threads of --calibrate-cpu")
     ap.add_argument("--serve", action="store_true", help="run the serving sweep instead")
     ap.add_argument("--serve-rates", default="20,60,120")
     ap.add_argument("--serve-seconds", type=float, default=4.0)
@@ -371,6 +519,9 @@ def main():
     if args.impl == "reference":
         reference_impl(args)
         return
+    if args.calibrate_cpu:
+        calibrate_cpu(args)
+        return
     if args.serve:
         serve_bench(args)
         return
@@ -381,6 +532,13 @@ def main():
 
     # host work (texture generation) before the first GPU call
     imgs = make_texture_set(min(16, os.cpu_count() or 1))
+    extras = rank == 0 and not args.no_extras
+    if extras:
+        from fastc_gb300 import synth
+
+        c2_img = synth.tile_mix(2, 2048, 2048)
+        c5_img = config5_image()
+        pool = serve_pool()
 
     import numpy as np
     import torch
@@ -486,17 +644,13 @@ def main():
     e2e_value = aggregate_mpix_s(total_px, world, e2e_steps, e2e_dt)
     e2e_identical = all(np.array_equal(h.numpy(), d.cpu().numpy()) for h, d in zip(hout, dout))
 
-    # --- PSNR of the batched output (GPU decoder, reference semantics) ---
-    from fastc_gb300 import decompress
+    # --- PSNR of the batched output (FasTC's metric, on the GPU) ---
+    from fastc_gb300 import psnr as gpu_psnr
 
-    mse, npx = 0.0, 0
-    for im, blk in zip(imgs, dout):
-        dec = decompress(blk, im.shape[1], im.shape[0]).to(torch.float64)
-        src = torch.from_numpy(im).cuda().to(torch.float64)
-        a0, a1 = src[..., 3:4] / 255.0, dec[..., 3:4] / 255.0
-        mse += float(((a0 * src[..., :3] - a1 * dec[..., :3]) ** 2).sum())
-        npx += im.shape[0] * im.shape[1]
-    psnr = 10 * np.log10(3 * 255.0 ** 2 / (mse / npx))
+    sse = 0.0
+    for a, blk, im in zip(din, dout, imgs):
+        sse += float(gpu_psnr(blk, a, im.shape[1], im.shape[0], block_sse=True)[1].sum())
+    psnr = 10 * np.log10(3 * 255.0 ** 2 / (sse / total_px))
 
     peak, peak_kind = measured_peaks()
     step_s = dt / args.steps
@@ -541,15 +695,42 @@ def main():
                                   "frac": issued / peak_issue,
                                   "instructions_per_block": ipb, "sms": sms, "sm_mhz": mhz}
     if rank == 0 and not args.no_cpu_baseline:
-        cb, sample, outs = run_cpu_baseline(imgs, args.cpu_budget_px)
-        # same bytes as the GPU on the sample
-        idx = [next(i for i, im in enumerate(imgs) if im is s) for s in sample]
-        cb["identical_to_gpu"] = all(np.array_equal(o, dout[i].cpu().numpy()) for o, i in zip(outs, idx))
+        cb, bands, outs = run_cpu_baseline(imgs)
+        # same bytes as the GPU on the sampled rows
+        cb["identical_to_gpu"] = all(
+            np.array_equal(o, dout[i][y0 * imgs[i].shape[1]:(y0 + 4) * imgs[i].shape[1]].cpu().numpy())
+            for o, (i, y0, _) in zip(outs, bands))
         line["cpu_baseline"] = cb
-    if rank == 0:
-        print(json.dumps(line))
     plan.close()
     small_plan.close()
+    if extras:
+        del din, dout, hin, hout
+        torch.cuda.empty_cache()
+        # config 2: one 2048x2048 tile-mix texture at q50 in one launch
+        mps, dt2, d_in, d_out, db = single_launch(c2_img, STEPS_Q, 2, 3)
+        ref_db = fasTC_full_size_psnr("c2_tile2048_q50")
+        line["config2"] = {"workload": "tile_mix_2048x2048_q50", "mpix_s": mps, "ms_per_launch": dt2 * 1e3,
+                           "psnr_db": db, "psnr_fasTC_db": ref_db, "psnr_delta_db": db - ref_db}
+        del d_in, d_out
+        # config 5: one 8192x8192 radial-alpha texture at q100 in one launch
+        with ClockSampler(local_rank) as c5_clocks:
+            mps, dt5, d_in, d_out, db = single_launch(c5_img, 100, 1, 2)
+        stripe = gpu_psnr(d_out[3840 * 8192:4352 * 8192], d_in[3840:4352], 8192, 512)
+        ref_db = fasTC_full_size_psnr("c5_stripe8192x512_q100")
+        line["config5"] = {"workload": "radial_alpha_8192x8192_q100", "mpix_s": mps, "ms_per_launch": dt5 * 1e3,
+                           "psnr_db": db, "stripe_rows_3840_4351_psnr_db": stripe,
+                           "stripe_psnr_fasTC_db": ref_db, "stripe_psnr_delta_db": stripe - ref_db,
+                           "clocks": c5_clocks.summary()}
+        del d_in, d_out
+        torch.cuda.empty_cache()
+        # serving: Poisson arrivals below and above saturation
+        sweep = serve_sweep(pool, [60.0, 2000.0], 2.0)
+        line["serve"] = {"workload": "poisson_mixed_q_8gb", "sides": "log-uniform 32..4096",
+                         "q": "{0,16,50} w.p. {0.3,0.4,0.3}", "sweep": sweep,
+                         "max_sustained_mpix_s": sweep[-1]["mpix_s"], "p99_ms_at_max": sweep[-1]["p99_ms"],
+                         "saturated": sweep[-1]["offered_mpix_s"] > sweep[-1]["mpix_s"]}
+    if rank == 0:
+        print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
 

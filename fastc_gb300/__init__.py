@@ -7,12 +7,14 @@ runtime, and the seeded synthetic workloads.
 """
 from .bptc import (WATERMARK_CONTINUE, BC7Error, BlockMode, CompressionJob, CompressionJobList, CompressionSettings,
                    ErrorMetric, Plan, compress, compress_atomic, compress_image_data, compress_jobs,
+                   compress_with_stats,
                    decompress, psnr, get_engine, get_launch_shape, get_watermark_counter, set_engine,
                    set_launch_shape, set_watermark_counter, ENGINE_PIPELINE, ENGINE_WARP_PER_BLOCK)
 
 __all__ = [
     "BC7Error", "BlockMode", "CompressionJob", "CompressionJobList", "CompressionSettings",
     "ErrorMetric", "Plan", "compress", "compress_atomic", "compress_image_data", "compress_jobs",
+    "compress_with_stats",
     "decompress", "psnr", "get_launch_shape", "set_launch_shape", "WATERMARK_CONTINUE",
     "get_watermark_counter", "set_watermark_counter", "get_engine", "set_engine",
     "ENGINE_PIPELINE", "ENGINE_WARP_PER_BLOCK",

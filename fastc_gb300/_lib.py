@@ -61,6 +61,13 @@ class LogicalBlock(C.Structure):
     ]
 
 
+class BlockStats(C.Structure):
+    """fastc_bc7_block_stats: what CompressWithStats logs for one block."""
+    _fields_ = [("path", C.c_int32), ("mode", C.c_int32), ("estimate", C.c_double * 8),
+                ("error", C.c_double * 8), ("n_two", C.c_int32), ("n_three", C.c_int32),
+                ("two_shape", C.c_double * 64), ("three_shape", C.c_double * 64)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("memory_budget", C.c_size_t), ("max_inflight", C.c_uint32),
                 ("max_batch_blocks", C.c_uint32), ("max_batch_jobs", C.c_uint32), ("reserved", C.c_uint32)]
@@ -114,6 +121,9 @@ SIGNATURES = {
     "fastc_bc7_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fastc_bc7_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
     "fastc_bc7_server_destroy": (C.c_int, [C.c_void_p]),
+    "fastc_bc7_compress_stats": (C.c_int, [C.POINTER(Job), C.POINTER(Settings), C.c_void_p]),
+    "fastc_bc7_stats_log": (C.c_int, [C.POINTER(Job), C.c_void_p, C.c_char_p, C.c_size_t,
+                                      C.POINTER(C.c_size_t)]),
     "fastc_bc7_psnr": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                  C.POINTER(C.c_double), C.c_void_p]),
     "fastc_bc7_block_error_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,

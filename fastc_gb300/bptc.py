@@ -218,6 +218,29 @@ def compress_atomic(job_list: CompressionJobList, stream=None) -> None:
     compress_jobs(list(job_list), CompressionSettings(), stream)
 
 
+def compress_with_stats(job: CompressionJob, settings: Optional[CompressionSettings] = None) -> str:
+    """BPTCC::CompressWithStats (BPTCCompressor.h:173) with a log stream: the
+    logging encoder writes the job's blocks to job.out (host arrays) and
+    returns FasTC's log text for them (Compressor.cpp:1373-1389,
+    1938-2183). Its shape selection differs from compress()'s."""
+    if job.on_device:
+        raise BC7Error(_lib.ERR_INVALID_ARGUMENT, "compress_with_stats", "host buffers only")
+    lib = load()
+    cj = job.to_c()
+    n = int(lib.fastc_bc7_job_blocks(C.byref(cj)))
+    stats = (_lib.BlockStats * max(n, 1))()
+    s = (settings or CompressionSettings()).to_c()
+    check(lib.fastc_bc7_compress_stats(C.byref(cj), C.byref(s), C.cast(stats, C.c_void_p)),
+          "fastc_bc7_compress_stats")
+    size = C.c_size_t()
+    check(lib.fastc_bc7_stats_log(C.byref(cj), C.cast(stats, C.c_void_p), None, 0, C.byref(size)),
+          "fastc_bc7_stats_log")
+    buf = C.create_string_buffer(max(size.value, 1))
+    check(lib.fastc_bc7_stats_log(C.byref(cj), C.cast(stats, C.c_void_p), buf, size.value,
+                                  C.byref(size)), "fastc_bc7_stats_log")
+    return buf.raw[:size.value].decode()
+
+
 def compress_image_data(data, width: int, height: int,
                         settings: Optional[CompressionSettings] = None) -> np.ndarray:
     """CompressImageData (Core/include/FasTC/TexComp.h:81-88) for BC7:

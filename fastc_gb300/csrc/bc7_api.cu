@@ -11,6 +11,7 @@
 #include <utility>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -121,6 +122,7 @@ EncodeScratch carve_scratch(void *base, uint64_t total) {
   s.counter = reinterpret_cast<unsigned long long *>(p);
   s.status = reinterpret_cast<uint32_t *>(p + 8);
   s.singles = reinterpret_cast<uint32_t *>(p + 12);
+  s.carry = reinterpret_cast<uint32_t *>(p + 16);
   s.chunk_prefix = reinterpret_cast<uint32_t *>(p + 256);
   s.rank_local = reinterpret_cast<uint16_t *>(p + 256 + ((nchunks * 4 + 255) & ~255ull));
   return s;
@@ -158,13 +160,14 @@ uint32_t align_flags(const void *in, const void *out) {
 // carving the rank and pipeline scratch out of `scratch`.
 int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
                   LaunchShape shape, int task_bound, const ClassStreams *cls,
-                  const fastc::PipelineTuning &tune, cudaStream_t st) {
+                  const fastc::PipelineTuning &tune, cudaStream_t st,
+                  fastc_bc7_block_stats *stats, const fastc::ChunkEvents *events) {
   const EncodeScratch rank = carve_scratch(scratch, total);
-  if (engine == FASTC_BC7_ENGINE_PIPELINE) {
+  if (engine == FASTC_BC7_ENGINE_PIPELINE || stats) {
     void *pipe = static_cast<uint8_t *>(scratch) + rank_scratch_bytes(total);
     return fastc::launch_pipeline(jobs, njobs, total, rank, pipe,
                                   fastc::device_sm_count(current_device()), task_bound, cls, tune,
-                                  st);
+                                  st, stats, events);
   }
   return fastc::launch_encode(jobs, njobs, total, rank, shape, st);
 }
@@ -231,18 +234,40 @@ struct DevBuf {
 struct HostCtx {
   int device = -1;
   cudaStream_t stream = nullptr;
-  DevBuf in, out, jobs, scratch;
+  DevBuf in, out, jobs, scratch, stats;
   ClassStreams *cls = nullptr;
+  cudaStream_t copy = nullptr;      // host copies that overlap the encode
+  std::vector<cudaEvent_t> in_ev;   // chunk k's texels are on the device
+  std::vector<cudaEvent_t> out_ev;  // chunk k's blocks are written
+  cudaEvent_t copied = nullptr;     // the copy stream's work is done
 } g_host;
+
+// At least n events in each list of the host context.
+cudaError_t ensure_chunk_events(size_t n) {
+  for (std::vector<cudaEvent_t> *v : {&g_host.in_ev, &g_host.out_ev})
+    while (v->size() < n) {
+      cudaEvent_t e;
+      const cudaError_t ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+      if (ce != cudaSuccess) return ce;
+      v->push_back(e);
+    }
+  return cudaSuccess;
+}
 
 fastc_bc7_status host_ctx_init() {
   const int dev = current_device();
   if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
   if (g_host.device != dev) {
     if (g_host.stream) cudaStreamDestroy(g_host.stream);
+    if (g_host.copy) cudaStreamDestroy(g_host.copy);
+    for (cudaEvent_t e : g_host.in_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : g_host.out_ev) cudaEventDestroy(e);
+    if (g_host.copied) cudaEventDestroy(g_host.copied);
     if (g_host.cls) release_class_streams(g_host.device, g_host.cls);
     g_host = HostCtx();
     CK(cudaStreamCreateWithFlags(&g_host.stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&g_host.copy, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&g_host.copied, cudaEventDisableTiming));
     g_host.device = dev;
     g_host.cls = acquire_class_streams(dev);
   }
@@ -257,8 +282,9 @@ const fastc_bc7_settings &settings_for(const fastc_bc7_settings *s, int per_job,
 }
 
 // Host-memory batch: stage rows, launch, copy back. Caller holds g_mu.
+// `stats` (one job only): the logging encoder, its statistics copied there.
 fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7_settings *s,
-                          int per_job) {
+                          int per_job, fastc_bc7_block_stats *stats = nullptr) {
   fastc_bc7_settings dflt;
   fastc_bc7_settings_default(&dflt);
   std::vector<JobDev> dj(n);
@@ -296,34 +322,100 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
   CK(g_host.in.ensure(in_total));
   CK(g_host.out.ensure(out_total));
   CK(g_host.jobs.ensure(n * sizeof(JobDev)));
-  const int tb = task_bound_of(s, per_job, n);
-  CK(g_host.scratch.ensure(scratch_bytes(total, g_engine, tb)));
+  const int engine = stats ? FASTC_BC7_ENGINE_PIPELINE : g_engine;
+  const int tb = stats ? fastc::block_task_bound(settings_for(s, per_job, 0, dflt).block_modes, true)
+                       : task_bound_of(s, per_job, n);
+  CK(g_host.scratch.ensure(scratch_bytes(total, engine, tb)));
+  if (stats) CK(g_host.stats.ensure(total * sizeof(fastc_bc7_block_stats)));
   cudaStream_t cs = g_host.stream;
   uint8_t *din = static_cast<uint8_t *>(g_host.in.p);
   uint8_t *dout = static_cast<uint8_t *>(g_host.out.p);
   for (uint32_t i = 0; i < n; i++) {
     if (!dj[i].nblocks) continue;
-    const uint8_t *src = jobs[i].in + (size_t)dj[i].row0 * jobs[i].width * 4;
-    CK(cudaMemcpyAsync(din + in_off[i], src, in_bytes[i], cudaMemcpyHostToDevice, cs));
     dj[i].in = din + in_off[i];
     dj[i].out = dout + out_off[i];
     dj[i].flags |= fastc::kJobIn16 | fastc::kJobOut16;
   }
   CK(cudaMemcpyAsync(g_host.jobs.p, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs));
-  const EncodeScratch sc = carve_scratch(g_host.scratch.p, total);
-  const int le = launch_engine(static_cast<const JobDev *>(g_host.jobs.p), (int)n, total,
-                               g_host.scratch.p, g_engine, pick_shape(total), tb, g_host.cls, cs);
-  if (le) return fail_cuda((cudaError_t)le);
-  for (uint32_t i = 0; i < n; i++) {
-    if (!dj[i].nblocks) continue;
-    CK(cudaMemcpyAsync(jobs[i].out + (size_t)dj[i].first * 16, dout + out_off[i],
-                       (size_t)dj[i].nblocks * 16, cudaMemcpyDeviceToHost, cs));
+  // Texels go up on the copy stream in job order, chunk by chunk of the
+  // pipeline, so that chunk k starts once its own jobs are in while later
+  // ones are still copying; blocks come back the same way as each chunk is
+  // packed. (The warp-per-block engine encodes all blocks in one pass, so
+  // it takes everything first.) Overlap needs page-locked host buffers;
+  // with pageable ones each copy returns once staged, in the same order.
+  const bool chunked = engine == FASTC_BC7_ENGINE_PIPELINE;
+  const uint64_t cap = chunked ? fastc::pipeline_chunk(std::min(
+                                     tb, stats ? fastc::kMaxStatsBlockTasks : fastc::kMaxBlockTasks))
+                               : total;
+  const size_t nchunk = (size_t)((total + cap - 1) / cap);
+  CK(ensure_chunk_events(nchunk));
+  auto copy_in = [&](uint32_t i) -> cudaError_t {
+    if (!dj[i].nblocks) return cudaSuccess;
+    const uint8_t *src = jobs[i].in + (size_t)dj[i].row0 * jobs[i].width * 4;
+    return cudaMemcpyAsync(din + in_off[i], src, in_bytes[i], cudaMemcpyHostToDevice, g_host.copy);
+  };
+  auto copy_out = [&](uint32_t i) -> cudaError_t {
+    if (!dj[i].nblocks) return cudaSuccess;
+    return cudaMemcpyAsync(jobs[i].out + (size_t)dj[i].first * 16, dout + out_off[i],
+                           (size_t)dj[i].nblocks * 16, cudaMemcpyDeviceToHost, g_host.copy);
+  };
+  {
+    uint32_t next = 0;
+    for (size_t k = 0; k < nchunk; k++) {
+      const uint64_t end = (k + 1) * cap;
+      while (next < n && dj[next].begin < end) CK(copy_in(next++));
+      CK(cudaEventRecord(g_host.in_ev[k], g_host.copy));
+    }
   }
-  uint32_t singles = 0;
+  if (!chunked) CK(cudaStreamWaitEvent(cs, g_host.in_ev[nchunk - 1], 0));
+  const EncodeScratch sc = carve_scratch(g_host.scratch.p, total);
+  fastc_bc7_block_stats *dstats =
+      static_cast<fastc_bc7_block_stats *>(stats ? g_host.stats.p : nullptr);
+  fastc::ChunkEvents ev;
+  ev.in_ready = g_host.in_ev.data();
+  ev.packed = g_host.out_ev.data();
+  ev.count = (int)nchunk;
+  const int le = launch_engine(static_cast<const JobDev *>(g_host.jobs.p), (int)n, total,
+                               g_host.scratch.p, engine, pick_shape(total), tb, g_host.cls,
+                               fastc::PipelineTuning{}, cs, dstats, chunked ? &ev : nullptr);
+  if (le) return fail_cuda((cudaError_t)le);
+  if (chunked) {
+    uint32_t next = 0;
+    for (size_t k = 0; k < nchunk; k++) {
+      const uint64_t end = k + 1 == nchunk ? total : (k + 1) * cap;
+      CK(cudaStreamWaitEvent(g_host.copy, g_host.out_ev[k], 0));
+      while (next < n && dj[next].begin + dj[next].nblocks <= end) CK(copy_out(next++));
+    }
+  } else {
+    CK(cudaEventRecord(g_host.out_ev[0], cs));
+    CK(cudaStreamWaitEvent(g_host.copy, g_host.out_ev[0], 0));
+    for (uint32_t i = 0; i < n; i++) CK(copy_out(i));
+  }
+  CK(cudaEventRecord(g_host.copied, g_host.copy));
+  CK(cudaStreamWaitEvent(cs, g_host.copied, 0));
+  if (stats)
+    CK(cudaMemcpyAsync(stats, dstats, total * sizeof(fastc_bc7_block_stats),
+                       cudaMemcpyDeviceToHost, cs));
+  uint32_t singles = 0, status = 0;
   if (any_continue)
     CK(cudaMemcpyAsync(&singles, sc.singles, sizeof(singles), cudaMemcpyDeviceToHost, cs));
+  CK(cudaMemcpyAsync(&status, sc.status, sizeof(status), cudaMemcpyDeviceToHost, cs));
   CK(cudaStreamSynchronize(cs));
+  if (status & 2u) {  // the task-overflow status bit (bc7_block.cuh)
+    // a block needed more cluster fits than the scratch was sized for; its
+    // bytes are not FasTC's (never expected: the bound is computed above)
+    t_last_error = "a block needed more cluster fits than the launch's task bound";
+    return FASTC_BC7_ERR_INTERNAL;
+  }
   if (any_continue) g_wm_next = (uint32_t)((g_wm_next + (uint64_t)singles) % 9u);
+  if (stats) {
+    // the mode written: the unary mode prefix of the block (CP:1096-1298)
+    const uint8_t *blk = jobs[0].out + (size_t)dj[0].first * 16;
+    for (uint64_t b = 0; b < total; b++) {
+      const uint8_t m0 = blk[16 * b];
+      stats[b].mode = m0 ? __builtin_ctz(m0) : 8;
+    }
+  }
   return FASTC_BC7_OK;
 }
 
@@ -433,6 +525,54 @@ fastc_bc7_status fastc_bc7_compress(const fastc_bc7_job *job, const fastc_bc7_se
   if (!job) return FASTC_BC7_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(g_mu);
   return run_host(job, 1, s, 0);
+}
+
+fastc_bc7_status fastc_bc7_compress_stats(const fastc_bc7_job *job, const fastc_bc7_settings *s,
+                                          fastc_bc7_block_stats *stats) {
+  if (!job || !stats) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(g_mu);
+  return run_host(job, 1, s, 0, stats);
+}
+
+fastc_bc7_status fastc_bc7_stats_log(const fastc_bc7_job *job, const fastc_bc7_block_stats *stats,
+                                     char *buf, size_t cap, size_t *len) {
+  if (!job || !len || (cap && !buf)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  uint32_t first, count;
+  if (!job_range(*job, &first, &count)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  if (count && !stats) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  static const char *const kNames[8] = {"Zero", "One", "Two", "Three",
+                                        "Four", "Five", "Six", "Seven"};
+  std::string out;
+  char line[128];
+  auto put_d = [&](uint64_t idx, const char *name, double v) {
+    const int k = std::snprintf(line, sizeof(line), "%llu: BlockStat_%s -- %g\n",
+                                (unsigned long long)idx, name, v);
+    out.append(line, (size_t)k);
+  };
+  auto put_i = [&](uint64_t idx, const char *name, int v) {
+    const int k = std::snprintf(line, sizeof(line), "%llu: BlockStat_%s -- %d\n",
+                                (unsigned long long)idx, name, v);
+    out.append(line, (size_t)k);
+  };
+  char nm[64];
+  for (uint32_t b = 0; b < count; b++) {
+    const fastc_bc7_block_stats &st = stats[b];
+    const uint64_t idx = (uint64_t)first + b;
+    for (int k = 0; k < st.n_two && k < 64; k++) put_d(idx, "TwoShapeEstimate", st.two_shape[k]);
+    for (int k = 0; k < st.n_three && k < 64; k++)
+      put_d(idx, "ThreeShapeEstimate", st.three_shape[k]);
+    put_i(idx, "Path", st.path);
+    put_i(idx, "Mode", st.mode);
+    for (int m = 0; m < 8; m++) {
+      std::snprintf(nm, sizeof(nm), "Mode%sEstimate", kNames[m]);
+      put_d(idx, nm, st.estimate[m]);
+      std::snprintf(nm, sizeof(nm), "Mode%sError", kNames[m]);
+      put_d(idx, nm, st.error[m]);
+    }
+  }
+  *len = out.size();
+  if (cap) std::memcpy(buf, out.data(), out.size() < cap ? out.size() : cap);
+  return FASTC_BC7_OK;
 }
 
 fastc_bc7_status fastc_bc7_compress_batch(const fastc_bc7_job *jobs, uint32_t n,

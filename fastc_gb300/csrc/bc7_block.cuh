@@ -56,7 +56,7 @@ __device__ inline double estimate_shape(const uint32_t *px, uint32_t part, int n
 #pragma unroll
     for (int k = 0; k < 4; k++) v[k] = __fsub_rn(c.mx[k], c.mn[k]);
     double e = 0.0;
-    if (dot4(v, v) != 0.0f) {
+    if (sqlen4(v) != 0.0f) {
       e = 0.0001;
       e = e + (double)quantized_error(c, c.mn, c.mx, bits, 0xFFFFFFFFu, w, -1, nullptr);
     }

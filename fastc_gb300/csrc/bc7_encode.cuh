@@ -42,8 +42,17 @@ __device__ __forceinline__ float dot4(const float *a, const float *b) {
   return s;
 }
 
+// dot4(a, a) without its leading 0 + a0 * a0: a square is never -0, so
+// adding it to +0 gives it back exactly and the sum is the same float.
+__device__ __forceinline__ float sqlen4(const float *a) {
+  float s = __fmul_rn(a[0], a[0]);
+#pragma unroll
+  for (int i = 1; i < 4; i++) s = __fadd_rn(s, __fmul_rn(a[i], a[i]));
+  return s;
+}
+
 __device__ __forceinline__ float length4(const float *a) {
-  return __fsqrt_rn(dot4(a, a));
+  return __fsqrt_rn(sqlen4(a));
 }
 
 __device__ __forceinline__ void normalize4(float *a) {
@@ -281,7 +290,7 @@ __device__ inline float quantized_error(const Cluster &c, const float *p1, const
     d[k] = __fsub_rn(u1[k], u2[k]);
     dir[k] = __fsub_rn(u2[k], u1[k]);
   }
-  const float lsq = dot4(d, d);
+  const float lsq = sqlen4(d);
   float total = 0.0f;
   if (lsq == 0.0f) {
     for (int i = 0; i < c.n; i++) {
@@ -292,7 +301,7 @@ __device__ inline float quantized_error(const Cluster &c, const float *p1, const
         const uint32_t ip = (q1 >> (8 * k)) & 0xFF;
         ev[k] = __fmul_rn((float)sad8(e >> (8 * k), ip), w[k]);
       }
-      total = __fadd_rn(total, dot4(ev, ev));
+      total = __fadd_rn(total, sqlen4(ev));
       if (idx) set_nib(*idx, cl_texel(c, i), 0);
     }
     return total;
@@ -321,7 +330,7 @@ __device__ inline float quantized_error(const Cluster &c, const float *p1, const
         const uint32_t ip = ((a * w0 + b * w1 + 32u) >> 6) & 0xFF;
         ev[k] = __fmul_rn((float)sad8(epx >> (8 * k), ip), w[k]);
       }
-      const float err = dot4(ev, ev);
+      const float err = sqlen4(ev);
       if (err < min_err) {
         min_err = err;
         best = (uint32_t)j;
@@ -777,8 +786,17 @@ __device__ __forceinline__ uint32_t cl_packed(const Cluster &c, int k) {
 // QuantizedError. With kNB a constant the level loops unroll and the k-means
 // levels stay in registers; the members' per-level sums are exact integers
 // (sums of at most 16 bytes), so they are accumulated as integers, which
-// equals FasTC's float sums.
-template <int kNB>
+// equals FasTC's float sums. kSmemAcc: the per-level sums live in the
+// thread's palette scratch (ka_level) instead of registers, one
+// read-modify-write per point instead of a predicated add per level.
+// Level j's sum in the thread's own palette slots (the 8 uint4 words
+// m.pal[k * kLaneStride], two 64-bit halves each), which no other thread
+// touches.
+__device__ __forceinline__ uint64_t &ka_level(const ModeCtx &m, int j) {
+  return reinterpret_cast<uint64_t *>(m.pal + (j >> 1) * kLaneStride)[j & 1];
+}
+
+template <int kNB, bool kSmemAcc = false>
 __device__ inline void fit_rgb_setup_t(ModeCtx &m, const Cluster &c, FitSetup &st) {
   float *p1 = st.p1, *p2 = st.p2;
   uint64_t &idx = st.idx;
@@ -831,9 +849,14 @@ __device__ inline void fit_rgb_setup_t(ModeCtx &m, const Cluster &c, FitSetup &s
       break;
     }
     // per level: channel sums in 13-bit fields, member count from bit 52
-    uint64_t acc[kNB];
+    uint64_t acc[kSmemAcc ? 1 : kNB];
+    if constexpr (kSmemAcc) {
+#pragma unroll
+      for (int j = 0; j < nb; j++) ka_level(m, j) = 0;
+    } else {
 #pragma unroll kUnroll
-    for (int j = 0; j < nb; j++) acc[j] = 0;
+      for (int j = 0; j < nb; j++) acc[j] = 0;
+    }
     for (int i = 0; i < c.n; i++) {
       float p[4];
       cl_point(c, i, p);
@@ -844,7 +867,7 @@ __device__ inline void fit_rgb_setup_t(ModeCtx &m, const Cluster &c, FitSetup &s
         float v[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) v[k] = __fsub_rn(p[k], pts[j][k]);
-        const float d = dot4(v, v);
+        const float d = sqlen4(v);
         if (d < mind) {
           mind = d;
           minb = j;
@@ -854,17 +877,22 @@ __device__ inline void fit_rgb_setup_t(ModeCtx &m, const Cluster &c, FitSetup &s
       const uint64_t add = (uint64_t)(q & 0xFF) | ((uint64_t)((q >> 8) & 0xFF) << 13) |
                            ((uint64_t)((q >> 16) & 0xFF) << 26) | ((uint64_t)(q >> 24) << 39) |
                            (1ull << 52);
+      if constexpr (kSmemAcc) {
+        ka_level(m, minb) += add;
+      } else {
 #pragma unroll
-      for (int j = 0; j < nb; j++) acc[j] += j == minb ? add : 0ull;
+        for (int j = 0; j < nb; j++) acc[j] += j == minb ? add : 0ull;
+      }
     }
     fixed = true;
 #pragma unroll kUnroll
     for (int j = 0; j < nb; j++) {
-      const uint32_t cnt = (uint32_t)(acc[j] >> 52);
+      const uint64_t aj = kSmemAcc ? ka_level(m, j) : acc[j];
+      const uint32_t cnt = (uint32_t)(aj >> 52);
       float np[4];
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        np[k] = (float)(uint32_t)((acc[j] >> (13 * k)) & 0x1FFFu);
+        np[k] = (float)(uint32_t)((aj >> (13 * k)) & 0x1FFFu);
         if (cnt) np[k] = __fdiv_rn(np[k], (float)cnt);
       }
       npts[j] = cnt;
@@ -1035,7 +1063,7 @@ __device__ inline double fit_alpha(ModeCtx &m, const Cluster &c, const uint32_t 
 // The separate-alpha fit up to the colour fit's annealing: the colour part
 // in `st` (rotated cluster, CP:664-701), the alpha part complete. kNB: the
 // colour and alpha palette sizes (0: from the mode context).
-template <int kNB = 0, int kANB = 0>
+template <int kNB = 0, int kANB = 0, bool kSmemAcc = false>
 __device__ inline void fit_alpha_setup(ModeCtx &m, const Cluster &c, const uint32_t *opt6,
                                 FitSetup &st, float &a1, float &a2, uint64_t &aidx,
                                 double &aerr) {
@@ -1053,7 +1081,7 @@ __device__ inline void fit_alpha_setup(ModeCtx &m, const Cluster &c, const uint3
   st.idx = 0;
   st.pbit = 0;
   if constexpr (kNB > 0) {
-    fit_rgb_setup_t<kNB>(m, rgb, st);
+    fit_rgb_setup_t<kNB, kSmemAcc>(m, rgb, st);
     alpha_fit_t<kANB>(m, c, ch, amin, amax, opt6, a1, a2, aidx, aerr);
   } else {
     fit_rgb_setup(m, rgb, st);

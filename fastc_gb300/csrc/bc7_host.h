@@ -50,9 +50,12 @@ uint32_t align_flags(const void *in, const void *out);
 // `cls`: side streams for the pipeline engine's classes (null: one stream).
 int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
                   LaunchShape shape, int task_bound, const ClassStreams *cls, cudaStream_t st);
+// `stats` not null: the logging encoder of CompressWithStats (pipeline
+// engine only).
 int launch_engine(const JobDev *jobs, int njobs, uint64_t total, void *scratch, int engine,
                   LaunchShape shape, int task_bound, const ClassStreams *cls,
-                  const PipelineTuning &tune, cudaStream_t st);
+                  const PipelineTuning &tune, cudaStream_t st,
+                  fastc_bc7_block_stats *stats = nullptr, const ChunkEvents *events = nullptr);
 // Side-stream sets for callers without their own: taken for one enqueue
 // and given back (per device; created on first need).
 ClassStreams *acquire_class_streams(int device);

@@ -204,12 +204,14 @@ __device__ __forceinline__ void store_block(const JobDev &jb, uint32_t lin, cons
 // 1+2. Single-colour watermark ranks
 // ---------------------------------------------------------------------------
 
+// CTA b ranks the blocks of rank chunk r0 + b.
 __global__ void __launch_bounds__(kRankChunk) classify_kernel(const JobDev *jobs, int njobs,
                                                               uint64_t total,
                                                               uint16_t *rank_local,
-                                                              uint32_t *chunk_total) {
+                                                              uint32_t *chunk_total, uint32_t r0) {
   __shared__ uint32_t s_warp[32];
-  const uint64_t g = (uint64_t)blockIdx.x * kRankChunk + threadIdx.x;
+  const uint32_t rc = r0 + blockIdx.x;
+  const uint64_t g = (uint64_t)rc * kRankChunk + threadIdx.x;
   bool same = false;
   if (g < total) {
     const JobDev &jb = jobs[find_job(jobs, njobs, g)];
@@ -235,11 +237,63 @@ __global__ void __launch_bounds__(kRankChunk) classify_kernel(const JobDev *jobs
       if (lane >= o) incl += t;
     }
     s_warp[lane] = incl - v;
-    if (lane == 31) chunk_total[blockIdx.x] = incl;
+    if (lane == 31) chunk_total[rc] = incl;
   }
   __syncthreads();
   if (g < total)
     rank_local[g] = (uint16_t)(s_warp[wid] + __popc(bal & ((1u << lane) - 1u)));
+}
+
+// Exclusive scan of the chunk counts [r0, r1) in place, continuing from
+// *carry (the single-colour blocks before chunk r0; r0 == 0 starts from 0
+// and resets the work counter and status); leaves the running total in
+// *carry and in *singles. One CTA.
+__global__ void __launch_bounds__(1024) scan_range_kernel(uint32_t *chunk, uint32_t r0, uint32_t r1,
+                                                          uint32_t *carry, unsigned long long *counter,
+                                                          uint32_t *status, uint32_t *singles) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_carry;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    s_carry = r0 == 0 ? 0u : *carry;
+    if (r0 == 0) {
+      *counter = 0ull;
+      *status = 0u;
+    }
+  }
+  __syncthreads();
+  for (uint32_t base = r0; base < r1; base += 1024) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < r1 ? chunk[i] : 0u;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_warp[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      const uint32_t w = s_warp[lane];
+      uint32_t wi = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+        if (lane >= o) wi += t;
+      }
+      s_warp[lane] = wi - w;
+    }
+    __syncthreads();
+    const uint32_t c = s_carry;
+    if (i < r1) chunk[i] = c + s_warp[wid] + incl - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) s_carry = c + s_warp[wid] + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *carry = s_carry;
+    *singles = s_carry;
+  }
 }
 
 // Exclusive scan of the chunk counts, in place; also resets the counter.
@@ -459,9 +513,22 @@ int launch_rank_prepass(const JobDev *jobs_dev, int njobs, uint64_t total,
   if (total == 0) return 0;
   const uint32_t nchunks = (uint32_t)((total + kRankChunk - 1) / kRankChunk);
   classify_kernel<<<nchunks, kRankChunk, 0, st>>>(jobs_dev, njobs, total, sc.rank_local,
-                                                  sc.chunk_prefix);
+                                                  sc.chunk_prefix, 0u);
   scan_kernel<<<1, 1024, 0, st>>>(sc.chunk_prefix, nchunks, sc.counter, sc.status,
                                   sc.singles);
+  return (int)cudaPeekAtLastError();
+}
+
+int launch_rank_prepass_range(const JobDev *jobs_dev, int njobs, uint64_t total, uint64_t g0,
+                              uint64_t g1, const EncodeScratch &sc, void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (g1 <= g0) return 0;
+  const uint32_t r0 = (uint32_t)(g0 / kRankChunk);
+  const uint32_t r1 = (uint32_t)((g1 + kRankChunk - 1) / kRankChunk);
+  classify_kernel<<<r1 - r0, kRankChunk, 0, st>>>(jobs_dev, njobs, total, sc.rank_local,
+                                                  sc.chunk_prefix, r0);
+  scan_range_kernel<<<1, 1024, 0, st>>>(sc.chunk_prefix, r0, r1, sc.carry, sc.counter, sc.status,
+                                        sc.singles);
   return (int)cudaPeekAtLastError();
 }
 

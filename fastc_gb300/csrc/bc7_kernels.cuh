@@ -37,6 +37,7 @@ struct EncodeScratch {
   unsigned long long *counter;  // work counter of the persistent kernel
   uint32_t *status;        // device-side status bits
   uint32_t *singles;       // single-colour blocks in the launch (written by the scan)
+  uint32_t *carry;         // running single-colour count of the ranged pre-pass
 };
 
 struct LaunchShape {
@@ -60,6 +61,13 @@ int launch_block_error(const uint8_t *blocks, const uint8_t *rgba, uint32_t widt
 // counter and status of `scratch`.
 int launch_rank_prepass(const JobDev *jobs_dev, int njobs, uint64_t total_blocks,
                         const EncodeScratch &scratch, void *stream);
+// The same for the blocks [g0, g1) of the launch only, continuing the
+// ranks of the blocks before g0 (ranked by earlier calls in order on the
+// same stream); g0 a multiple of kRankChunk, and the call with g0 == 0
+// resets the counter and status. Lets a caller rank each piece of a launch
+// once its texels have arrived.
+int launch_rank_prepass_range(const JobDev *jobs_dev, int njobs, uint64_t total_blocks,
+                              uint64_t g0, uint64_t g1, const EncodeScratch &scratch, void *stream);
 // Resident CTAs per SM of the encoder with this many warps per CTA.
 int encode_ctas_per_sm(int warps_per_cta);
 

@@ -490,11 +490,207 @@ __device__ __forceinline__ Selection box_selection_pipe(const uint32_t *px,
   return r;
 }
 
-template <int kWarps>
+// ---------------------------------------------------------------------------
+// The logging encoder's shape search (CompressWithStats with a log stream,
+// CP:1862-1936, 2046-2166), with the statistics it logs
+// ---------------------------------------------------------------------------
+
+// EstimateTwoClusterErrorStats / EstimateThreeClusterErrorStats
+// (CP:1862-1928) for subset ci of a shape: the subset's bounding box
+// quantised with the colour grids of two modes (1 and 3, or 0 and 2), each
+// error the estimate of its mode; the subset adds 0.0001 + the smaller.
+__device__ __noinline__ double stats_subset(const uint32_t *px, uint32_t part, int ci, bool three,
+                                            int metric, double &e0, double &e1) {
+  Cluster c;
+  uint32_t buf[16];
+  make_cluster(px, part, ci, buf, 1, c);
+  float v[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) v[k] = __fsub_rn(c.mx[k], c.mn[k]);
+  if (sqlen4(v) == 0.0f) {
+    e0 = e1 = 0.0;
+    return 0.0;
+  }
+  float w[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) w[k] = base_weight(metric, k);
+  const int bits = three ? 2 : 3;
+  const uint32_t m0 = three ? 0xFFF0F0F0u : 0xFFFCFCFCu;
+  const uint32_t m1 = three ? 0xFFF8F8F8u : 0xFFFEFEFEu;
+  const double bias = three ? 0.0001 : 0.0;
+  e0 = bias + (double)quantized_error(c, c.mn, c.mx, bits, m0, w, -1, nullptr);
+  e1 = bias + (double)quantized_error(c, c.mn, c.mx, bits, m1, w, -1, nullptr);
+  double err = 0.0001;
+  err += e0 < e1 ? e0 : e1;
+  return err;
+}
+
+__device__ __forceinline__ double warp_min_double(double v) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v = fmin(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  return v;
+}
+
+// One shape loop of the logging encoder (CP:2066-2114 with nsub 2,
+// 2118-2166 with nsub 3), shapes `lane` and `lane + 32` on this lane. The
+// loop stops after the first shape whose estimate is below 1e-9; over the
+// shapes up to there it records each estimate below all before it (the
+// last of them is the shape chosen) and keeps the least of each mode's
+// summed estimates. Returns the chosen shape; `exact` is set on the stop.
+template <int kNSub>
+__device__ int stats_shapes(const uint32_t *px, const uint32_t *part, int metric, int lane,
+                            fastc_bc7_block_stats *st, double &est_a, double &est_b, bool &exact) {
+  constexpr bool kThree = kNSub == 3;
+  double err[2], acc[2][2];
+#pragma unroll 1
+  for (int h = 0; h < 2; h++) {
+    const uint32_t pw = part[lane + 32 * h];
+    double e = 0.0, a0 = 0.0, a1 = 0.0;
+#pragma unroll 1
+    for (int ci = 0; ci < kNSub; ci++) {
+      double e0, e1;
+      e += stats_subset(px, pw, ci, kThree, metric, e0, e1);
+      a0 = ci == 0 ? e0 : a0 + e0;
+      a1 = ci == 0 ? e1 : a1 + e1;
+    }
+    err[h] = e;
+    acc[h][0] = a0;
+    acc[h][1] = a1;
+  }
+  const uint64_t z = (uint64_t)__ballot_sync(0xFFFFFFFFu, err[0] < 1e-9) |
+                     ((uint64_t)__ballot_sync(0xFFFFFFFFu, err[1] < 1e-9) << 32);
+  const int last = z ? __ffsll((long long)z) - 1 : 63;  // last shape the loop visits
+  exact = z != 0;
+  // exclusive prefix minimum of the estimates in shape order
+  double incl[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    double v = err[h];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+      if (lane >= o) v = fmin(v, t);
+    }
+    incl[h] = v;
+  }
+  const double min0 = __shfl_sync(0xFFFFFFFFu, incl[0], 31);
+  incl[1] = fmin(incl[1], min0);
+  double excl[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const double t = __shfl_up_sync(0xFFFFFFFFu, incl[h], 1);
+    excl[h] = lane > 0 ? t : (h == 0 ? DBL_MAX : min0);
+  }
+  bool rec[2];
+  double ea = DBL_MAX, eb = DBL_MAX;
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int sh = lane + 32 * h;
+    const bool in = sh <= last;
+    rec[h] = in && err[h] < excl[h];
+    if (in) {
+      ea = fmin(ea, acc[h][0]);
+      eb = fmin(eb, acc[h][1]);
+    }
+  }
+  est_a = warp_min_double(ea);
+  est_b = warp_min_double(eb);
+  const uint32_t r0 = __ballot_sync(0xFFFFFFFFu, rec[0]), r1 = __ballot_sync(0xFFFFFFFFu, rec[1]);
+  const uint32_t below = (1u << lane) - 1u;
+  double *list = kThree ? st->three_shape : st->two_shape;
+  if (rec[0]) list[__popc(r0 & below)] = err[0];
+  if (rec[1]) list[__popc(r0) + __popc(r1 & below)] = err[1];
+  if (lane == 0) {
+    if (kThree) st->n_three = __popc(r0) + __popc(r1);
+    else st->n_two = __popc(r0) + __popc(r1);
+  }
+  return r1 ? 32 + 31 - __clz((int)r1) : 31 - __clz((int)r0);
+}
+
+// CompressBC7Block with a BlockLogger (CP:1938-2183) up to the cluster
+// fits, for a block that is neither one colour nor fully transparent: the
+// selection and the statistics (path, per-mode estimates, improving shape
+// estimates; the errors stay -1).
+__device__ Selection box_selection_stats(const uint32_t *px, const uint32_t *part2,
+                                         const uint32_t *part3, int metric, int lane,
+                                         fastc_bc7_block_stats *st) {
+  bool opaque = true;
+  for (int i = 0; i < 16; i++) opaque = opaque && (px[i] >> 24) == 255u;
+  // mode 6's estimate: the whole block's box, 4 buckets (CP:2046-2058)
+  double est6;
+  {
+    Cluster c;
+    uint32_t buf[16];
+    make_cluster(px, 0u, 0, buf, 1, c);
+    float v[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = __fsub_rn(c.mx[k], c.mn[k]);
+    if (sqlen4(v) == 0.0f) {
+      est6 = 0.0;
+    } else {
+      float w[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) w[k] = base_weight(metric, k);
+      est6 = 0.0001 + (double)quantized_error(c, c.mn, c.mx, 2, 0xFEFEFEFEu, w, -1, nullptr);
+    }
+  }
+  Selection r;
+  r.nshapes = opaque ? 2 : 1;
+  r.nparts[0] = 2;
+  r.nparts[1] = opaque ? 3 : 0;
+  r.shape[1] = 0;
+  r.modes = 0xFF;
+  double e1, e3, e0 = -1.0, e2 = -1.0;
+  bool exact;
+  r.shape[0] = (uint32_t)stats_shapes<2>(px, part2, metric, lane, st, e1, e3, exact);
+  int path = 3;
+  if (exact) {
+    r.modes = kModesTwo;
+    path = 2;
+  }
+  if (opaque) {
+    r.shape[1] = (uint32_t)stats_shapes<3>(px, part3, metric, lane, st, e0, e2, exact);
+    if (exact) {
+      r.modes = kModesThree;
+      path = 2;
+    }
+  } else if (lane == 0) {
+    st->n_three = 0;
+  }
+  if (lane < 8) {
+    const double v = lane == 0 ? e0 : lane == 1 ? e1 : lane == 2 ? e2 : lane == 3 ? e3
+                     : lane == 6 ? est6 : -1.0;
+    st->estimate[lane] = v;
+    st->error[lane] = -1.0;
+  }
+  if (lane == 0) {
+    st->path = path;
+    st->mode = -1;
+  }
+  return r;
+}
+
+// A one-colour or transparent block's statistics (CP:1938-1960).
+__device__ __forceinline__ void trivial_stats(fastc_bc7_block_stats *st, int lane, int path) {
+  if (lane < 8) {
+    st->estimate[lane] = -1.0;
+    st->error[lane] = -1.0;
+  }
+  if (lane == 0) {
+    st->path = path;
+    st->mode = path == 0 ? 5 : 6;
+    st->n_two = st->n_three = 0;
+  }
+}
+
+// kStats: the logging encoder's selection, with its statistics written to
+// stats[global block index].
+template <int kWarps, bool kStats>
 __global__ void __launch_bounds__(kWarps * 32) select_kernel(
     const JobDev *__restrict__ jobs, int njobs, uint64_t c0, uint32_t nb,
     const uint16_t *__restrict__ rank_local, const uint32_t *__restrict__ rank_chunk,
-    BlockSel *__restrict__ sel, uint8_t *__restrict__ counts, int task_bound, uint32_t *status) {
+    BlockSel *__restrict__ sel, uint8_t *__restrict__ counts, int task_bound, uint32_t *status,
+    fastc_bc7_block_stats *__restrict__ stats) {
   static_assert(kWarps * 32 == kLaneStride, "shared arrays use the lane stride");
   __shared__ uint32_t s_part2[64], s_part3[64];
   __shared__ uint32_t s_px[kWarps][16];
@@ -533,6 +729,7 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
     bs.done = 1;
     bs.pad[0] = bs.pad[1] = bs.pad[2] = 0;
     if (same || transparent) {
+      if (kStats) trivial_stats(stats + g, lane, same ? 0 : 1);
       if (lane < kClasses) counts[(uint64_t)lane * nb + gl] = 0;
       if (lane == 0) {
         uint32_t out[4];
@@ -553,8 +750,10 @@ __global__ void __launch_bounds__(kWarps * 32) select_kernel(
       __syncwarp();
       continue;
     }
-    const Selection s = box_selection_pipe(px, s_part2, s_part3, (int)jb.metric, lane,
-                                           s_pal + threadIdx.x, s_est[wid]);
+    const Selection s =
+        kStats ? box_selection_stats(px, s_part2, s_part3, (int)jb.metric, lane, stats + g)
+               : box_selection_pipe(px, s_part2, s_part3, (int)jb.metric, lane,
+                                    s_pal + threadIdx.x, s_est[wid]);
     uint32_t modes = s.modes & jb.modes;
     if (modes == 0) modes = jb.modes & 0xFF;  // FasTC: undefined behaviour
     const int c = lane < kClasses ? class_task_count(s, modes, lane) : 0;
@@ -769,9 +968,9 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 3 : 6)) s
     constexpr int kNB = 1 << (class_im(C) ? kA.alpha_idx_bits : kA.idx_bits);
     constexpr int kANB = 1 << (class_im(C) ? kA.idx_bits : kA.alpha_idx_bits);
     if constexpr (kA.has_rotation != 0) {
-      fit_alpha_setup<kNB, kANB>(m, c, q_opt6, st, o.a1, o.a2, o.aidx, o.aerr);
+      fit_alpha_setup<kNB, kANB, (kNB >= 8)>(m, c, q_opt6, st, o.a1, o.a2, o.aidx, o.aerr);
     } else {
-      fit_rgb_setup_t<kNB>(m, c, st);
+      fit_rgb_setup_t<kNB, (kNB >= 8)>(m, c, st);
     }
     o.err = st.err;
     o.idx = st.idx;
@@ -973,7 +1172,7 @@ __device__ __forceinline__ float texel_err(uint32_t e, uint32_t pal, const float
     float ev[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) ev[c] = __fmul_rn((float)((ad >> (8 * c)) & 0xFF), w[c]);
-    return dot4(ev, ev);
+    return sqlen4(ev);
   }
 }
 
@@ -1673,16 +1872,21 @@ ChunkBuf carve_chunk(uint8_t *p, uint64_t nb, int tb, int sm_count) {
 
 }  // namespace
 
-int block_task_bound(uint32_t modes) {
+int block_task_bound(uint32_t modes, bool stats) {
   modes &= 0xFFu;
   // BoxSelection's outcomes (CP:1670-1750): opaque blocks search two shape
   // slots (2 and 3 subsets) with modes 4 and 5 removed, or one slot's modes
   // after an exact fit; other blocks one 2-subset slot with the alpha modes.
+  // The logging encoder's (CP:2046-2166): every mode, on two slots for
+  // opaque blocks and one for the others, or the exact fit's modes.
   struct Outcome { uint32_t modes; int nshapes; };
-  const Outcome outs[4] = {{0xFFu & ~((1u << 4) | (1u << 5)), 2}, {kModesTwo, 1}, {kModesThree, 2},
-                           {kModesAlpha, 1}};
+  const Outcome plain[4] = {{0xFFu & ~((1u << 4) | (1u << 5)), 2}, {kModesTwo, 1},
+                            {kModesThree, 2}, {kModesAlpha, 1}};
+  const Outcome logged[4] = {{0xFFu, 2}, {kModesTwo, 2}, {kModesThree, 2}, {0xFFu, 1}};
+  const Outcome *outs = stats ? logged : plain;
   int worst = 0;
-  for (const Outcome &o : outs) {
+  for (int oi = 0; oi < 4; oi++) {
+    const Outcome &o = outs[oi];
     uint32_t m = o.modes & modes;
     if (m == 0) m = modes;  // the fallback to the caller's mask
     int n = 0;
@@ -1868,12 +2072,13 @@ void reindex_all(const JobDev *jobs, const ChunkBuf &b, int sm_count, cudaStream
 // pack(i - 2), earlier on `st`.
 int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
                     void *scratch, int sm_count, int task_bound, const ClassStreams *cls,
-                    const PipelineTuning &tune, void *stream) {
+                    const PipelineTuning &tune, void *stream, fastc_bc7_block_stats *stats,
+                    const ChunkEvents *events) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (total == 0) return 0;
-  const int tb = task_bound < 1 ? 1 : (task_bound > kMaxBlockTasks ? kMaxBlockTasks : task_bound);
-  int e = launch_rank_prepass(jobs, njobs, total, rank, stream);
-  if (e) return e;
+  const int tmax = stats ? kMaxStatsBlockTasks : kMaxBlockTasks;
+  const int tb = task_bound < 1 ? 1 : (task_bound > tmax ? tmax : task_bound);
+  int e = 0;
   const uint64_t cap = pipeline_chunk(tb);
   const uint64_t nbmax = total < cap ? total : cap;
   ChunkBuf bufs[2];
@@ -1882,7 +2087,7 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
                                           chunk_buffer_bytes(nbmax, tb, sm_count),
                                       nbmax, tb, sm_count)
                         : bufs[0];
-  auto pack = [&](const ChunkBuf &b, uint32_t nb, int parity) -> int {
+  auto pack = [&](const ChunkBuf &b, uint32_t nb, int parity, int chunk) -> int {
     if (cls) {
       for (int c = 0; c < kClasses; c++) {
         const cudaError_t ce = cudaStreamWaitEvent(st, cls->join[parity][c], 0);
@@ -1894,6 +2099,10 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
                                                  b.rlist, b.rcap);
     reindex_all(jobs, b, sm_count, st);
     pack_kernel<<<ctas, kPackThreads, 0, st>>>(jobs, nb, b.sel, b.win, b.state);
+    if (events && events->packed && chunk < events->count) {
+      const cudaError_t ce = cudaEventRecord(events->packed[chunk], st);
+      if (ce != cudaSuccess) return (int)ce;
+    }
     return (int)cudaPeekAtLastError();
   };
   uint32_t prev_nb = 0;
@@ -1904,8 +2113,22 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     const uint64_t n8 = (uint64_t)kClasses * nb;
     const uint32_t nchunks = (uint32_t)((n8 + kRankChunk - 1) / kRankChunk);
     const int sel_ctas = (int)((nb + 3) / 4 < (uint64_t)sm_count * 16 ? (nb + 3) / 4 : (uint64_t)sm_count * 16);
-    select_kernel<4><<<sel_ctas, 128, 0, st>>>(jobs, njobs, c0, nb, rank.rank_local, rank.chunk_prefix,
-                                               b.sel, b.counts, tb, rank.status);
+    // the chunk's texels, then its single-colour ranks (continuing the
+    // earlier chunks'), before anything reads them
+    if (events && events->in_ready && i < events->count) {
+      const cudaError_t ce = cudaStreamWaitEvent(st, events->in_ready[i], 0);
+      if (ce != cudaSuccess) return (int)ce;
+    }
+    e = launch_rank_prepass_range(jobs, njobs, total, c0, c0 + nb, rank, stream);
+    if (e) return e;
+    if (stats)
+      select_kernel<4, true><<<sel_ctas, 128, 0, st>>>(jobs, njobs, c0, nb, rank.rank_local,
+                                                       rank.chunk_prefix, b.sel, b.counts, tb,
+                                                       rank.status, stats);
+    else
+      select_kernel<4, false><<<sel_ctas, 128, 0, st>>>(jobs, njobs, c0, nb, rank.rank_local,
+                                                        rank.chunk_prefix, b.sel, b.counts, tb,
+                                                        rank.status, nullptr);
     scan_local_u8_kernel<<<nchunks, kRankChunk, 0, st>>>(b.counts, n8, b.local, b.chunk);
     scan_chunks_kernel<<<1, 1024, 0, st>>>(b.chunk, nchunks, b.ctr);
     emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, b.counts, b.local, b.chunk, b.desc);
@@ -1939,21 +2162,21 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
         ce = cudaEventRecord(cls->join[par][c], side[c]);
       if (ce != cudaSuccess) return (int)ce;
       if (i > 0) {
-        e = pack(bufs[(i - 1) & 1], prev_nb, (i - 1) & 1);
+        e = pack(bufs[(i - 1) & 1], prev_nb, (i - 1) & 1, i - 1);
         if (e) return e;
       }
     } else {
       for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], false, args, st);
       launch_bound(args, st);
       for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], true, args, st);
-      e = pack(b, nb, 0);
+      e = pack(b, nb, 0, i);
       if (e) return e;
     }
     e = (int)cudaPeekAtLastError();
     if (e) return e;
     prev_nb = nb;
   }
-  if (cls) return pack(bufs[(i - 1) & 1], prev_nb, (i - 1) & 1);
+  if (cls) return pack(bufs[(i - 1) & 1], prev_nb, (i - 1) & 1, i - 1);
   return 0;
 }
 

@@ -6,6 +6,7 @@
 #include <cstdint>
 
 #include "bc7_kernels.cuh"
+#include "fastc_bc7.h"
 
 namespace fastc {
 
@@ -14,14 +15,22 @@ namespace fastc {
 // with all modes enabled it is 15 (block_task_bound() computes the bound of
 // a mask). Scratch is sized by the bound of the launch's masks.
 constexpr int kMaxBlockTasks = 32;
+// The logging encoder of CompressWithStats keeps modes 4 and 5 on for
+// opaque blocks, which then run once per shape slot: up to 38 fits (mode 4
+// 2 x 8, mode 5 2 x 4, mode 6 2, modes 0 and 2 3 each, modes 1, 3 and 7 2
+// each).
+constexpr int kMaxStatsBlockTasks = 38;
 // Blocks per pipeline chunk: scratch grows with chunk x task bound, and
 // longer annealing lists keep more lanes busy, so the chunk is larger when
 // the bound is small. Launches of more than one chunk use two scratch
 // buffers so that the select stage of a chunk runs while the previous chunk
 // anneals.
 constexpr uint64_t kChunkTaskBudget = 16ull * 1024 * 1024;  // chunk blocks x task bound
+// (a multiple of the watermark-rank chunk, so that each pipeline chunk
+// ranks its own blocks)
 __host__ __device__ constexpr uint64_t pipeline_chunk(int task_bound) {
-  return kChunkTaskBudget / (uint64_t)(task_bound > 16 ? 32 : 16);
+  return kChunkTaskBudget / (uint64_t)(task_bound > 32 ? 48 : (task_bound > 16 ? 32 : 16)) /
+         kRankChunk * kRankChunk;
 }
 
 // Per-block outcome of the select stage (16 bytes).
@@ -119,8 +128,9 @@ cudaError_t class_streams_create(ClassStreams *cs);
 void class_streams_destroy(ClassStreams *cs);
 
 void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t opt6[256]);
-// Most cluster fits a block can need when the caller enables `modes`.
-int block_task_bound(uint32_t modes);
+// Most cluster fits a block can need when the caller enables `modes`
+// (`stats`: under the logging encoder's shape selection).
+int block_task_bound(uint32_t modes, bool stats = false);
 // sm_count: of the device that runs the launch (bounds the continuation lists).
 size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound, int sm_count);
 // Launch parameters the plan autotuner chooses (defaults: measured best on
@@ -131,9 +141,24 @@ struct PipelineTuning {
 };
 
 // `cls` null: every stage runs in order on `stream`. `task_bound`: the most
-// block_task_bound() of the jobs' masks.
+// block_task_bound() of the jobs' masks. `stats` not null: the logging
+// encoder of CompressWithStats (its own shape selection), writing each
+// block's statistics to stats[global block index] (the mode is left to the
+// host, which reads it from the block).
+// Events a caller can place between the pipeline's chunks (chunk k covers
+// global blocks [k * pipeline_chunk(task_bound), ...)): before chunk k
+// reads any texel the caller's stream waits for in_ready[k]; packed[k] is
+// recorded on it once chunk k's blocks are written. Either array may be
+// null; `count` is their length (chunks past it take no event).
+struct ChunkEvents {
+  const cudaEvent_t *in_ready = nullptr;
+  const cudaEvent_t *packed = nullptr;
+  int count = 0;
+};
+
 int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeScratch &rank,
                     void *scratch, int sm_count, int task_bound, const ClassStreams *cls,
-                    const PipelineTuning &tune, void *stream);
+                    const PipelineTuning &tune, void *stream,
+                    fastc_bc7_block_stats *stats = nullptr, const ChunkEvents *events = nullptr);
 
 }  // namespace fastc

@@ -15,6 +15,8 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <ostream>
+#include <string>
 #include <vector>
 
 #include "FasTC/BPTCCompressor.h"
@@ -67,19 +69,31 @@ void Compress(const FasTC::CompressionJob &cj, CompressionSettings settings) {
 
 // BPTCCompressor.h:173. Without a log stream FasTC encodes each block as
 // Compress does (Compressor.cpp:1591-1596); with one it runs a logging
-// encoder that selects shapes differently (Compressor.cpp:1862-2183), which
-// is not provided. Its block loop runs to y <= YEnd with no clamp to
-// Height - 4 (Compressor.cpp:1583-1584, unlike Compress at :1478), so for a
-// job whose YEnd equals Height FasTC reads and writes one block row past
-// the buffers; here the range is clamped as Compress clamps it, and the
-// blocks written are those of Compress.
+// encoder that selects shapes differently (Compressor.cpp:1862-2183) and
+// writes each block's statistics to the stream: fastc_bc7_compress_stats
+// runs that encoder on the GPU and fastc_bc7_stats_log formats the same
+// text. Its block loop runs to y <= YEnd with no clamp to Height - 4
+// (Compressor.cpp:1583-1584, unlike Compress at :1478), so for a job whose
+// YEnd equals Height FasTC reads and writes one block row past the
+// buffers; here the range is clamped as Compress clamps it.
 void CompressWithStats(const FasTC::CompressionJob &cj, std::ostream *logStream,
                        CompressionSettings settings) {
   if (!logStream) {
     Compress(cj, settings);
     return;
   }
-  Die("BPTCC::CompressWithStats", FASTC_BC7_ERR_UNSUPPORTED);
+  const fastc_bc7_job j = ToC(cj);
+  const fastc_bc7_settings s = ToC(settings);
+  std::vector<fastc_bc7_block_stats> stats(fastc_bc7_job_blocks(&j) + 1);
+  fastc_bc7_status st = fastc_bc7_compress_stats(&j, &s, stats.data());
+  if (st != FASTC_BC7_OK) Die("BPTCC::CompressWithStats", st);
+  size_t len = 0;
+  st = fastc_bc7_stats_log(&j, stats.data(), nullptr, 0, &len);
+  if (st != FASTC_BC7_OK) Die("BPTCC::CompressWithStats", st);
+  std::string text(len, '\0');
+  st = fastc_bc7_stats_log(&j, stats.data(), &text[0], len, &len);
+  if (st != FASTC_BC7_OK) Die("BPTCC::CompressWithStats", st);
+  logStream->write(text.data(), (std::streamsize)text.size());
 }
 
 #ifdef HAS_ATOMICS

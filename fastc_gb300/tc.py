@@ -10,7 +10,8 @@ computed as FasTC's Image::ComputePSNR (alpha-premultiplied RGB, peak
 layout, a .png name the decoded image. -nd writes nothing; -n N repeats the
 compression and reports the time. Options that choose host threading (-t,
 -j, -a, -simd) are accepted and have no effect: the work is distributed on
-the GPU. -l (CompressWithStats) and formats other than BPTC are refused.
+the GPU. -l runs CompressWithStats with a log stream and writes FasTC's
+per-block log to <basename>.log; formats other than BPTC are refused.
 Inputs: PNG (8-bit), .npy RGBA8 arrays, raw RGBA (.rgba/.raw with -s WxH).
 """
 from __future__ import annotations
@@ -26,15 +27,10 @@ def usage(out=sys.stderr) -> None:
     print(__doc__.strip(), file=out)
 
 
-def psnr(src: np.ndarray, dec: np.ndarray) -> float:
-    """FasTC's Image::ComputePSNR (Base/src/Image.cpp:206-255)."""
-    a0 = src[..., 3:4].astype(np.float64) / 255.0
-    a1 = dec[..., 3:4].astype(np.float64) / 255.0
-    d = a0 * src[..., :3].astype(np.float64) - a1 * dec[..., :3].astype(np.float64)
-    mse = float((d * d).sum()) / (src.shape[0] * src.shape[1])
-    if mse == 0.0:
-        return float("inf")
-    return 10.0 * np.log10(3.0 * 255.0 * 255.0 / mse)
+def basename(path: str) -> str:
+    """ExtractBasename (CLTool/src/tc.cpp:57-79): the file name without its
+    directory and without everything from its first dot."""
+    return os.path.basename(path).split(".", 1)[0]
 
 
 def main(argv=None) -> int:
@@ -42,7 +38,7 @@ def main(argv=None) -> int:
     if not argv:
         usage()
         return 1
-    quality, repeats, out_name, write_out = 50, 1, "", True
+    quality, repeats, out_name, write_out, save_log = 50, 1, "", True, False
     width = height = 0
     i = 0
     while i < len(argv) and argv[i].startswith("-"):
@@ -71,9 +67,7 @@ def main(argv=None) -> int:
         if opt == "-nd":
             write_out = False
         elif opt == "-l":
-            print("-l (CompressWithStats) is not supported: its shape selection differs from "
-                  "BPTCC::Compress", file=sys.stderr)
-            return 1
+            save_log = True
         elif opt not in ("-a", "-v", "-simd"):
             usage()
             return 1
@@ -84,24 +78,30 @@ def main(argv=None) -> int:
     path = argv[i]
 
     from . import imageio
-    from .bptc import CompressionJob, CompressionSettings, compress, decompress
+    from .bptc import CompressionJob, CompressionSettings, compress, compress_with_stats, decompress, psnr
 
     img = imageio.pad_to_blocks(imageio.load_image(path, width, height))
     h, w = img.shape[:2]
     blocks = np.zeros(w * h, dtype=np.uint8)
     settings = CompressionSettings(num_simulated_annealing_steps=quality)
+    logs = []
     t0 = time.perf_counter()
     for _ in range(repeats):
-        compress(CompressionJob(img, blocks, w, h), settings)
+        if save_log:  # the log stream sees every compression, as FasTC's does
+            logs.append(compress_with_stats(CompressionJob(img, blocks, w, h), settings))
+        else:
+            compress(CompressionJob(img, blocks, w, h), settings)
     dt = (time.perf_counter() - t0) / repeats
     if repeats > 1:
         print(f"Compression time: {dt * 1e3:.3f} ms")
-    dec = decompress(blocks, w, h)
-    print(f"PSNR: {psnr(img, dec):.3f}")
+    if save_log:
+        with open(basename(path) + ".log", "w") as f:
+            f.write("".join(logs))
+    print(f"PSNR: {psnr(blocks, img, w, h):.3f}")
     if write_out:
+        dec = decompress(blocks, w, h)
         if not out_name:
-            base = os.path.splitext(os.path.basename(path))[0]
-            out_name = base + "-bptc.png"
+            out_name = basename(path) + "-bptc.png"
         with open(out_name, "wb") as f:
             if out_name.endswith(".ktx"):
                 f.write(imageio.ktx_bytes(blocks, w, h))

@@ -158,6 +158,45 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_block_error_device(const uint8_t *block
                                                             uint32_t height, double *block_sse,
                                                             double *sse_total, void *stream);
 
+/* What BPTCC::CompressWithStats logs for one block through its BlockLogger
+ * (BPTCEncoder/src/Compressor.cpp:1373-1389, 1938-2183). */
+typedef struct {
+  int32_t path;          /* 0 single colour, 1 transparent, 2 a shape with
+                            estimate below 1e-9, 3 searched */
+  int32_t mode;          /* BC7 mode of the block written */
+  double estimate[8];    /* per-mode error estimate, -1 where none was made */
+  double error[8];       /* per-mode error as FasTC logs it: always -1, since
+                            its CompressClusters keeps min(error, -1) (:1801) */
+  int32_t n_two, n_three;
+  double two_shape[64];  /* each improving 2-subset shape estimate, in order */
+  double three_shape[64];/* each improving 3-subset shape estimate, in order */
+} fastc_bc7_block_stats;
+
+/* BPTCC::CompressWithStats(job, logStream, settings) with a log stream
+ * (BPTCEncoder/include/FasTC/BPTCCompressor.h:173; Compressor.cpp:1577-1624):
+ * the logging encoder, whose shape selection differs from Compress's
+ * (opaque means every alpha is 255, modes 4 and 5 stay on for opaque
+ * blocks, 3-subset shapes are searched for opaque blocks even after an
+ * exact 2-subset shape, bounding boxes are quantised to two colour grids).
+ * Host buffers; the job's blocks are written to job->out and the
+ * statistics of its fastc_bc7_job_blocks(job) blocks, in raster order, to
+ * `stats`. FasTC's loop runs to y <= YEnd with no clamp to height - 4
+ * (:1583-1584), reading and writing a row past the buffers when YEnd is
+ * the height; here the range is clamped as Compress clamps it. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_compress_stats(const fastc_bc7_job *job,
+                                                        const fastc_bc7_settings *s,
+                                                        fastc_bc7_block_stats *stats);
+/* FasTC's log text for the job's blocks: per block, "<block index>:
+ * BlockStat_<name> -- <value>" lines (doubles as an ostream prints them, 6
+ * significant digits), the improving shape estimates first, then Path, then
+ * Mode and each mode's estimate and error. The block index is the block's
+ * raster index in the whole texture (CompressionJob::CoordsToBlockIdx).
+ * Writes at most cap bytes (no terminating zero); *len receives the full
+ * length, so a call with cap 0 sizes the buffer. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_stats_log(const fastc_bc7_job *job,
+                                                   const fastc_bc7_block_stats *stats,
+                                                   char *buf, size_t cap, size_t *len);
+
 /* BPTCC::LogicalBlock (BPTCCompressor.h:203-209): the stored fields of one
  * block. Endpoints are at their stored precision (p-bit appended as the
  * lowest bit), depth[] gives that precision per channel (0: channel absent,

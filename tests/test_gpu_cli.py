@@ -34,3 +34,21 @@ def test_tc_pads_odd_sizes_and_writes_decoded_png(gpu, tmp_path):
     assert tc.main(["-q", "0", "-d", str(out), str(src)]) == 0
     dec = imageio.read_png(out.read_bytes())
     assert dec.shape == (16, 12, 4)
+
+
+def test_tc_log_is_compress_with_stats(gpu, tmp_path, monkeypatch):
+    """-l writes FasTC's per-block log to <basename>.log, the blocks those
+    of the logging encoder."""
+    from fastc_gb300 import CompressionJob, CompressionSettings, compress_with_stats, imageio, tc
+
+    img = make_image("tile_mix(43, 32, 24)")
+    src = tmp_path / "logged.tex.png"
+    src.write_bytes(imageio.png_bytes(img))
+    monkeypatch.chdir(tmp_path)
+    assert tc.main(["-l", "-q", "4", "-d", "out.ktx", str(src)]) == 0
+    want = np.zeros(32 * 24, np.uint8)
+    log = compress_with_stats(CompressionJob(img, want, 32, 24),
+                              CompressionSettings(num_simulated_annealing_steps=4))
+    assert (tmp_path / "logged.log").read_text() == log
+    blocks, _, _ = imageio.read_ktx((tmp_path / "out.ktx").read_bytes())
+    assert np.array_equal(blocks, want)

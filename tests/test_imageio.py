@@ -65,21 +65,20 @@ def test_ktx_layout_matches_fastc_writer():
     assert (w, h) == (8, 8) and np.array_equal(b, blocks)
 
 
-def test_pad_to_blocks_and_psnr():
+def test_pad_to_blocks_and_basename():
     from fastc_gb300 import imageio, tc
 
     img = make_image("tile_mix(4, 16, 16)")[:13, :10]
     p = imageio.pad_to_blocks(img)
     assert p.shape == (16, 12, 4) and np.array_equal(p[:13, :10], img) and not p[13:].any()
-    assert tc.psnr(p, p) == float("inf")
-    noisy = p.copy()
-    noisy[..., 0] ^= 1
-    assert 40.0 < tc.psnr(p, noisy) < 60.0
+    # FasTC's ExtractBasename: no directory, nothing from the first dot on
+    assert tc.basename("dir/sub/tex.v2.png") == "tex"
+    assert tc.basename("tex") == "tex"
 
 
 def test_cli_refuses_what_it_does_not_do(capsys):
     from fastc_gb300 import tc
 
-    assert tc.main(["-l", "x.png"]) == 1
     assert tc.main(["-f", "DXT1", "x.png"]) == 1
+    assert tc.main(["-q"]) == 1
     assert tc.main([]) == 1
