@@ -178,7 +178,7 @@ def _single_colour_blocks_before(tex, y0: int) -> int:
     return int((blk == blk[..., :1]).all(-1).sum())
 
 
-def encode_bands(bands, threads: int, kind: str, textures=None):
+def encode_bands(bands, threads: int, kind: str, textures=None, steps: int = STEPS_Q):
     """One pass over the bands on `threads` host threads (each thread takes
     every threads-th band): FasTC's own encoder (kind "reference", the
     in-place build; its global RNG is shared by the threads, as under
@@ -206,12 +206,12 @@ def encode_bands(bands, threads: int, kind: str, textures=None):
             h, w = img.shape[:2]
             if kind == "reference":
                 o = np.zeros(w * h, dtype=np.uint8)
-                enc.lib.ref_compress(O._ptr(img), O._ptr(o), w, h, 0, 0, w, h, STEPS_Q, 0xFF, 0)
+                enc.lib.ref_compress(O._ptr(img), O._ptr(o), w, h, 0, 0, w, h, steps, 0xFF, 0)
                 outs[k] = o
             elif textures is None or y0 == 0:
-                outs[k] = enc.compress(img, steps=STEPS_Q, seed=ANNEAL_SEED)
+                outs[k] = enc.compress(img, steps=steps, seed=ANNEAL_SEED)
             else:
-                o = enc.compress(textures[i], steps=STEPS_Q, seed=ANNEAL_SEED, rect=(0, y0, w, y0),
+                o = enc.compress(textures[i], steps=steps, seed=ANNEAL_SEED, rect=(0, y0, w, y0),
                                  state=np.array([0, prior[k]], np.uint32))
                 outs[k] = o[y0 * w:(y0 + 4) * w]
 
@@ -296,6 +296,40 @@ def calibrate_cpu(args):
                                         "port_over_reference": res["port"] / res["reference"],
                                         "threads": threads, "passes": args.steps, "texels": px,
                                         "rows": len(bands), "steps_q": STEPS_Q}}))
+
+
+def cpu_configs(args):
+    """--cpu-configs: the CPU encoder (FasTC's own where oracle/_ref is built
+    here, else the port) on each configuration, all host threads unless
+    --threads: config 1 (256x256 gradient, q0, also on 1 thread), config 2
+    (2048x2048 tile mix, q50), config 3 (the texture set's row sample, q50)
+    and config 5 (rows 3840..3903 of the 8192x8192 radial-alpha image,
+    q100). Threads take block rows in turn, as tc -t N splits an image.
+    One JSON line of MPix/s."""
+    import numpy as np
+
+    from fastc_gb300 import synth
+    from oracle import oracle as O
+
+    kind = "reference" if os.path.exists(O.REF_SO) else "port"
+    threads = args.threads or (os.cpu_count() or 1)
+
+    def rows_of(img):
+        h = img.shape[0]
+        return [(0, y, np.ascontiguousarray(img[y:y + 4])) for y in range(0, h, 4)]
+
+    def rate(bands, steps, nthreads):
+        dt, _ = encode_bands(bands, nthreads, kind, steps=steps)
+        return band_texels(bands) / dt / 1e6
+
+    c1 = rows_of(synth.gradient_noise_alpha_ramp(1, 256, 256))
+    out = {"kind": kind, "threads": threads,
+           "c1_256_q0_t1": rate(c1, 0, 1), "c1_256_q0": rate(c1, 0, threads),
+           "c2_2048_q50": rate(rows_of(synth.tile_mix(2, 2048, 2048)), 50, threads),
+           "c3_row_sample_q50": rate(band_sample(), 50, threads),
+           "c5_rows_3840_3903_q100": rate(rows_of(synth.tile_mix_radial_alpha(5, 8192, 64, 0, 3840)), 100,
+                                          threads)}
+    print(json.dumps({"cpu_configs": out}))
 
 
 def max_over_ranks(seconds: float, dist, device: str) -> float:
@@ -498,7 +532,10 @@ def main():
                     help="skip the config-2, config-5 and serving measurements")
     ap.add_argument("--calibrate-cpu", action="store_true",
                     help="time FasTC's own encoder (oracle/_ref) against the port on the CPU sample")
-    ap.add_argument("--threads", type=int, default=0, help="host threads of --calibrate-cpu")
+    ap.add_argument("--cpu-configs", action="store_true",
+                    help="time the CPU encoder on each configuration (MPix/s)")
+    ap.add_argument("--threads", type=int, default=0,
+                    help="host threads of --calibrate-cpu and --cpu-configs")
     ap.add_argument("--serve", action="store_true", help="run the serving sweep instead")
     ap.add_argument("--serve-rates", default="20,60,120")
     ap.add_argument("--serve-seconds", type=float, default=4.0)
@@ -521,6 +558,9 @@ def main():
         return
     if args.calibrate_cpu:
         calibrate_cpu(args)
+        return
+    if args.cpu_configs:
+        cpu_configs(args)
         return
     if args.serve:
         serve_bench(args)
@@ -676,10 +716,12 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": (tpb * total_blocks) if tpb else None,
-                     "note": "issue-bound integer/FP32 search: the annealing and select kernels keep "
-                             "the ALU pipe 60-69 % busy and the setup kernels are latency-bound, "
-                             "while HBM traffic stays under 1 % of peak; traffic counts the stages' "
-                             "fit state exchanged through HBM and the setup kernels' spills"},
+                     "note": "issue-bound integer/FP32 search: the annealing kernels issue on 74 % of "
+                             "cycles with the ALU pipe 62 % busy, the setup kernels are latency-bound "
+                             "(47 % issue), while HBM traffic stays under 1 % of peak; traffic (ncu, "
+                             "per block of a 4096x4096 tile-mix launch, scaled to the set's blocks) "
+                             "counts the stages' fit state exchanged through HBM and the setup "
+                             "kernels' spills"},
         "clocks": clocks.summary(),
     }
     if ipb:

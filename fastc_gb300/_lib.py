@@ -78,7 +78,8 @@ class ServerStats(C.Structure):
                 ("cancelled", C.c_uint64), ("rejected", C.c_uint64), ("batches", C.c_uint64),
                 ("pixels_completed", C.c_uint64), ("bytes_in_use", C.c_size_t), ("peak_bytes", C.c_size_t),
                 ("p50_latency_ms", C.c_double), ("p99_latency_ms", C.c_double),
-                ("mean_latency_ms", C.c_double), ("max_latency_ms", C.c_double), ("mpix_per_s", C.c_double)]
+                ("mean_latency_ms", C.c_double), ("max_latency_ms", C.c_double), ("mpix_per_s", C.c_double),
+                ("psnr_db", C.c_double)]
 
 
 # Every function include/fastc_bc7.h declares, with its ctypes signature.
@@ -117,6 +118,7 @@ SIGNATURES = {
                                           C.POINTER(C.c_uint64)]),
     "fastc_bc7_server_poll": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fastc_bc7_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int64]),
+    "fastc_bc7_server_request_psnr": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]),
     "fastc_bc7_server_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fastc_bc7_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fastc_bc7_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),

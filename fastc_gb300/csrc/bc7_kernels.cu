@@ -755,6 +755,42 @@ __global__ void __launch_bounds__(1024) sum_kernel(const double *__restrict__ v,
   if (threadIdx.x == 0) *out = s[0];
 }
 
+// The same over a raster range of blocks [first, first + count) of a
+// texture of `width` texels, blocks[k] holding block first + k and `rows`
+// the texels from row row0 on (as a job uploads them).
+__global__ void range_error_kernel(const uint8_t *__restrict__ blocks,
+                                   const uint8_t *__restrict__ rows, uint32_t width, uint32_t row0,
+                                   uint32_t first, uint32_t count, double *__restrict__ sse) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const uint32_t bw = width / 4, b = first + k;
+  const uint32_t bx = b % bw, by = b / bw;
+  uint32_t w[4];
+  load_block_words(blocks + (size_t)k * 16, w);
+  uint32_t dec[16];
+  decode_block(w, 0, dec);
+  double s = 0.0;
+  for (int r = 0; r < 4; r++)
+    for (int c = 0; c < 4; c++) {
+      const uint8_t *p = rows + ((size_t)(by * 4 + r - row0) * width + bx * 4 + c) * 4;
+      const uint32_t orig = (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) |
+                            ((uint32_t)p[3] << 24);
+      s += texel_sse(orig, dec[4 * r + c]);
+    }
+  sse[k] = s;
+}
+
+int launch_range_error(const uint8_t *blocks, const uint8_t *rows, uint32_t width, uint32_t row0,
+                       uint32_t first, uint32_t count, double *block_sse, double *total,
+                       void *stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (count == 0) return 0;
+  range_error_kernel<<<(count + 127) / 128, 128, 0, st>>>(blocks, rows, width, row0, first, count,
+                                                           block_sse);
+  sum_kernel<<<1, 1024, 0, st>>>(block_sse, count, total);
+  return (int)cudaPeekAtLastError();
+}
+
 int launch_block_error(const uint8_t *blocks, const uint8_t *rgba, uint32_t width,
                        uint32_t height, double *block_sse, double *total, void *stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);

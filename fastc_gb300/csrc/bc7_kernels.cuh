@@ -57,6 +57,12 @@ int device_sm_count(int device);
 // total is not null.
 int launch_block_error(const uint8_t *blocks, const uint8_t *rgba, uint32_t width,
                        uint32_t height, double *block_sse, double *total, void *stream);
+// The same for the blocks [first, first + count) of a texture `width`
+// texels wide, `blocks` holding them from `first` on and `rows` its texels
+// from row `row0` on.
+int launch_range_error(const uint8_t *blocks, const uint8_t *rows, uint32_t width, uint32_t row0,
+                       uint32_t first, uint32_t count, double *block_sse, double *total,
+                       void *stream);
 // The single-colour rank pre-pass (classify + scan); also resets the work
 // counter and status of `scratch`.
 int launch_rank_prepass(const JobDev *jobs_dev, int njobs, uint64_t total_blocks,

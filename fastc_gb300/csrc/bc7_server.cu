@@ -12,11 +12,14 @@
 // uploaded and launched on another stream, so requests that arrive during a
 // batch overlap with it on the device. Each block's result depends only on
 // its texture, position and settings, so a request gives the same bytes
-// alone or in any mix.
+// alone or in any mix. After the encode each request's blocks are decoded
+// and compared with its texels on the device (FasTC's PSNR metric), so the
+// server reports every request's quality beside its latency.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -48,6 +51,7 @@ struct Request {
   size_t in_bytes = 0, out_bytes = 0;
   ReqState state = kPending;
   fastc_bc7_status status = FASTC_BC7_OK;
+  double sse = 0.0;               // FasTC's PSNR metric summed over the blocks
   Clock::time_point t_submit, t_done;
 };
 
@@ -87,13 +91,16 @@ struct fastc_bc7_server_s {
   std::vector<double> latencies_ms;
   uint64_t submitted = 0, completed = 0, failed = 0, cancelled = 0, rejected = 0, batches = 0;
   uint64_t pixels = 0;
+  double sse = 0.0;  // of the completed requests
   bool started = false;
   Clock::time_point t_first;
   Clock::time_point t_last;
 
   // device bytes a batch needs, beyond the per-request texels and blocks
+  // (job table, the quality sums, encoder scratch)
   size_t batch_overhead(uint64_t blocks, size_t njobs) const {
-    return round_up(njobs * sizeof(JobDev)) + scratch_bytes_worst(blocks, engine);
+    return round_up(njobs * sizeof(JobDev)) + round_up(njobs * sizeof(double)) +
+           round_up(blocks * sizeof(double)) + scratch_bytes_worst(blocks, engine);
   }
 
   void loop();
@@ -130,22 +137,26 @@ void fastc_bc7_server_s::launch(Slot &s) {
     total += s.reqs[i]->count;
   }
   const size_t table = round_up(s.reqs.size() * sizeof(JobDev));
+  const size_t sums = round_up(s.reqs.size() * sizeof(double));  // per-request error
+  const size_t errs = round_up(total * sizeof(double));          // per-block error
   int tb = 0;
   for (Request *r : s.reqs) tb = std::max(tb, fastc::block_task_bound(r->settings.block_modes));
-  const size_t need = in_total + out_total + table + scratch_bytes(total, engine, tb);
-  if (s.pinned_cap < out_total) {
+  const size_t need = in_total + out_total + table + sums + errs + scratch_bytes(total, engine, tb);
+  if (s.pinned_cap < out_total + sums) {
     if (s.pinned) cudaFreeHost(s.pinned);
     s.pinned = nullptr;
     s.pinned_cap = 0;
-    e = cudaMallocHost(reinterpret_cast<void **>(&s.pinned), out_total);
-    if (e == cudaSuccess) s.pinned_cap = out_total;
+    e = cudaMallocHost(reinterpret_cast<void **>(&s.pinned), out_total + sums);
+    if (e == cudaSuccess) s.pinned_cap = out_total + sums;
   }
   if (e == cudaSuccess) e = cudaMallocAsync(&s.dev, need, s.stream);
   if (e == cudaSuccess) {
     uint8_t *din = static_cast<uint8_t *>(s.dev);
     uint8_t *dout = din + in_total;
     JobDev *dtab = reinterpret_cast<JobDev *>(dout + out_total);
-    void *scratch = reinterpret_cast<uint8_t *>(dtab) + table;
+    double *dsum = reinterpret_cast<double *>(reinterpret_cast<uint8_t *>(dtab) + table);
+    double *derr = reinterpret_cast<double *>(reinterpret_cast<uint8_t *>(dsum) + sums);
+    void *scratch = reinterpret_cast<uint8_t *>(derr) + errs;
     std::vector<JobDev> dj(s.reqs.size());
     uint64_t begin = 0;
     for (size_t i = 0; i < s.reqs.size() && e == cudaSuccess; i++) {
@@ -172,8 +183,19 @@ void fastc_bc7_server_s::launch(Slot &s) {
       e = (cudaError_t)launch_engine(dtab, (int)dj.size(), total, scratch, engine, shape, tb, s.cls,
                                      s.stream);
     }
+    uint64_t at = 0;  // each request's quality, from its uploaded texels and its blocks
+    for (size_t i = 0; i < s.reqs.size() && e == cudaSuccess; i++) {
+      const Request &r = *s.reqs[i];
+      e = (cudaError_t)fastc::launch_range_error(dout + s.out_off[i], din + in_off[i], r.job.width,
+                                                 r.row0, r.first, r.count, derr + at, dsum + i,
+                                                 s.stream);
+      at += r.count;
+    }
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(s.pinned, dout, out_total, cudaMemcpyDeviceToHost, s.stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s.pinned + out_total, dsum, s.reqs.size() * sizeof(double),
+                          cudaMemcpyDeviceToHost, s.stream);
     cudaFreeAsync(s.dev, s.stream);
     s.dev = nullptr;
   }
@@ -192,9 +214,12 @@ void fastc_bc7_server_s::launch(Slot &s) {
 void fastc_bc7_server_s::retire(Slot &s) {
   // Called by the worker without the lock, after the batch finished.
   if (s.error == cudaSuccess) {
+    size_t out_total = 0;
+    for (size_t i = 0; i < s.reqs.size(); i++) out_total += round_up(s.reqs[i]->out_bytes);
     for (size_t i = 0; i < s.reqs.size(); i++) {
       Request &r = *s.reqs[i];
       std::memcpy(r.job.out + (size_t)r.first * 16, s.pinned + s.out_off[i], r.out_bytes);
+      std::memcpy(&r.sse, s.pinned + out_total + i * sizeof(double), sizeof(double));
     }
   }
   const Clock::time_point now = Clock::now();
@@ -205,6 +230,7 @@ void fastc_bc7_server_s::retire(Slot &s) {
       r->state = kDone;
       completed++;
       pixels += (uint64_t)r->count * 16;
+      sse += r->sse;
       latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
     } else {
       r->state = kFailed;
@@ -379,6 +405,13 @@ fastc_bc7_status fastc_bc7_server_submit(fastc_bc7_server s, const fastc_bc7_job
   return FASTC_BC7_OK;
 }
 
+// FasTC's Image::ComputePSNR from a summed error (Base/src/Image.cpp:206-255):
+// peak 3 * 255^2 over the mean per texel; 0 texels give 0.
+static double psnr_of(double sse, uint64_t texels) {
+  if (texels == 0) return 0.0;
+  return 10.0 * std::log10((3.0 * 255.0 * 255.0) / (sse / (double)texels));
+}
+
 static fastc_bc7_status state_status(const Request &r) {
   switch (r.state) {
     case kDone: return FASTC_BC7_OK;
@@ -469,6 +502,19 @@ fastc_bc7_status fastc_bc7_server_get_stats(fastc_bc7_server s, fastc_bc7_server
     const double secs = std::chrono::duration<double>(s->t_last - s->t_first).count();
     out->mpix_per_s = secs > 0 ? (double)s->pixels / secs / 1e6 : 0.0;
   }
+  out->psnr_db = psnr_of(s->sse, s->pixels);
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_server_request_psnr(fastc_bc7_server s, uint64_t id, double *psnr) {
+  if (!s || !psnr) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return FASTC_BC7_ERR_NOT_FOUND;
+  const Request &r = *it->second;
+  const fastc_bc7_status st = state_status(r);
+  if (st != FASTC_BC7_OK) return st;
+  *psnr = psnr_of(r.sse, (uint64_t)r.count * 16);
   return FASTC_BC7_OK;
 }
 

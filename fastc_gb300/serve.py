@@ -74,6 +74,14 @@ class Server:
         check(self._lib.fastc_bc7_server_wait(self._h, req.id, int(timeout_ms)), "fastc_bc7_server_wait")
         return req.out
 
+    def psnr(self, req: Request) -> float:
+        """The PSNR of a finished request (FasTC's metric, measured on the
+        device after its encode)."""
+        v = C.c_double()
+        check(self._lib.fastc_bc7_server_request_psnr(self._h, req.id, C.byref(v)),
+              "fastc_bc7_server_request_psnr")
+        return v.value
+
     def cancel(self, req: Request) -> None:
         check(self._lib.fastc_bc7_server_cancel(self._h, req.id), "fastc_bc7_server_cancel")
 

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define FASTC_BC7_ABI_VERSION 1
+#define FASTC_BC7_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define FASTC_BC7_API __attribute__((visibility("default")))
@@ -311,6 +311,8 @@ typedef struct {
   size_t bytes_in_use, peak_bytes;
   double p50_latency_ms, p99_latency_ms, mean_latency_ms, max_latency_ms;
   double mpix_per_s; /* texels completed / time from first submit to last completion */
+  double psnr_db;    /* FasTC's PSNR (Image::ComputePSNR) over every completed
+                        request's texels, measured on the device */
 } fastc_bc7_server_stats;
 
 FASTC_BC7_API void fastc_bc7_server_config_default(fastc_bc7_server_config *cfg);
@@ -326,6 +328,11 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_server_poll(fastc_bc7_server s, uint64_
 /* Wait up to timeout_ms (negative: forever). */
 FASTC_BC7_API fastc_bc7_status fastc_bc7_server_wait(fastc_bc7_server s, uint64_t request_id,
                                                      int64_t timeout_ms);
+/* The PSNR of a finished request's blocks against its texels, by FasTC's
+ * Image::ComputePSNR metric (Base/src/Image.cpp:206-255), computed on the
+ * device after its encode; the request's status while it is not finished. */
+FASTC_BC7_API fastc_bc7_status fastc_bc7_server_request_psnr(fastc_bc7_server s,
+                                                             uint64_t request_id, double *psnr);
 /* Cancel a request that is still queued. */
 FASTC_BC7_API fastc_bc7_status fastc_bc7_server_cancel(fastc_bc7_server s, uint64_t request_id);
 /* Forget a finished request. */

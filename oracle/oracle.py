@@ -20,7 +20,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libbc7_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfastc_ref.so")
-DEFAULT_REFERENCE = "/root/reference"
+# the FasTC checkout, where this machine has one (FASTC_REFERENCE overrides)
+DEFAULT_REFERENCE = os.environ.get("FASTC_REFERENCE", "/root/reference")
 
 RNG_PER_FIT = 0
 RNG_SINGLE_STREAM = 1

@@ -46,7 +46,7 @@ def test_settings_defaults_mirror_fastc(bc7lib):
     # BPTCCompressor.h:150-156: all modes, uniform metric, 50 steps
     assert (s.block_modes, s.error_metric, s.steps) == (0xFF, 0, 50)
     assert s.shape_selection_fn is None and s.seed == 0 and s.watermark_start == 0
-    assert bc7lib.fastc_bc7_abi_version() == 1
+    assert bc7lib.fastc_bc7_abi_version() == 2
 
 
 def test_status_strings(bc7lib):

@@ -1,6 +1,7 @@
 """The continuous-batching request server on the GPU: results are the same
 alone and in a concurrent mix, the memory budget is enforced, queued
-requests can be cancelled, statistics add up."""
+requests can be cancelled, statistics (latency, PSNR per request and
+overall) add up."""
 import threading
 import time
 
@@ -47,6 +48,7 @@ def test_alone_equals_in_the_mix(gpu, port):
             t.join()
         mixed = [srv.wait(hd) for hd in handles]
         st = srv.stats()
+        psnrs = [srv.psnr(hd) for hd in handles]
     for (img, q), a, m in zip(reqs, alone, mixed):
         assert np.array_equal(a, m)
     # and the same bytes as the oracle
@@ -56,6 +58,17 @@ def test_alone_equals_in_the_mix(gpu, port):
     assert st["batches"] >= 2
     assert st["p99_latency_ms"] >= st["p50_latency_ms"] > 0
     assert st["pixels_completed"] == sum(im.shape[0] * im.shape[1] for im, _ in reqs)
+    # each request's quality, measured on the device, is the oracle's PSNR of
+    # its blocks (FasTC's metric; the sums differ in order only), and the
+    # server's overall PSNR is that of all requests' texels together
+    sse = 0.0
+    for (img, q), blocks, db in zip(reqs, mixed, psnrs):
+        h, w = img.shape[:2]
+        dec = port.decompress(blocks, w, h)
+        assert abs(db - port.psnr(img, dec)) <= 1e-9
+        sse += float(port.block_sse(img, dec).sum())
+    px = st["pixels_completed"]
+    assert abs(st["psnr_db"] - 10 * np.log10(3 * 255.0 ** 2 / (sse / px))) <= 1e-9
 
 
 def test_budget_rejects_oversized_and_queues_the_rest(gpu):
