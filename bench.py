@@ -166,28 +166,38 @@ def band_sample(stride: int = BAND_STRIDE):
     return out
 
 
-def _single_colour_blocks_before(tex, y0: int) -> int:
-    """Single-colour blocks of `tex` in the block rows above texel row y0."""
+def _single_colour_blocks_before(tex, y0: int, x0: int = 0) -> int:
+    """Single-colour blocks of `tex` before the block at texel (x0, y0) in
+    raster order."""
     import numpy as np
 
-    top = tex[:y0].view("<u4")[..., 0]
-    if top.size == 0:
-        return 0
-    h, w = top.shape
-    blk = top.reshape(h // 4, 4, w // 4, 4).transpose(0, 2, 1, 3).reshape(h // 4, w // 4, 16)
-    return int((blk == blk[..., :1]).all(-1).sum())
+    def count(region):
+        px = region.view("<u4")[..., 0]
+        if px.size == 0:
+            return 0
+        h, w = px.shape
+        blk = px.reshape(h // 4, 4, w // 4, 4).transpose(0, 2, 1, 3).reshape(h // 4, w // 4, 16)
+        return int((blk == blk[..., :1]).all(-1).sum())
+
+    return count(tex[:y0]) + count(tex[y0:y0 + 4, :x0])
+
+
+# Work items of the CPU legs: pieces of at most PIECE texels of a row, so
+# that the host threads stay balanced whatever the rows' widths.
+PIECE = 256
 
 
 def encode_bands(bands, threads: int, kind: str, textures=None, steps: int = STEPS_Q):
-    """One pass over the bands on `threads` host threads (each thread takes
-    every threads-th band): FasTC's own encoder (kind "reference", the
-    in-place build; its global RNG is shared by the threads, as under
-    tc -t N) or the oracle port (kind "port", per-fit streams). With the
-    whole `textures` the port encodes each band as that row of its texture
-    (the texture's block coordinates seed the annealing, the watermark
-    counter continues from the rows above), giving the GPU's bytes. Returns
-    (seconds, the band's blocks for each band)."""
+    """One pass over the bands on `threads` host threads, which take pieces
+    of at most PIECE texels of a row in turn from a shared cursor: FasTC's
+    own encoder (kind "reference", the in-place build; its global RNG is
+    shared by the threads, as under tc -t N) or the oracle port (kind
+    "port", per-fit streams). With the whole `textures` the port encodes
+    each piece inside its texture (the texture's block coordinates seed the
+    annealing, the watermark counter continues from the blocks before it),
+    giving the GPU's bytes. Returns (seconds, the blocks of each band)."""
     import concurrent.futures as cf
+    import itertools
 
     import numpy as np
 
@@ -196,24 +206,45 @@ def encode_bands(bands, threads: int, kind: str, textures=None, steps: int = STE
     enc = O.Reference() if kind == "reference" else O.Port()
     if kind == "reference":
         enc.lib.ref_set_seed(ANNEAL_SEED)
-    prior = [_single_colour_blocks_before(textures[i], y0) for i, y0, _ in bands] if textures else None
-    outs = [None] * len(bands)
+    items = [(k, x0, min(x0 + PIECE, band.shape[1]))
+             for k, (_, _, band) in enumerate(bands) for x0 in range(0, band.shape[1], PIECE)]
+    prior = {}
+    if textures is not None:
+        for k, x0, _ in items:
+            i, y0, _ = bands[k]
+            prior[(k, x0)] = _single_colour_blocks_before(textures[i], y0, x0)
+    outs = [np.zeros(b.shape[0] * b.shape[1], dtype=np.uint8) for _, _, b in bands]
+    bufs = [np.ascontiguousarray(b) for _, _, b in bands]
+    cursor = itertools.count()
 
-    def work(t):
-        for k in range(t, len(bands), threads):
+    def work(_):
+        while True:
+            n = next(cursor)
+            if n >= len(items):
+                return
+            k, x0, x1 = items[n]
             i, y0, band = bands[k]
-            img = np.ascontiguousarray(band)
-            h, w = img.shape[:2]
-            if kind == "reference":
-                o = np.zeros(w * h, dtype=np.uint8)
-                enc.lib.ref_compress(O._ptr(img), O._ptr(o), w, h, 0, 0, w, h, steps, 0xFF, 0)
-                outs[k] = o
-            elif textures is None or y0 == 0:
-                outs[k] = enc.compress(img, steps=steps, seed=ANNEAL_SEED)
+            if textures is None:
+                # the piece as its own 4-texel-high image
+                piece = np.ascontiguousarray(bufs[k][:, x0:x1])
+                pw = x1 - x0
+                if kind == "reference":
+                    o = np.zeros(pw * 4, dtype=np.uint8)
+                    enc.lib.ref_compress(O._ptr(piece), O._ptr(o), pw, 4, 0, 0, pw, 4, steps, 0xFF, 0)
+                else:
+                    o = enc.compress(piece, steps=steps, seed=ANNEAL_SEED)
+                outs[k][x0 * 4:x1 * 4] = o
             else:
-                o = enc.compress(textures[i], steps=steps, seed=ANNEAL_SEED, rect=(0, y0, w, y0),
-                                 state=np.array([0, prior[k]], np.uint32))
-                outs[k] = o[y0 * w:(y0 + 4) * w]
+                # the piece inside its texture: row y0, texels [x0, x1)
+                tex = textures[i]
+                w = tex.shape[1]
+                if y0 > 0:
+                    o = enc.compress(tex, steps=steps, seed=ANNEAL_SEED, rect=(x0, y0, x1, y0),
+                                     state=np.array([0, prior[(k, x0)]], np.uint32))
+                    outs[k][x0 * 4:x1 * 4] = o[y0 * w + x0 * 4:y0 * w + x1 * 4]
+                else:  # the first block row, whole (a rect cannot end on row 0)
+                    o = enc.compress(np.ascontiguousarray(tex[:4]), steps=steps, seed=ANNEAL_SEED)
+                    outs[k][x0 * 4:x1 * 4] = o[x0 * 4:x1 * 4]
 
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(threads) as ex:

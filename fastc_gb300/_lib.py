@@ -68,6 +68,13 @@ class BlockStats(C.Structure):
                 ("two_shape", C.c_double * 64), ("three_shape", C.c_double * 64)]
 
 
+class PlanTuning(C.Structure):
+    """fastc_bc7_plan_tuning_info."""
+    _fields_ = [("engine", C.c_int32), ("warps_per_cta", C.c_int32), ("anneal_ctas_per_sm", C.c_int32),
+                ("yield_lanes", C.c_int32), ("select_ctas_per_sm", C.c_int32),
+                ("setup_ctas_per_sm", C.c_int32), ("chunk_blocks", C.c_uint64)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("memory_budget", C.c_size_t), ("max_inflight", C.c_uint32),
                 ("max_batch_blocks", C.c_uint32), ("max_batch_jobs", C.c_uint32), ("reserved", C.c_uint32)]
@@ -109,6 +116,7 @@ SIGNATURES = {
     "fastc_bc7_plan_kernels": (C.c_uint64, [C.c_void_p]),
     "fastc_bc7_plan_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "fastc_bc7_plan_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "fastc_bc7_plan_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(PlanTuning)]),
     "fastc_bc7_plan_destroy": (C.c_int, [C.c_void_p]),
     "fastc_bc7_set_watermark_counter": (None, [C.c_uint32]),
     "fastc_bc7_get_watermark_counter": (C.c_uint32, []),

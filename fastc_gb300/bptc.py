@@ -347,9 +347,11 @@ class Plan:
         return self.tuning()
 
     def tuning(self) -> dict:
-        a, y = C.c_int(), C.c_int()
-        check(load().fastc_bc7_plan_tuning(self._h, C.byref(a), C.byref(y)), "fastc_bc7_plan_tuning")
-        return {"anneal_ctas_per_sm": int(a.value), "yield_lanes": int(y.value)}
+        """Every parameter the plan's graph was captured with
+        (fastc_bc7_plan_get_tuning)."""
+        t = _lib.PlanTuning()
+        check(load().fastc_bc7_plan_get_tuning(self._h, C.byref(t)), "fastc_bc7_plan_get_tuning")
+        return {name: int(getattr(t, name)) for name, _ in _lib.PlanTuning._fields_}
 
     def launch(self, stream=None) -> None:
         check(load().fastc_bc7_plan_launch(self._h, C.c_void_p(_stream_handle(stream))),

@@ -433,28 +433,43 @@ struct fastc_bc7_plan_s {
   cudaGraphExec_t exec = nullptr;
   uint64_t kernels = 0;  // kernel nodes of the graph
   int task_bound = 0;
+  size_t scratch_size = 0;  // bytes at d_scratch
+  int warps = 4;            // warps per CTA when the engine is warp-per-block
   fastc::PipelineTuning tune;
 };
 
 namespace {
 
-// Captures the plan's whole launch with `tune` into a graph (private
-// stream and side streams, released after the capture) and instantiates it.
-cudaError_t capture_plan(const fastc_bc7_plan_s *p, const fastc::PipelineTuning &tune,
-                         cudaGraph_t *graph, cudaGraphExec_t *exec, uint64_t *kernels) {
+// The warp-per-block engine's launch shape with `warps` warps per CTA.
+LaunchShape shape_with(uint64_t total, int warps) {
+  const int sms = fastc::device_sm_count(current_device());
+  const int per_sm = std::max(1, fastc::encode_ctas_per_sm(warps));
+  uint64_t ctas = (uint64_t)sms * (uint64_t)per_sm;
+  const uint64_t need = (total + (uint64_t)warps - 1) / (uint64_t)warps;
+  ctas = std::max<uint64_t>(1, std::min(ctas, need));
+  return LaunchShape{warps, (int)ctas};
+}
+
+// Captures the plan's whole launch with `engine` (`warps` warps per CTA for
+// the warp-per-block engine) and `tune` into a graph (private stream and
+// side streams, released after the capture) and instantiates it.
+cudaError_t capture_plan(const fastc_bc7_plan_s *p, int engine, int warps,
+                         const fastc::PipelineTuning &tune, cudaGraph_t *graph,
+                         cudaGraphExec_t *exec, uint64_t *kernels) {
   *graph = nullptr;
   *exec = nullptr;
   cudaStream_t cs = nullptr;
   cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   ClassStreams cls{};
-  const bool use_cls = p->engine == FASTC_BC7_ENGINE_PIPELINE;
+  const bool use_cls = engine == FASTC_BC7_ENGINE_PIPELINE;
   if (e == cudaSuccess && use_cls) e = fastc::class_streams_create(&cls);
   if (e == cudaSuccess) {
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      const int le = launch_engine(p->d_jobs, p->njobs, p->total, p->d_scratch, p->engine,
-                                   pick_shape(p->total), p->task_bound, use_cls ? &cls : nullptr,
-                                   tune, cs);
+      const LaunchShape shape =
+          engine == FASTC_BC7_ENGINE_PIPELINE ? pick_shape(p->total) : shape_with(p->total, warps);
+      const int le = launch_engine(p->d_jobs, p->njobs, p->total, p->d_scratch, engine, shape,
+                                   p->task_bound, use_cls ? &cls : nullptr, tune, cs);
       cudaError_t ee = cudaStreamEndCapture(cs, graph);
       e = le ? (cudaError_t)le : ee;
     }
@@ -810,14 +825,15 @@ fastc_bc7_status fastc_bc7_plan_create(const fastc_bc7_job *jobs, uint32_t n,
   p->njobs = (int)n;
   cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p->d_jobs), n * sizeof(JobDev));
   p->engine = g_engine;
+  p->warps = g_warps;
   p->task_bound = task_bound_of(settings, per_job_settings, n);
-  if (e == cudaSuccess)
-    e = cudaMalloc(&p->d_scratch, scratch_bytes(total > 0 ? total : 1, p->engine, p->task_bound));
+  p->scratch_size = scratch_bytes(total > 0 ? total : 1, p->engine, p->task_bound);
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_scratch, p->scratch_size);
   if (e == cudaSuccess)
     e = cudaMemcpy(p->d_jobs, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
     p->sc = carve_scratch(p->d_scratch, total);
-    e = capture_plan(p, p->tune, &p->graph, &p->exec, &p->kernels);
+    e = capture_plan(p, p->engine, p->warps, p->tune, &p->graph, &p->exec, &p->kernels);
   }
   if (e != cudaSuccess) {
     fastc_bc7_plan_destroy(p);
@@ -832,6 +848,9 @@ fastc_bc7_status fastc_bc7_plan_launch(fastc_bc7_plan p, void *stream) {
   CK(cudaGraphLaunch(p->exec, static_cast<cudaStream_t>(stream)));
   return FASTC_BC7_OK;
 }
+
+// Sets of at most this many blocks also try the warp-per-block engine.
+constexpr uint64_t kSmallSetBlocks = 1ull << 16;
 
 fastc_bc7_status fastc_bc7_plan_autotune(fastc_bc7_plan p, void *stream, uint32_t launches) {
   if (!p || !p->exec || launches == 0) return FASTC_BC7_ERR_INVALID_ARGUMENT;
@@ -852,38 +871,82 @@ fastc_bc7_status fastc_bc7_plan_autotune(fastc_bc7_plan p, void *stream, uint32_
   };
   float best_ms = 0.0f;
   if (e == cudaSuccess) e = time_exec(p->exec, &best_ms);
-  // coordinate search: CTAs per SM of the annealing kernels, then the
-  // hand-on threshold at the best CTA count
+  // tries one candidate and keeps its graph when it is faster
+  auto trial = [&](int engine, int warps, const fastc::PipelineTuning &t) -> cudaError_t {
+    if (engine == FASTC_BC7_ENGINE_PIPELINE &&
+        rank_scratch_bytes(p->total) +
+                fastc::pipeline_scratch_bytes(p->total, p->task_bound,
+                                              fastc::device_sm_count(current_device()),
+                                              t.chunk_blocks) >
+            p->scratch_size)
+      return cudaSuccess;  // needs more scratch than the plan holds
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    uint64_t kern = 0;
+    cudaError_t r = capture_plan(p, engine, warps, t, &g, &ex, &kern);
+    float ms = 0.0f;
+    if (r == cudaSuccess) r = time_exec(ex, &ms);
+    if (r == cudaSuccess && ms < best_ms) {
+      std::swap(g, p->graph);
+      std::swap(ex, p->exec);
+      p->kernels = kern;
+      p->engine = engine;
+      p->warps = warps;
+      p->tune = t;
+      best_ms = ms;
+    }
+    if (ex) cudaGraphExecDestroy(ex);
+    if (g) cudaGraphDestroy(g);
+    return r;
+  };
+  // coordinate search over the pipeline's launch parameters, each at the
+  // best of the ones before: CTAs per SM of the annealing kernels, the
+  // hand-on threshold, the chunk size, the select grid, the setup grid
   const int ctas[] = {3, 4, 5, 6, 7};
   const int yields[] = {8, 12, 16};
-  for (int phase = 0; phase < 2 && e == cudaSuccess; phase++) {
-    const int ncand = phase == 0 ? 5 : 3;
+  const uint64_t dflt_chunk = fastc::pipeline_chunk(p->task_bound);
+  const uint64_t chunks[] = {dflt_chunk, dflt_chunk / 2, dflt_chunk / 4};
+  const int sel[] = {8, 16, 32};
+  const int setup[] = {6, 12, 24, 128};
+  const fastc::PipelineTuning base = p->tune;
+  for (int phase = 0; phase < 5 && e == cudaSuccess && p->engine == FASTC_BC7_ENGINE_PIPELINE;
+       phase++) {
+    const int ncand = phase == 0 ? 5 : phase == 1 ? 3 : phase == 2 ? 3 : phase == 3 ? 3 : 4;
     for (int i = 0; i < ncand && e == cudaSuccess; i++) {
       fastc::PipelineTuning t = p->tune;
       if (phase == 0) t.anneal_ctas_per_sm = ctas[i];
-      else t.yield_lanes = yields[i];
-      if (t.anneal_ctas_per_sm == p->tune.anneal_ctas_per_sm && t.yield_lanes == p->tune.yield_lanes)
+      else if (phase == 1) t.yield_lanes = yields[i];
+      else if (phase == 2) t.chunk_blocks = chunks[i] == dflt_chunk ? 0 : chunks[i];
+      else if (phase == 3) t.select_ctas_per_sm = sel[i];
+      else t.setup_ctas_per_sm = setup[i];
+      if (t.anneal_ctas_per_sm == p->tune.anneal_ctas_per_sm && t.yield_lanes == p->tune.yield_lanes &&
+          t.chunk_blocks == p->tune.chunk_blocks && t.select_ctas_per_sm == p->tune.select_ctas_per_sm &&
+          t.setup_ctas_per_sm == p->tune.setup_ctas_per_sm)
         continue;
-      cudaGraph_t g = nullptr;
-      cudaGraphExec_t ex = nullptr;
-      uint64_t kern = 0;
-      e = capture_plan(p, t, &g, &ex, &kern);
-      float ms = 0.0f;
-      if (e == cudaSuccess) e = time_exec(ex, &ms);
-      if (e == cudaSuccess && ms < best_ms) {
-        std::swap(g, p->graph);
-        std::swap(ex, p->exec);
-        p->kernels = kern;
-        p->tune = t;
-        best_ms = ms;
-      }
-      if (ex) cudaGraphExecDestroy(ex);
-      if (g) cudaGraphDestroy(g);
+      e = trial(FASTC_BC7_ENGINE_PIPELINE, p->warps, t);
     }
   }
+  // small sets: the warp-per-block engine (one persistent kernel instead of
+  // the pipeline's stages) at 2, 4 or 8 warps per CTA
+  if (p->total <= kSmallSetBlocks)
+    for (int w : {2, 4, 8})
+      if (e == cudaSuccess) e = trial(FASTC_BC7_ENGINE_WARP_PER_BLOCK, w, base);
   cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   if (e != cudaSuccess) return fail_cuda(e);
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_plan_get_tuning(fastc_bc7_plan p, fastc_bc7_plan_tuning_info *out) {
+  if (!p || !out) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::memset(out, 0, sizeof(*out));
+  out->engine = p->engine;
+  out->warps_per_cta = p->warps;
+  out->anneal_ctas_per_sm = p->tune.anneal_ctas_per_sm;
+  out->yield_lanes = p->tune.yield_lanes;
+  out->select_ctas_per_sm = p->tune.select_ctas_per_sm;
+  out->setup_ctas_per_sm = p->tune.setup_ctas_per_sm;
+  out->chunk_blocks = fastc::pipeline_chunk_blocks(p->task_bound, p->tune);
   return FASTC_BC7_OK;
 }
 

@@ -1904,6 +1904,23 @@ int block_task_bound(uint32_t modes, bool stats) {
   return worst;
 }
 
+uint64_t pipeline_chunk_blocks(int task_bound, const PipelineTuning &tune) {
+  const uint64_t dflt = pipeline_chunk(task_bound);
+  if (tune.chunk_blocks == 0 || tune.chunk_blocks >= dflt) return dflt;
+  const uint64_t c = tune.chunk_blocks / kRankChunk * kRankChunk;
+  return c < kRankChunk ? kRankChunk : c;
+}
+
+size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound, int sm_count,
+                              uint64_t chunk_blocks) {
+  PipelineTuning t;
+  t.chunk_blocks = chunk_blocks;
+  const uint64_t cap = pipeline_chunk_blocks(task_bound, t);
+  const uint64_t nb = total_blocks < cap ? total_blocks : cap;
+  const int nbuf = total_blocks > cap ? 2 : 1;
+  return (size_t)nbuf * chunk_buffer_bytes(nb, task_bound, sm_count);
+}
+
 size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound, int sm_count) {
   const uint64_t cap = pipeline_chunk(task_bound);
   const uint64_t nb = total_blocks < cap ? total_blocks : cap;
@@ -1963,6 +1980,7 @@ struct ChunkArgs {
   uint32_t *status;
   int sm_count;
   int anneal_ctas, yield_lanes;
+  int setup_ctas;  // per SM, cap of the setup grid
 };
 
 // Resident CTAs per SM of a kernel (queried once per process; the kernels
@@ -1989,7 +2007,7 @@ void launch_setup(const ChunkArgs &a, cudaStream_t s) {
   // one thread per fit (per block for mode 6; latency-bound; threads past
   // the class's fits return at once)
   const uint64_t fits = (uint64_t)a.nb * (class_mode(C) == 6 ? 1 : class_block_fits(C));
-  const uint64_t setup_ctas_max = (uint64_t)a.sm_count * 128;
+  const uint64_t setup_ctas_max = (uint64_t)a.sm_count * (uint64_t)a.setup_ctas;
   uint64_t setup_ctas = (fits + kSetupThreads - 1) / kSetupThreads;
   if (setup_ctas > setup_ctas_max) setup_ctas = setup_ctas_max;
   setup_kernel<C><<<(unsigned)setup_ctas, kSetupThreads, 0, s>>>(a.jobs, a.nb, a.sel, a.desc, a.local,
@@ -2079,7 +2097,7 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
   const int tmax = stats ? kMaxStatsBlockTasks : kMaxBlockTasks;
   const int tb = task_bound < 1 ? 1 : (task_bound > tmax ? tmax : task_bound);
   int e = 0;
-  const uint64_t cap = pipeline_chunk(tb);
+  const uint64_t cap = pipeline_chunk_blocks(tb, tune);
   const uint64_t nbmax = total < cap ? total : cap;
   ChunkBuf bufs[2];
   bufs[0] = carve_chunk(static_cast<uint8_t *>(scratch), nbmax, tb, sm_count);
@@ -2112,7 +2130,8 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     const uint32_t nb = (uint32_t)(total - c0 < cap ? total - c0 : cap);
     const uint64_t n8 = (uint64_t)kClasses * nb;
     const uint32_t nchunks = (uint32_t)((n8 + kRankChunk - 1) / kRankChunk);
-    const int sel_ctas = (int)((nb + 3) / 4 < (uint64_t)sm_count * 16 ? (nb + 3) / 4 : (uint64_t)sm_count * 16);
+    const uint64_t sel_max = (uint64_t)sm_count * (uint64_t)(tune.select_ctas_per_sm > 0 ? tune.select_ctas_per_sm : 16);
+    const int sel_ctas = (int)((nb + 3) / 4 < sel_max ? (nb + 3) / 4 : sel_max);
     // the chunk's texels, then its single-colour ranks (continuing the
     // earlier chunks'), before anything reads them
     if (events && events->in_ready && i < events->count) {
@@ -2134,7 +2153,8 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     emit_kernel<<<(nb + 255) / 256, 256, 0, st>>>(nb, b.counts, b.local, b.chunk, b.desc);
     const ChunkArgs args{jobs,   nb,     b.sel,  b.desc,     b.local, b.chunk, b.counts, b.ctr, b.state,
                          b.arec, b.cont, b.cont_cap, b.keys, b.perm, rank.status, sm_count,
-                         tune.anneal_ctas_per_sm < 1 ? 1 : tune.anneal_ctas_per_sm, tune.yield_lanes};
+                         tune.anneal_ctas_per_sm < 1 ? 1 : tune.anneal_ctas_per_sm, tune.yield_lanes,
+                         tune.setup_ctas_per_sm < 1 ? 128 : tune.setup_ctas_per_sm};
     if (cls) {
       const int par = i & 1;
       cudaError_t ce = cudaEventRecord(cls->fork[par], st);

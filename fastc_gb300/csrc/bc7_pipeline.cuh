@@ -133,12 +133,21 @@ void upload_pipeline_tables(int device, const uint32_t opt7[256], const uint32_t
 int block_task_bound(uint32_t modes, bool stats = false);
 // sm_count: of the device that runs the launch (bounds the continuation lists).
 size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound, int sm_count);
+// The same with chunks of `chunk_blocks` (0: the default size; larger
+// values are cut to it).
+size_t pipeline_scratch_bytes(uint64_t total_blocks, int task_bound, int sm_count,
+                              uint64_t chunk_blocks);
 // Launch parameters the plan autotuner chooses (defaults: measured best on
 // the mixed-size texture set).
 struct PipelineTuning {
   int anneal_ctas_per_sm = 5;  // persistent annealing CTAs per SM (capped by residency)
   int yield_lanes = 12;        // a warp with at most this many lanes annealing hands its fits on
+  int select_ctas_per_sm = 16; // grid of the select stage (grid-stride over the chunk's blocks)
+  int setup_ctas_per_sm = 128; // grid cap of the setup stage (one thread per fit up to it)
+  uint64_t chunk_blocks = 0;   // blocks per chunk, 0: pipeline_chunk(task bound); never more
 };
+// Blocks per chunk a launch uses for this task bound and tuning.
+uint64_t pipeline_chunk_blocks(int task_bound, const PipelineTuning &tune);
 
 // `cls` null: every stage runs in order on `stream`. `task_bound`: the most
 // block_task_bound() of the jobs' masks. `stats` not null: the logging

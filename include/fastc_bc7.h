@@ -277,17 +277,33 @@ FASTC_BC7_API uint64_t fastc_bc7_plan_blocks(fastc_bc7_plan plan);
 /* Kernel launches one fastc_bc7_plan_launch makes (kernel nodes of the
  * captured graph). */
 FASTC_BC7_API uint64_t fastc_bc7_plan_kernels(fastc_bc7_plan plan);
-/* Autotuner (replaces FasTC's fixed thread-count choice): tries the
+/* Autotuner (replaces FasTC's fixed thread-count choice, Core/src/
+ * TexComp.cpp:503-514): on the plan's own jobs, timing `launches` graph
+ * launches per candidate on `stream`, a coordinate search over the
  * pipeline's launch parameters -- persistent CTAs per SM of the annealing
- * kernels, then the lane count below which a warp hands its unfinished fits
- * on -- on the plan's own jobs, timing `launches` graph launches per
- * candidate on `stream`, and keeps the fastest graph. The plan's outputs
- * are rewritten with the same bytes (results do not depend on the launch
- * parameters). Synchronises `stream`. */
+ * kernels, the lane count below which a warp hands its unfinished fits on,
+ * blocks per chunk (the default, a half, a quarter), the select grid and
+ * the setup grid -- and, for sets of at most 65,536 blocks, the
+ * warp-per-block engine at 2, 4 or 8 warps per CTA; the fastest graph is
+ * kept. The plan's outputs are rewritten with the same bytes (results do
+ * not depend on the launch parameters or the engine). Synchronises
+ * `stream`. A plan created under the warp-per-block engine is left as is. */
 FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_autotune(fastc_bc7_plan plan, void *stream,
                                          uint32_t launches);
 FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_tuning(fastc_bc7_plan plan, int *anneal_ctas_per_sm,
                                        int *yield_lanes);
+/* Every parameter the plan's graph was captured with. */
+typedef struct {
+  int32_t engine;             /* FASTC_BC7_ENGINE_PIPELINE or _WARP_PER_BLOCK */
+  int32_t warps_per_cta;      /* warp-per-block engine */
+  int32_t anneal_ctas_per_sm; /* pipeline: persistent annealing CTAs per SM */
+  int32_t yield_lanes;        /* pipeline: hand-on threshold of the rotation classes */
+  int32_t select_ctas_per_sm; /* pipeline: select grid */
+  int32_t setup_ctas_per_sm;  /* pipeline: cap of the setup grid */
+  uint64_t chunk_blocks;      /* pipeline: blocks per chunk */
+} fastc_bc7_plan_tuning_info;
+FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_get_tuning(fastc_bc7_plan plan,
+                                                         fastc_bc7_plan_tuning_info *out);
 FASTC_BC7_API fastc_bc7_status fastc_bc7_plan_destroy(fastc_bc7_plan plan);
 
 /* --- Request server: continuous batching under a device-memory budget. ---

@@ -184,7 +184,13 @@ def test_plan_autotune_keeps_the_bytes(gpu):
         d.zero_()
     plan = Plan(jobs, s)
     t = plan.autotune(launches=1)
-    assert t["anneal_ctas_per_sm"] in (3, 4, 5, 6, 7) and t["yield_lanes"] in (8, 12, 16)
+    assert t["engine"] in (0, 1)
+    if t["engine"] == 0:  # the pipeline's parameters, from the candidate lists
+        assert t["anneal_ctas_per_sm"] in (3, 4, 5, 6, 7) and t["yield_lanes"] in (8, 12, 16)
+        assert t["select_ctas_per_sm"] in (8, 16, 32) and t["setup_ctas_per_sm"] in (6, 12, 24, 128)
+        assert t["chunk_blocks"] > 0 and t["chunk_blocks"] % 1024 == 0
+    else:  # 6,400 blocks: a small set, where the warp-per-block engine is a candidate
+        assert t["warps_per_cta"] in (2, 4, 8)
     for d in dout:
         d.zero_()
     plan.launch()
