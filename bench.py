@@ -512,6 +512,87 @@ def single_launch(img, steps: int, warmup: int, reps: int):
     return w * h / dt / 1e6, dt, din, dout, psnr(dout, din, w, h)
 
 
+def dxt_bench(imgs, din, hin, c2_img, reps: int = 5):
+    """DXT1 and DXT5 (FasTC's CompressImageDXT1 / DXT5) over the texture set:
+    device-resident jobs through fastc_dxt_compress_device (launches of up
+    to 32 jobs), timed by CUDA events over `reps` passes; the same set end
+    to end through the host-memory entry point (pinned inputs, one call per
+    texture, copies included); parity of every texture against the GPU's
+    own device path and of a band of the 2048x2048 tile mix against the
+    oracle, which is also timed on one host core for the CPU figure."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from fastc_gb300 import CompressionFormat, CompressionJob
+    from fastc_gb300._lib import Job, check, load
+    from oracle import oracle as O
+
+    lib = load()
+    stream = torch.cuda.current_stream()
+    total_px = sum(im.shape[0] * im.shape[1] for im in imgs)
+    blocks = total_px // 16
+    peak, peak_kind = measured_peaks()
+    port = O.Port()
+    band = np.ascontiguousarray(c2_img[:256])
+    res = {"workload": "texture_set_512", "texels": total_px, "blocks": blocks,
+           "l2": "inputs 462 MB > L2, no flush"}
+    for fmt in (CompressionFormat.DXT1, CompressionFormat.DXT5):
+        bsz = 8 if fmt == CompressionFormat.DXT1 else 16
+        outs = [torch.zeros(im.shape[0] * im.shape[1] * bsz // 16, dtype=torch.uint8, device="cuda")
+                for im in imgs]
+        jobs = [CompressionJob(a, o, im.shape[1], im.shape[0], format=fmt) for a, o, im in zip(din, outs, imgs)]
+        jarr = (Job * len(jobs))(*[j.to_c() for j in jobs])
+
+        def launch():
+            check(lib.fastc_dxt_compress_device(jarr, len(jobs), int(fmt), C.c_void_p(stream.cuda_stream)),
+                  "fastc_dxt_compress_device")
+
+        for _ in range(3):
+            launch()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dt = e0.elapsed_time(e1) / 1e3 / reps
+        # end to end: host buffers, one synchronous call per texture
+        houts = [np.zeros(im.shape[0] * im.shape[1] * bsz // 16, np.uint8) for im in imgs]
+        hj = [CompressionJob(a.numpy(), o, im.shape[1], im.shape[0], format=fmt).to_c()
+              for a, o, im in zip(hin, houts, imgs)]
+        for j in hj[:8]:
+            check(lib.fastc_dxt_compress(C.byref(j), int(fmt)), "fastc_dxt_compress")
+        t0 = time.perf_counter()
+        for j in hj:
+            check(lib.fastc_dxt_compress(C.byref(j), int(fmt)), "fastc_dxt_compress")
+        e2e_dt = time.perf_counter() - t0
+        same = all(np.array_equal(h, o.cpu().numpy()) for h, o in zip(houts, outs))
+        # the oracle on one core: a 2048x256 band of the 2048x2048 tile mix
+        t0 = time.perf_counter()
+        want = port.dxt_compress(band, fmt == CompressionFormat.DXT5)
+        cpu_dt = time.perf_counter() - t0
+        got = np.zeros(band.shape[0] * band.shape[1] * bsz // 16, np.uint8)
+        bj = CompressionJob(band, got, band.shape[1], band.shape[0], format=fmt).to_c()
+        check(lib.fastc_dxt_compress(C.byref(bj), int(fmt)), "fastc_dxt_compress")
+        algo = (64 + bsz) * blocks
+        res[fmt.name.lower()] = {
+            "mpix_s": total_px / dt / 1e6, "ms_per_pass": dt * 1e3, "launches_per_pass": (len(jobs) + 31) // 32,
+            "roofline": {"bound": "hbm", "achieved": algo / dt / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": algo / dt / 1e9 / peak, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_block": 64 + bsz},
+            "e2e": {"value": total_px / e2e_dt / 1e6, "unit": "MPix/s", "h2d_bytes_per_step": total_px * 4,
+                    "d2h_bytes_per_step": blocks * bsz, "calls": len(hj)},
+            "host_equals_device": bool(same),
+            "cpu_port_1core_mpix_s": band.shape[0] * band.shape[1] / cpu_dt / 1e6,
+            "band_equals_oracle": bool(np.array_equal(got, want)),
+        }
+        del outs
+    return res
+
+
 def fasTC_full_size_psnr(name: str):
     """FasTC's mean PSNR over its pinned seeds for a full-size fixture."""
     with open(os.path.join(ROOT, "tests", "golden", "manifest.json")) as f:
@@ -777,6 +858,7 @@ def main():
     plan.close()
     small_plan.close()
     if extras:
+        line["dxt"] = dxt_bench(imgs, din, hin, c2_img)
         del din, dout, hin, hout
         torch.cuda.empty_cache()
         # config 2: one 2048x2048 tile-mix texture at q50 in one launch

@@ -47,6 +47,20 @@ class BlockMode(enum.IntFlag):
     ALL = 0xFF
 
 
+class CompressionFormat(enum.IntEnum):
+    """The formats of FasTC's ECompressionFormat (Base/include/FasTC/
+    CompressionFormat.h) that this library encodes; values are the C ABI's
+    format codes (FASTC_DXT1, FASTC_DXT5; 7 for BPTC)."""
+
+    DXT1 = 1
+    DXT5 = 5
+    BPTC = 7
+
+
+#: bytes per 4x4 block of each format
+FORMAT_BLOCK_BYTES = {CompressionFormat.DXT1: 8, CompressionFormat.DXT5: 16, CompressionFormat.BPTC: 16}
+
+
 @dataclass
 class CompressionSettings:
     """BPTCC::CompressionSettings (BPTCCompressor.h:123-158) plus GPU knobs.
@@ -93,9 +107,11 @@ def _nbytes(buf) -> int:
 
 @dataclass
 class CompressionJob:
-    """FasTC::CompressionJob: RGBA8 in (width*height*4 bytes), BC7 out
-    (width*height bytes), and the raster block range [start, end) in pixel
-    coordinates; ``y_end`` past the last block row means the whole image."""
+    """FasTC::CompressionJob: RGBA8 in (width*height*4 bytes), blocks out
+    (width*height bytes for BPTC and DXT5, half that for DXT1), and the
+    raster block range [start, end) in pixel coordinates; ``y_end`` past the
+    last block row means the whole image. ``format`` is the job's
+    ECompressionFormat (CompressionJob.h:42)."""
 
     in_buf: object
     out_buf: object
@@ -105,16 +121,20 @@ class CompressionJob:
     y_start: int = 0
     x_end: Optional[int] = None
     y_end: Optional[int] = None
+    format: CompressionFormat = CompressionFormat.BPTC
 
     def __post_init__(self):
         if self.x_end is None:
             self.x_end = self.width
         if self.y_end is None:
             self.y_end = self.height
+        self.format = CompressionFormat(self.format)
         if _nbytes(self.in_buf) < self.width * self.height * 4:
             raise BC7Error(_lib.ERR_INVALID_ARGUMENT, "CompressionJob", "input smaller than width*height*4")
-        if _nbytes(self.out_buf) < self.width * self.height:
-            raise BC7Error(_lib.ERR_INVALID_ARGUMENT, "CompressionJob", "output smaller than width*height")
+        need = self.width * self.height * FORMAT_BLOCK_BYTES[self.format] // 16
+        if _nbytes(self.out_buf) < need:
+            raise BC7Error(_lib.ERR_INVALID_ARGUMENT, "CompressionJob",
+                           f"output smaller than {need} bytes for {self.format.name}")
 
     @property
     def on_device(self) -> bool:
@@ -194,6 +214,9 @@ def compress_jobs(jobs: Sequence[CompressionJob],
     sarr = _settings_array(settings if per_job else [settings or CompressionSettings()])
     jarr = (Job * len(jobs))()
     for i, j in enumerate(jobs):
+        if j.format != CompressionFormat.BPTC:
+            raise BC7Error(_lib.ERR_INVALID_ARGUMENT, "compress_jobs",
+                           f"a {j.format.name} job: use fastc_gb300.dxt")
         jarr[i] = j.to_c()
     on_dev = {j.on_device for j in jobs}
     if len(on_dev) != 1:
@@ -242,15 +265,25 @@ def compress_with_stats(job: CompressionJob, settings: Optional[CompressionSetti
 
 
 def compress_image_data(data, width: int, height: int,
-                        settings: Optional[CompressionSettings] = None) -> np.ndarray:
-    """CompressImageData (Core/include/FasTC/TexComp.h:81-88) for BC7:
-    returns width*height bytes of blocks."""
+                        settings: Optional[CompressionSettings] = None,
+                        format: CompressionFormat = CompressionFormat.BPTC) -> np.ndarray:
+    """CompressImageData (Core/include/FasTC/TexComp.h:81-88; the format
+    dispatch of Core/src/TexComp.cpp:110-134): returns the image's blocks,
+    width*height bytes for BPTC and DXT5, half that for DXT1. `settings`
+    applies to BPTC only."""
     data = np.ascontiguousarray(np.asarray(data, dtype=np.uint8))
     if width % 4 or height % 4:
         raise BC7Error(_lib.ERR_INVALID_ARGUMENT, "compress_image_data",
                        "width or height is not a multiple of the block dimension")
-    out = np.zeros(width * height, dtype=np.uint8)
-    compress(CompressionJob(data, out, width, height), settings)
+    format = CompressionFormat(format)
+    out = np.zeros(width * height * FORMAT_BLOCK_BYTES[format] // 16, dtype=np.uint8)
+    job = CompressionJob(data, out, width, height, format=format)
+    if format == CompressionFormat.BPTC:
+        compress(job, settings)
+    else:
+        from . import dxt
+
+        dxt.compress_dxt_jobs([job])
     return out
 
 

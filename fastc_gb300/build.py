@@ -35,7 +35,8 @@ SOURCES = [("bc7_kernels.cu", "bc7_kernels", []),
            ("bc7_pipeline.cu", "bc7_pipeline", []),
            ("bc7_api.cu", "bc7_api", []),
            ("bc7_server.cu", "bc7_server", []),
-           ("bc7_static.cu", "bc7_static", [])]
+           ("bc7_static.cu", "bc7_static", []),
+           ("dxt.cu", "dxt", [])]
 
 
 def nvcc() -> str:

@@ -1,0 +1,657 @@
+// DXT1 / DXT5 (BC1 / BC3) encoder and decoder for sm_103a, FasTC's second
+// compression path (DXTEncoder/src/Compressor.cpp:44-93): every 4x4 block
+// of a job through the stb_dxt v1.06 block encoder that FasTC vendors
+// (DXTEncoder/src/stb_dxt.h), with dithering and one refinement pass; DXT5
+// adds the alpha block. The method, restated per step below from its
+// published description, keeps every integer step and the float and double
+// operation order (the file is compiled without contraction), so the
+// blocks are FasTC's bit for bit. One thread per block: the work per block
+// is a few hundred instructions, all in registers.
+//
+// Jobs travel to the device inside kernel parameters (up to 32 per launch),
+// so the device entry point allocates nothing.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "bc7_host.h"
+#include "bc7_kernels.cuh"
+#include "fastc_bc7.h"
+
+namespace fastc {
+namespace {
+
+// 565 expansion by bit replication; the best endpoint pair (high, low) whose
+// 1/3 interpolant reproduces each 8-bit value, with 3 % of the endpoints'
+// distance as a penalty; the 565 quantisers of the dither (offset by 8).
+struct DxtTables {
+  uint8_t exp5[32], exp6[64];
+  uint8_t match5[256][2], match6[256][2];
+  uint8_t quant_rb[256 + 16], quant_g[256 + 16];
+};
+__constant__ DxtTables c_dxt;
+
+__host__ __device__ inline int mul8bit(int a, int b) {
+  const int t = a * b + 128;
+  return (t + (t >> 8)) >> 8;
+}
+__host__ __device__ inline int lerp13(int a, int b) { return (2 * a + b) / 3; }
+
+void build_dxt_tables(DxtTables *t) {
+  for (int i = 0; i < 32; i++) t->exp5[i] = (uint8_t)((i << 3) | (i >> 2));
+  for (int i = 0; i < 64; i++) t->exp6[i] = (uint8_t)((i << 2) | (i >> 4));
+  for (int i = 0; i < 256 + 16; i++) {
+    const int v = i < 8 ? 0 : (i - 8 > 255 ? 255 : i - 8);
+    t->quant_rb[i] = t->exp5[mul8bit(v, 31)];
+    t->quant_g[i] = t->exp6[mul8bit(v, 63)];
+  }
+  for (int pass = 0; pass < 2; pass++) {
+    const uint8_t *expand = pass ? t->exp6 : t->exp5;
+    const int size = pass ? 64 : 32;
+    uint8_t(*tab)[2] = pass ? t->match6 : t->match5;
+    for (int v = 0; v < 256; v++) {
+      int best = 256;
+      for (int lo = 0; lo < size; lo++)
+        for (int hi = 0; hi < size; hi++) {
+          int err = std::abs(lerp13(expand[hi], expand[lo]) - v);
+          err += std::abs(expand[hi] - expand[lo]) * 3 / 100;
+          if (err < best) {
+            tab[v][0] = (uint8_t)hi;
+            tab[v][1] = (uint8_t)lo;
+            best = err;
+          }
+        }
+    }
+  }
+}
+
+__device__ __forceinline__ int ch8(uint32_t p, int c) { return (int)((p >> (8 * c)) & 0xFF); }
+
+__device__ __forceinline__ uint16_t as565(int r, int g, int b) {
+  return (uint16_t)((mul8bit(r, 31) << 11) + (mul8bit(g, 63) << 5) + mul8bit(b, 31));
+}
+
+// The palette of endpoints c0, c1 as packed RGB (4-colour interpolation).
+__device__ __forceinline__ void dxt_palette(uint16_t c0, uint16_t c1, int col[4][3]) {
+  col[0][0] = c_dxt.exp5[(c0 >> 11) & 31];
+  col[0][1] = c_dxt.exp6[(c0 >> 5) & 63];
+  col[0][2] = c_dxt.exp5[c0 & 31];
+  col[1][0] = c_dxt.exp5[(c1 >> 11) & 31];
+  col[1][1] = c_dxt.exp6[(c1 >> 5) & 63];
+  col[1][2] = c_dxt.exp5[c1 & 31];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    col[2][k] = lerp13(col[0][k], col[1][k]);
+    col[3][k] = lerp13(col[1][k], col[0][k]);
+  }
+}
+
+// Floyd-Steinberg dither of each RGB channel to its 565 grid, row by row.
+__device__ __forceinline__ void dxt_dither(const uint32_t (&px)[16], uint32_t (&out)[16]) {
+#pragma unroll
+  for (int i = 0; i < 16; i++) out[i] = 0;
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) {
+    const uint8_t *q = (ch == 1 ? c_dxt.quant_g : c_dxt.quant_rb) + 8;
+    int p0 = 0, p1 = 0, p2 = 0, p3 = 0;  // the row above's errors
+#pragma unroll
+    for (int y = 0; y < 4; y++) {
+      const int s0 = ch8(px[4 * y], ch), s1 = ch8(px[4 * y + 1], ch);
+      const int s2 = ch8(px[4 * y + 2], ch), s3 = ch8(px[4 * y + 3], ch);
+      const int d0 = q[s0 + ((3 * p1 + 5 * p0) >> 4)];
+      const int e0 = s0 - d0;
+      const int d1 = q[s1 + ((7 * e0 + 3 * p2 + 5 * p1 + p0) >> 4)];
+      const int e1 = s1 - d1;
+      const int d2 = q[s2 + ((7 * e1 + 3 * p3 + 5 * p2 + p1) >> 4)];
+      const int e2 = s2 - d2;
+      const int d3 = q[s3 + ((7 * e2 + 5 * p3 + p2) >> 4)];
+      const int e3 = s3 - d3;
+      out[4 * y] |= (uint32_t)d0 << (8 * ch);
+      out[4 * y + 1] |= (uint32_t)d1 << (8 * ch);
+      out[4 * y + 2] |= (uint32_t)d2 << (8 * ch);
+      out[4 * y + 3] |= (uint32_t)d3 << (8 * ch);
+      p0 = e0;
+      p1 = e1;
+      p2 = e2;
+      p3 = e3;
+    }
+  }
+}
+
+// Indices: each texel's projection on the endpoint direction against the
+// midpoints of the palette's projections, with the projection error diffused
+// Floyd-Steinberg style.
+__device__ __forceinline__ uint32_t dxt_match(const uint32_t (&px)[16], const int (&col)[4][3]) {
+  const int dr = col[0][0] - col[1][0], dg = col[0][1] - col[1][1], db = col[0][2] - col[1][2];
+  int stops[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) stops[i] = col[i][0] * dr + col[i][1] * dg + col[i][2] * db;
+  const int c0p = ((stops[1] + stops[3]) >> 1) << 4;
+  const int half = ((stops[3] + stops[2]) >> 1) << 4;
+  const int c3p = ((stops[2] + stops[0]) >> 1) << 4;
+  int p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+  uint32_t mask = 0;
+#pragma unroll
+  for (int y = 0; y < 4; y++) {
+    int e[4];
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+      const uint32_t t = px[4 * y + x];
+      const int dot = ch8(t, 0) * dr + ch8(t, 1) * dg + ch8(t, 2) * db;
+      const int diff = x == 0 ? 3 * p1 + 5 * p0
+                       : x == 1 ? 7 * e[0] + 3 * p2 + 5 * p1 + p0
+                       : x == 2 ? 7 * e[1] + 3 * p3 + 5 * p2 + p1
+                                : 7 * e[2] + 5 * p3 + p2;
+      const int v = (dot << 4) + diff;
+      const int step = v < half ? (v < c0p ? 1 : 3) : (v < c3p ? 2 : 0);
+      e[x] = dot - stops[step];
+      mask |= (uint32_t)step << (8 * y + 2 * x);
+    }
+    p0 = e[0];
+    p1 = e[1];
+    p2 = e[2];
+    p3 = e[3];
+  }
+  return mask;
+}
+
+// Endpoints from the principal axis of the (dithered) texels: four power
+// iterations on the RGB covariance from the bounding box's extent, the
+// axis scaled to 512 (or the luma weights when it is short), the texels
+// with the least and greatest projection.
+__device__ __forceinline__ void dxt_axis(const uint32_t (&px)[16], uint16_t &max16, uint16_t &min16) {
+  int mu[3], mn[3], mx[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    int s = ch8(px[0], c), lo = s, hi = s;
+#pragma unroll
+    for (int i = 1; i < 16; i++) {
+      const int v = ch8(px[i], c);
+      s += v;
+      if (v < lo) lo = v;
+      else if (v > hi) hi = v;
+    }
+    mu[c] = (s + 8) >> 4;
+    mn[c] = lo;
+    mx[c] = hi;
+  }
+  int cov[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    const int r = ch8(px[i], 0) - mu[0], g = ch8(px[i], 1) - mu[1], b = ch8(px[i], 2) - mu[2];
+    cov[0] += r * r;
+    cov[1] += r * g;
+    cov[2] += r * b;
+    cov[3] += g * g;
+    cov[4] += g * b;
+    cov[5] += b * b;
+  }
+  float cf[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) cf[i] = __fdiv_rn((float)cov[i], 255.0f);
+  float vr = (float)(mx[0] - mn[0]), vg = (float)(mx[1] - mn[1]), vb = (float)(mx[2] - mn[2]);
+#pragma unroll
+  for (int it = 0; it < 4; it++) {
+    const float r = __fadd_rn(__fadd_rn(__fmul_rn(vr, cf[0]), __fmul_rn(vg, cf[1])), __fmul_rn(vb, cf[2]));
+    const float g = __fadd_rn(__fadd_rn(__fmul_rn(vr, cf[1]), __fmul_rn(vg, cf[3])), __fmul_rn(vb, cf[4]));
+    const float b = __fadd_rn(__fadd_rn(__fmul_rn(vr, cf[2]), __fmul_rn(vg, cf[4])), __fmul_rn(vb, cf[5]));
+    vr = r;
+    vg = g;
+    vb = b;
+  }
+  double magn = fabs((double)vr);
+  if (fabs((double)vg) > magn) magn = fabs((double)vg);
+  if (fabs((double)vb) > magn) magn = fabs((double)vb);
+  int ar, ag, ab;
+  if (magn < 4.0) {
+    ar = 299;
+    ag = 587;
+    ab = 114;
+  } else {
+    magn = __ddiv_rn(512.0, magn);
+    ar = (int)__dmul_rn((double)vr, magn);
+    ag = (int)__dmul_rn((double)vg, magn);
+    ab = (int)__dmul_rn((double)vb, magn);
+  }
+  int dmin = 0x7fffffff, dmax = -0x7fffffff;
+  uint32_t pmin = px[0], pmax = px[0];
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    const int d = ch8(px[i], 0) * ar + ch8(px[i], 1) * ag + ch8(px[i], 2) * ab;
+    if (d < dmin) {
+      dmin = d;
+      pmin = px[i];
+    }
+    if (d > dmax) {
+      dmax = d;
+      pmax = px[i];
+    }
+  }
+  max16 = as565(ch8(pmax, 0), ch8(pmax, 1), ch8(pmax, 2));
+  min16 = as565(ch8(pmin, 0), ch8(pmin, 1), ch8(pmin, 2));
+}
+
+__device__ __forceinline__ int clamp_trunc(float y, int hi) {
+  const int x = (int)y;  // toward zero; y is finite and small here
+  return x < 0 ? 0 : (x > hi ? hi : x);
+}
+
+__device__ __forceinline__ void single_colour_pair(int r, int g, int b, uint16_t &max16,
+                                                   uint16_t &min16) {
+  max16 = (uint16_t)((c_dxt.match5[r][0] << 11) | (c_dxt.match6[g][0] << 5) | c_dxt.match5[b][0]);
+  min16 = (uint16_t)((c_dxt.match5[r][1] << 11) | (c_dxt.match6[g][1] << 5) | c_dxt.match5[b][1]);
+}
+
+// Least-squares endpoints for the indices in `mask` (normal equations,
+// Cramer's rule), or the mean's single-colour pair when every texel has the
+// same index; true when the endpoints changed.
+__device__ __forceinline__ bool dxt_refine(const uint32_t (&px)[16], uint16_t &max16, uint16_t &min16,
+                                           uint32_t mask) {
+  const uint16_t old_min = min16, old_max = max16;
+  uint16_t mx16, mn16;
+  if ((mask ^ (mask << 2)) < 4) {
+    int r = 8, g = 8, b = 8;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      r += ch8(px[i], 0);
+      g += ch8(px[i], 1);
+      b += ch8(px[i], 2);
+    }
+    single_colour_pair(r >> 4, g >> 4, b >> 4, mx16, mn16);
+  } else {
+    // per index: the high endpoint's weight in thirds, and the products of
+    // the weights packed as xx << 16 | yy << 8 | xy
+    int acc = 0, a1[3] = {0, 0, 0}, a2[3] = {0, 0, 0};
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int step = (int)((mask >> (2 * i)) & 3);
+      const int w1 = step == 0 ? 3 : step == 1 ? 0 : step == 2 ? 2 : 1;
+      acc += step == 0 ? 0x090000 : step == 1 ? 0x000900 : step == 2 ? 0x040102 : 0x010402;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        a1[c] += w1 * ch8(px[i], c);
+        a2[c] += ch8(px[i], c);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) a2[c] = 3 * a2[c] - a1[c];
+    const int xx = acc >> 16, yy = (acc >> 8) & 0xff, xy = acc & 0xff;
+    const float frb = __fdiv_rn(__fdiv_rn(93.0f, 255.0f), (float)(xx * yy - xy * xy));
+    const float fg = __fdiv_rn(__fmul_rn(frb, 63.0f), 31.0f);
+    auto q = [&](int v, float f, int hi) {
+      return clamp_trunc(__fadd_rn(__fmul_rn((float)v, f), 0.5f), hi);
+    };
+    mx16 = (uint16_t)((q(a1[0] * yy - a2[0] * xy, frb, 31) << 11) |
+                      (q(a1[1] * yy - a2[1] * xy, fg, 63) << 5) | q(a1[2] * yy - a2[2] * xy, frb, 31));
+    mn16 = (uint16_t)((q(a2[0] * xx - a1[0] * xy, frb, 31) << 11) |
+                      (q(a2[1] * xx - a1[1] * xy, fg, 63) << 5) | q(a2[2] * xx - a1[2] * xy, frb, 31));
+  }
+  min16 = mn16;
+  max16 = mx16;
+  return old_min != mn16 || old_max != mx16;
+}
+
+// The 8-byte colour block: max16, min16, 32 index bits.
+__device__ __forceinline__ uint2 dxt_color_block(const uint32_t (&px)[16]) {
+  uint32_t mask;
+  uint16_t mx16, mn16;
+  bool same = true;
+#pragma unroll
+  for (int i = 1; i < 16; i++) same = same && px[i] == px[0];
+  if (same) {
+    mask = 0xaaaaaaaau;
+    single_colour_pair(ch8(px[0], 0), ch8(px[0], 1), ch8(px[0], 2), mx16, mn16);
+  } else {
+    uint32_t d[16];
+    dxt_dither(px, d);
+    dxt_axis(d, mx16, mn16);
+    int col[4][3];
+    if (mx16 != mn16) {
+      dxt_palette(mx16, mn16, col);
+      mask = dxt_match(px, col);
+    } else {
+      mask = 0;
+    }
+    if (dxt_refine(d, mx16, mn16, mask)) {
+      if (mx16 != mn16) {
+        dxt_palette(mx16, mn16, col);
+        mask = dxt_match(px, col);
+      } else {
+        mask = 0;
+      }
+    }
+  }
+  if (mx16 < mn16) {
+    const uint16_t t = mn16;
+    mn16 = mx16;
+    mx16 = t;
+    mask ^= 0x55555555u;
+  }
+  return make_uint2((uint32_t)mx16 | ((uint32_t)mn16 << 16), mask);
+}
+
+// The 8-byte alpha block: max, min, 16 3-bit indices by the bias rule.
+__device__ __forceinline__ uint2 dxt_alpha_block(const uint32_t (&px)[16]) {
+  int mn = (int)(px[0] >> 24), mx = mn;
+#pragma unroll
+  for (int i = 1; i < 16; i++) {
+    const int a = (int)(px[i] >> 24);
+    if (a < mn) mn = a;
+    else if (a > mx) mx = a;
+  }
+  const int dist = mx - mn, dist4 = dist * 4, dist2 = dist * 2;
+  const int bias = (dist < 8 ? dist - 1 : dist / 2 + 2) - mn * 7;
+  uint64_t bits = 0;
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    int a = (int)(px[i] >> 24) * 7 + bias, ind = 0;
+    if (a >= dist4) {
+      ind = 4;
+      a -= dist4;
+    }
+    if (a >= dist2) {
+      ind += 2;
+      a -= dist2;
+    }
+    ind += a >= dist;
+    ind = -ind & 7;  // the linear scale to DXT5 order: 0 and 1 are the ends
+    ind ^= 2 > ind;
+    bits |= (uint64_t)ind << (3 * i);
+  }
+  const uint64_t w = (uint64_t)mx | ((uint64_t)mn << 8) | (bits << 16);
+  return make_uint2((uint32_t)w, (uint32_t)(w >> 32));
+}
+
+constexpr int kDxtJobsPerLaunch = 32;
+struct DxtLaunch {
+  JobDev job[kDxtJobsPerLaunch];
+  uint32_t njobs;
+};
+
+// One thread per block of up to 32 jobs (their blocks in one index space).
+template <bool kAlpha>
+__global__ void __launch_bounds__(128) dxt_encode_kernel(const DxtLaunch L, uint64_t total) {
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total) return;
+  int j = 0;
+  while (j + 1 < (int)L.njobs && L.job[j + 1].begin <= g) j++;
+  const JobDev &jb = L.job[j];
+  const uint32_t lin = jb.first + (uint32_t)(g - jb.begin);
+  const uint32_t bw = jb.width >> 2, bx = lin % bw, by = lin / bw;
+  uint32_t px[16];
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const uint8_t *p = jb.in + ((size_t)(by * 4 + r - jb.row0) * jb.width + (size_t)bx * 4) * 4;
+    uint4 v;
+    if (jb.flags & kJobIn16) {
+      v = __ldg(reinterpret_cast<const uint4 *>(p));
+    } else {
+      const uint32_t *q = reinterpret_cast<const uint32_t *>(p);
+      v = make_uint4(__ldg(q), __ldg(q + 1), __ldg(q + 2), __ldg(q + 3));
+    }
+    px[4 * r] = v.x;
+    px[4 * r + 1] = v.y;
+    px[4 * r + 2] = v.z;
+    px[4 * r + 3] = v.w;
+  }
+  const uint2 c = dxt_color_block(px);
+  uint8_t *dst = jb.out + (size_t)(lin - jb.out_first) * (kAlpha ? 16 : 8);
+  if (kAlpha) {
+    const uint2 a = dxt_alpha_block(px);
+    if (jb.flags & kJobOut16) {
+      *reinterpret_cast<uint4 *>(dst) = make_uint4(a.x, a.y, c.x, c.y);
+    } else {
+      uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+      d[0] = a.x;
+      d[1] = a.y;
+      d[2] = c.x;
+      d[3] = c.y;
+    }
+  } else if ((reinterpret_cast<uintptr_t>(dst) & 7) == 0) {
+    *reinterpret_cast<uint2 *>(dst) = c;
+  } else {
+    uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+    d[0] = c.x;
+    d[1] = c.y;
+  }
+}
+
+// FasTC's decoder (DXTEncoder/src/Decompressor.cpp:26-155): one thread per
+// block, texels outside the image skipped.
+template <bool kAlpha>
+__global__ void dxt_decode_kernel(const uint8_t *__restrict__ blocks, uint8_t *__restrict__ rgba,
+                                  uint32_t width, uint32_t height) {
+  const uint32_t bw = (width + 3) / 4, bh = (height + 3) / 4;
+  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= (uint64_t)bw * bh) return;
+  const uint32_t bx = (uint32_t)(b % bw), by = (uint32_t)(b / bw);
+  const uint8_t *src = blocks + b * (kAlpha ? 16 : 8);
+  uint32_t alpha[16];
+  if (kAlpha) {
+    const int a0 = src[0], a1 = src[1];
+    uint64_t m = 0;
+    for (int k = 0; k < 6; k++) m |= (uint64_t)src[2 + k] << (8 * k);
+    for (int i = 0; i < 16; i++) {
+      const int idx = (int)((m >> (3 * i)) & 7);
+      int v;
+      if (idx < 2) v = idx ? a1 : a0;
+      else if (a0 > a1) v = ((8 - idx) * a0 + (idx - 1) * a1) / 7;
+      else v = idx < 6 ? ((6 - idx) * a0 + (idx - 1) * a1) / 5 : (idx == 6 ? 0 : 255);
+      alpha[i] = (uint32_t)v << 24;
+    }
+    src += 8;
+  } else {
+    for (int i = 0; i < 16; i++) alpha[i] = 0xFF000000u;
+  }
+  const uint16_t c0 = (uint16_t)(src[0] | (src[1] << 8)), c1 = (uint16_t)(src[2] | (src[3] << 8));
+  int col[4][3];
+  dxt_palette(c0, c1, col);  // (2a + b) / 3 and (a + 2b) / 3, as FasTC's decoder
+  if (!kAlpha && !(c0 > c1)) {
+    for (int k = 0; k < 3; k++) {
+      col[2][k] = (col[0][k] + col[1][k]) / 2;
+      col[3][k] = 0;
+    }
+  }
+  const uint32_t m = (uint32_t)src[4] | ((uint32_t)src[5] << 8) | ((uint32_t)src[6] << 16) |
+                     ((uint32_t)src[7] << 24);
+  for (int y = 0; y < 4; y++) {
+    if (by * 4 + y >= height) break;
+    for (int x = 0; x < 4; x++) {
+      if (bx * 4 + x >= width) break;
+      const int i = 4 * y + x;
+      const int *c = col[(m >> (2 * i)) & 3];
+      const uint32_t p = alpha[i] | (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16);
+      *reinterpret_cast<uint32_t *>(rgba + ((size_t)(by * 4 + y) * width + bx * 4 + x) * 4) = p;
+    }
+  }
+}
+
+std::mutex g_dxt_mu;
+bool g_dxt_ready[64];
+
+cudaError_t dxt_setup(int dev) {
+  std::lock_guard<std::mutex> lk(g_dxt_mu);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (g_dxt_ready[dev]) return cudaSuccess;
+  static DxtTables t;
+  build_dxt_tables(&t);
+  const cudaError_t e = cudaMemcpyToSymbol(c_dxt, &t, sizeof(t));
+  if (e == cudaSuccess) g_dxt_ready[dev] = true;
+  return e;
+}
+
+// Encodes up to kDxtJobsPerLaunch device jobs (dj[k].begin their block
+// offsets) in one launch.
+cudaError_t dxt_launch(const JobDev *dj, uint32_t n, uint64_t total, bool alpha, cudaStream_t st) {
+  if (total == 0) return cudaSuccess;
+  DxtLaunch L{};
+  for (uint32_t k = 0; k < n; k++) L.job[k] = dj[k];
+  L.njobs = n;
+  const unsigned grid = (unsigned)((total + 127) / 128);
+  if (alpha) dxt_encode_kernel<true><<<grid, 128, 0, st>>>(L, total);
+  else dxt_encode_kernel<false><<<grid, 128, 0, st>>>(L, total);
+  return cudaPeekAtLastError();
+}
+
+// Validates the jobs and fills their device-side descriptions (pointers
+// set by the caller); returns false on a bad job.
+bool dxt_jobs(const fastc_bc7_job *jobs, uint32_t n, std::vector<JobDev> *out) {
+  fastc_bc7_settings dflt;
+  fastc_bc7_settings_default(&dflt);
+  out->resize(n);
+  for (uint32_t i = 0; i < n; i++) {
+    uint32_t first, count;
+    if (!jobs[i].in || !jobs[i].out || !host::job_range(jobs[i], &first, &count) ||
+        (reinterpret_cast<uintptr_t>(jobs[i].in) & 3) || (reinterpret_cast<uintptr_t>(jobs[i].out) & 3))
+      return false;
+    (*out)[i] = host::make_job(jobs[i], dflt, first, count, 0);
+  }
+  return true;
+}
+
+struct DxtHostBuffers {
+  void *in = nullptr, *out = nullptr;
+  size_t in_cap = 0, out_cap = 0;
+  cudaStream_t stream = nullptr;
+  int device = -1;
+} g_dxt_host;
+
+cudaError_t ensure(void **p, size_t *cap, size_t n) {
+  if (n <= *cap) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  const cudaError_t e = cudaMalloc(p, n);
+  if (e == cudaSuccess) *cap = n;
+  return e;
+}
+
+}  // namespace
+}  // namespace fastc
+
+using fastc::JobDev;
+using namespace fastc::host;
+
+extern "C" {
+
+fastc_bc7_status fastc_dxt_compress_device(const fastc_bc7_job *jobs, uint32_t n, int format,
+                                           void *stream) {
+  if ((!jobs && n) || (format != FASTC_DXT1 && format != FASTC_DXT5))
+    return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::vector<JobDev> dj;
+  if (!fastc::dxt_jobs(jobs, n, &dj)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  const int dev = current_device();
+  if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
+  CK(fastc::dxt_setup(dev));
+  const bool alpha = format == FASTC_DXT5;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  for (uint32_t k0 = 0; k0 < n; k0 += fastc::kDxtJobsPerLaunch) {
+    const uint32_t m = std::min<uint32_t>(fastc::kDxtJobsPerLaunch, n - k0);
+    uint64_t begin = 0;
+    for (uint32_t k = 0; k < m; k++) {
+      JobDev &d = dj[k0 + k];
+      d.flags = fastc::host::align_flags(jobs[k0 + k].in, jobs[k0 + k].out);
+      if (!alpha) d.flags &= ~fastc::kJobOut16;
+      d.begin = begin;
+      begin += d.nblocks;
+    }
+    CK(fastc::dxt_launch(dj.data() + k0, m, begin, alpha, st));
+  }
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_dxt_compress(const fastc_bc7_job *job, int format) {
+  if (!job || (format != FASTC_DXT1 && format != FASTC_DXT5)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  std::vector<JobDev> dj;
+  if (!fastc::dxt_jobs(job, 1, &dj)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  JobDev &d = dj[0];
+  if (d.nblocks == 0) return FASTC_BC7_OK;
+  const int dev = current_device();
+  if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
+  CK(fastc::dxt_setup(dev));
+  const bool alpha = format == FASTC_DXT5;
+  const size_t bsz = alpha ? 16 : 8;
+  std::lock_guard<std::mutex> lk(fastc::g_dxt_mu);
+  fastc::DxtHostBuffers &h = fastc::g_dxt_host;
+  if (h.device != dev) {
+    if (h.stream) cudaStreamDestroy(h.stream);
+    h = fastc::DxtHostBuffers();
+    CK(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
+    h.device = dev;
+  }
+  // the job's texel rows up, its blocks back
+  const uint32_t bw = job->width / 4;
+  const uint32_t r0 = d.first / bw, r1 = (d.first + d.nblocks - 1) / bw;
+  const size_t in_bytes = (size_t)(r1 - r0 + 1) * 4 * job->width * 4;
+  CK(fastc::ensure(&h.in, &h.in_cap, in_bytes));
+  CK(fastc::ensure(&h.out, &h.out_cap, (size_t)d.nblocks * bsz));
+  CK(cudaMemcpyAsync(h.in, job->in + (size_t)r0 * 4 * job->width * 4, in_bytes,
+                     cudaMemcpyHostToDevice, h.stream));
+  d.in = static_cast<const uint8_t *>(h.in);
+  d.out = static_cast<uint8_t *>(h.out);
+  d.row0 = r0 * 4;
+  d.out_first = d.first;
+  d.flags = fastc::kJobIn16 | (alpha ? fastc::kJobOut16 : 0u);
+  d.begin = 0;
+  CK(fastc::dxt_launch(&d, 1, d.nblocks, alpha, h.stream));
+  CK(cudaMemcpyAsync(job->out + (size_t)d.first * bsz, h.out, (size_t)d.nblocks * bsz,
+                     cudaMemcpyDeviceToHost, h.stream));
+  CK(cudaStreamSynchronize(h.stream));
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_dxt_decompress_device(const uint8_t *blocks, uint8_t *rgba, uint32_t width,
+                                             uint32_t height, int format, void *stream) {
+  if (!blocks || !rgba || width == 0 || height == 0 || (reinterpret_cast<uintptr_t>(rgba) & 3) ||
+      (format != FASTC_DXT1 && format != FASTC_DXT5))
+    return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  const int dev = current_device();
+  if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
+  CK(fastc::dxt_setup(dev));
+  const uint64_t nb = (uint64_t)((width + 3) / 4) * ((height + 3) / 4);
+  const unsigned grid = (unsigned)((nb + 127) / 128);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (format == FASTC_DXT5) fastc::dxt_decode_kernel<true><<<grid, 128, 0, st>>>(blocks, rgba, width, height);
+  else fastc::dxt_decode_kernel<false><<<grid, 128, 0, st>>>(blocks, rgba, width, height);
+  CK(cudaPeekAtLastError());
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_dxt_decompress(const uint8_t *blocks, uint8_t *rgba, uint32_t width,
+                                      uint32_t height, int format) {
+  if (!blocks || !rgba || width == 0 || height == 0 || (format != FASTC_DXT1 && format != FASTC_DXT5))
+    return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  const int dev = current_device();
+  if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
+  CK(fastc::dxt_setup(dev));
+  const size_t nb = (size_t)((width + 3) / 4) * ((height + 3) / 4);
+  const size_t bsz = format == FASTC_DXT5 ? 16 : 8, img = (size_t)width * height * 4;
+  std::lock_guard<std::mutex> lk(fastc::g_dxt_mu);
+  fastc::DxtHostBuffers &h = fastc::g_dxt_host;
+  if (h.device != dev) {
+    if (h.stream) cudaStreamDestroy(h.stream);
+    h = fastc::DxtHostBuffers();
+    CK(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
+    h.device = dev;
+  }
+  CK(fastc::ensure(&h.in, &h.in_cap, nb * bsz));
+  CK(fastc::ensure(&h.out, &h.out_cap, img));
+  CK(cudaMemcpyAsync(h.in, blocks, nb * bsz, cudaMemcpyHostToDevice, h.stream));
+  const unsigned grid = (unsigned)((nb + 127) / 128);
+  if (format == FASTC_DXT5)
+    fastc::dxt_decode_kernel<true><<<grid, 128, 0, h.stream>>>(static_cast<const uint8_t *>(h.in),
+                                                               static_cast<uint8_t *>(h.out), width, height);
+  else
+    fastc::dxt_decode_kernel<false><<<grid, 128, 0, h.stream>>>(static_cast<const uint8_t *>(h.in),
+                                                                static_cast<uint8_t *>(h.out), width, height);
+  CK(cudaPeekAtLastError());
+  CK(cudaMemcpyAsync(rgba, h.out, img, cudaMemcpyDeviceToHost, h.stream));
+  CK(cudaStreamSynchronize(h.stream));
+  return FASTC_BC7_OK;
+}
+
+}  // extern "C"

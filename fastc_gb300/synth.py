@@ -154,6 +154,17 @@ def tile_mix_radial_alpha(seed: int = 5, width: int = 8192, height: int = 8192, 
     return img
 
 
+def flat_blocks(seed: int = 0, width: int = 64, height: int = 64) -> np.ndarray:
+    """Every 4x4 block one colour: block k has R = k, G = 255 - k, B = 37k,
+    A = 91k (mod 256), offset by `seed`, so a 64x64 image walks every value
+    of every channel once. Exercises single-colour encodings."""
+    bx = np.arange(width // 4)[None, :]
+    by = np.arange(height // 4)[:, None]
+    k = (by * (width // 4) + bx + seed) % 256
+    blk = np.stack([k, 255 - k, (37 * k) % 256, (91 * k) % 256], -1).astype(np.uint8)
+    return np.ascontiguousarray(blk.repeat(4, 0).repeat(4, 1))
+
+
 def texture_sides(seed: int, count: int, lo_log2: int = 4, hi_log2: int = 11):
     """Side lengths 2^U{lo..hi} drawn independently per axis."""
     n = hi_log2 - lo_log2 + 1

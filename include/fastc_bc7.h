@@ -373,6 +373,35 @@ FASTC_BC7_API int fastc_bc7_get_engine(void);
 FASTC_BC7_API fastc_bc7_status fastc_bc7_set_launch_shape(int warps_per_cta, int ctas_per_sm);
 FASTC_BC7_API fastc_bc7_status fastc_bc7_get_launch_shape(int *warps_per_cta, int *ctas_per_sm);
 
+/* ---- DXT1 / DXT5 (BC1 / BC3) ----
+ * FasTC's DXT path: DXTC::CompressImageDXT1 / CompressImageDXT5
+ * (DXTEncoder/include/FasTC/DXTCompressor.h:24-25, Compressor.cpp:47-93),
+ * the stb_dxt block encoder with dithering, and DXTC::DecompressDXT1 /
+ * DecompressDXT5 (DXTCompressor.h:27-28, Decompressor.cpp:98-155). A job is
+ * the same fastc_bc7_job (width and height multiples of 4, the same
+ * x/y start/end walk); only `in`, `out`, the sizes and the range are read.
+ * Blocks are 8 bytes (DXT1) or 16 bytes (DXT5: alpha block, then colour
+ * block) and land at out + block_index * size, block_index counted from the
+ * texture's first block, as in FasTC. `in` and `out` must be 4-byte aligned.
+ * The output equals FasTC's byte for byte. */
+#define FASTC_DXT1 1
+#define FASTC_DXT5 5
+/* Host buffers; returns when `out` holds the blocks. */
+FASTC_BC7_API fastc_bc7_status fastc_dxt_compress(const fastc_bc7_job *job, int format);
+/* Device buffers, enqueued on `stream` (NULL: the legacy default stream);
+ * allocates nothing. The first DXT call on a device uploads the encoder's
+ * tables (a synchronous copy): make it outside stream capture. */
+FASTC_BC7_API fastc_bc7_status fastc_dxt_compress_device(const fastc_bc7_job *jobs, uint32_t n,
+                                                        int format, void *stream);
+/* Blocks of a width x height image (rounded up to whole blocks) to RGBA8
+ * texels (4-byte aligned); texels past the image edge are not written.
+ * DXT1 blocks with c0 <= c1 decode as 3 colours and black, alpha 255. */
+FASTC_BC7_API fastc_bc7_status fastc_dxt_decompress(const uint8_t *blocks, uint8_t *rgba,
+                                                   uint32_t width, uint32_t height, int format);
+FASTC_BC7_API fastc_bc7_status fastc_dxt_decompress_device(const uint8_t *blocks, uint8_t *rgba,
+                                                          uint32_t width, uint32_t height,
+                                                          int format, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

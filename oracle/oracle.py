@@ -119,6 +119,9 @@ class Port:
         lib.bc7o_expf.restype = C.c_float
         lib.bc7o_trace_block.argtypes = [_u32p, C.POINTER(Settings), C.c_uint32, C.c_uint32,
                                           _u32p, _u32p, _u8p, C.POINTER(FitTrace), C.c_int]
+        lib.dxto_compress.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32, C.c_int]
+        lib.dxto_decompress.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32, C.c_int]
+        lib.dxto_tables.argtypes = [_u8p, _u8p]
         lib.bc7o_trace_block.restype = C.c_int
         lib.bc7o_compress_block_stats.argtypes = [_u32p, C.POINTER(Settings), C.c_uint32,
                                                   C.c_uint32, _u32p, _u32p, _u8p,
@@ -225,6 +228,27 @@ class Port:
         self.lib.bc7o_block_sse(_ptr(a), _ptr(b), w, h, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
+    def dxt_compress(self, img: np.ndarray, alpha: bool) -> np.ndarray:
+        """The DXT restatement (oracle/dxt_oracle.c): DXT5 when `alpha`."""
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape[:2]
+        out = np.zeros((w // 4) * (h // 4) * (16 if alpha else 8), dtype=np.uint8)
+        if self.lib.dxto_compress(_ptr(img), _ptr(out), w, h, int(alpha)):
+            raise ValueError("dxto_compress: sizes must be multiples of 4")
+        return out
+
+    def dxt_decompress(self, blocks: np.ndarray, w: int, h: int, alpha: bool) -> np.ndarray:
+        blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+        out = np.zeros((h, w, 4), dtype=np.uint8)
+        self.lib.dxto_decompress(_ptr(blocks), _ptr(out), w, h, int(alpha))
+        return out
+
+    def dxt_tables(self):
+        m5 = np.zeros(512, dtype=np.uint8)
+        m6 = np.zeros(512, dtype=np.uint8)
+        self.lib.dxto_tables(_ptr(m5), _ptr(m6))
+        return m5, m6
+
     def box_selection(self, px: np.ndarray, metric=0):
         px = np.ascontiguousarray(px, dtype=np.uint32)
         out = np.zeros(4, dtype=np.uint32)
@@ -260,7 +284,23 @@ class Reference:
         lib.ref_compress_stats.argtypes = [_u8p, _u8p] + [C.c_uint32] * 8 + [C.c_int, C.c_char_p,
                                                                           C.c_size_t]
         lib.ref_compress_stats.restype = C.c_size_t
+        lib.ref_dxt_compress.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32, C.c_int]
+        lib.ref_dxt_decompress.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32, C.c_int]
         self.lib = lib
+
+    def dxt_compress(self, img: np.ndarray, alpha: bool) -> np.ndarray:
+        """DXTC::CompressImageDXT1 / DXT5 over the whole image."""
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape[:2]
+        out = np.zeros((w // 4) * (h // 4) * (16 if alpha else 8), dtype=np.uint8)
+        self.lib.ref_dxt_compress(_ptr(img), _ptr(out), w, h, int(alpha))
+        return out
+
+    def dxt_decompress(self, blocks: np.ndarray, w: int, h: int, alpha: bool) -> np.ndarray:
+        blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+        out = np.zeros((h, w, 4), dtype=np.uint8)
+        self.lib.ref_dxt_decompress(_ptr(blocks), _ptr(out), w, h, int(alpha))
+        return out
 
     def compress_stats(self, img: np.ndarray, steps=0, modes=0xFF, metric=0, seed=None, wm=0):
         """BPTCC::CompressWithStats with a log stream: (blocks, log text).

@@ -15,6 +15,11 @@
 //                            (Compressor.cpp:140)
 //   * ref_tables          -> the two endpoint lookup tables used on the
 //                            encode path (BCLookupTables.h:97,710)
+//   * ref_dxt_compress    -> DXTC::CompressImageDXT1 / DXT5
+//                            (DXTEncoder/src/Compressor.cpp:44-93, compiled
+//                            from its own file by the Makefile)
+//   * ref_dxt_decompress  -> DXTC::DecompressDXT1 / DXT5
+//                            (DXTEncoder/src/Decompressor.cpp:94-155)
 //
 // g_seed is seeded from time(NULL) at load time, which makes q>0 output
 // nondeterministic; the tests pin it with ref_set_seed before every call.
@@ -24,6 +29,8 @@
 #include "Compressor.cpp"
 
 #include <cstdint>
+
+#include "FasTC/DXTCompressor.h"
 
 extern "C" {
 
@@ -106,6 +113,21 @@ size_t ref_compress_stats(const uint8_t *rgba, uint8_t *out, uint32_t w, uint32_
 void ref_tables(uint8_t opt7[512], uint8_t opt6[1536]) {
   memcpy(opt7, ::Optimal7CompressBC7Mode5, 512);
   memcpy(opt6, ::Optimal6CompressDXT1, 1536);
+}
+
+
+void ref_dxt_compress(const uint8_t *rgba, uint8_t *out, uint32_t w, uint32_t h, int alpha) {
+  FasTC::CompressionJob cj(alpha ? FasTC::eCompressionFormat_DXT5 : FasTC::eCompressionFormat_DXT1,
+                           rgba, out, w, h);
+  if (alpha) DXTC::CompressImageDXT5(cj);
+  else DXTC::CompressImageDXT1(cj);
+}
+
+void ref_dxt_decompress(const uint8_t *blocks, uint8_t *rgba, uint32_t w, uint32_t h, int alpha) {
+  FasTC::DecompressionJob dj(alpha ? FasTC::eCompressionFormat_DXT5 : FasTC::eCompressionFormat_DXT1,
+                             blocks, rgba, w, h);
+  if (alpha) DXTC::DecompressDXT5(dj);
+  else DXTC::DecompressDXT1(dj);
 }
 
 }  // extern "C"

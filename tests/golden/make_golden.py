@@ -1,4 +1,4 @@
-"""Regenerate the golden BC7 fixtures from FasTC's own encoder.
+"""Regenerate the golden BC7 and DXT fixtures from FasTC's own encoders.
 
 Runs only where the FasTC checkout is available (it builds
 oracle/_ref/libfastc_ref.so from those sources in place):
@@ -61,6 +61,29 @@ FULL_SIZE = {
     "c2_tile2048_q50": ("tile_mix(2, 2048, 2048)", 50, [11, 22, 33]),
     "c5_stripe8192x512_q100": ("tile_mix_radial_alpha(5, 8192, 512, 0, 3840)", 100, [11, 22, 33]),
 }
+
+# DXT1 / DXT5: name -> (generator call, format); FasTC's CompressImageDXT1 /
+# CompressImageDXT5 blocks and its decoder's texels of them
+DXT = {
+    "dxt1_tile": ("tile_mix(2, 128, 128)", 1),
+    "dxt5_tile": ("tile_mix(2, 128, 128)", 5),
+    "dxt1_gradient": ("gradient_noise_alpha_ramp(1, 128, 64)", 1),
+    "dxt5_radial": ("tile_mix_radial_alpha(5, 128, 128, 1000, 2000)", 5),
+    "dxt1_flat": ("flat_blocks(0, 64, 64)", 1),
+    "dxt5_flat": ("flat_blocks(3, 64, 64)", 5),
+}
+# random block bytes, numpy default_rng(seed).integers(0, 256), decoded by
+# FasTC's decoder: name -> (width, height, format, seed); the sizes are not
+# multiples of 4, so the decoder's edge clipping is covered too
+DXT_DECODE = {
+    "dxt1_random_decode": (62, 45, 1, 101),
+    "dxt5_random_decode": (61, 46, 5, 102),
+}
+
+
+def dxt_random_blocks(w: int, h: int, fmt: int, seed: int) -> np.ndarray:
+    n = ((w + 3) // 4) * ((h + 3) // 4) * (8 if fmt == 1 else 16)
+    return np.random.default_rng(seed).integers(0, 256, n, dtype=np.uint8)
 
 
 def make(expr: str) -> np.ndarray:
@@ -148,6 +171,24 @@ def make_full_size(manifest, workers):
         print(name, [r[2] for r in rows])
 
 
+def make_dxt(ref, manifest):
+    manifest["dxt"] = {}
+    for name, (expr, fmt) in DXT.items():
+        img = make(expr)
+        blocks = ref.dxt_compress(img, fmt == 5)
+        blocks.tofile(os.path.join(HERE, name + ".bin"))
+        dec = ref.dxt_decompress(blocks, img.shape[1], img.shape[0], fmt == 5)
+        manifest["dxt"][name] = {"image": expr, "format": fmt, "input_sha256": sha(img),
+                                 "blocks_sha256": sha(blocks), "decoded_sha256": sha(dec)}
+        print(name, len(blocks), "bytes")
+    for name, (w, h, fmt, seed) in DXT_DECODE.items():
+        blocks = dxt_random_blocks(w, h, fmt, seed)
+        dec = ref.dxt_decompress(blocks, w, h, fmt == 5)
+        manifest["dxt"][name] = {"width": w, "height": h, "format": fmt, "rng_seed": seed,
+                                 "blocks_sha256": sha(blocks), "decoded_sha256": sha(dec)}
+        print(name)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=O.DEFAULT_REFERENCE)
@@ -155,16 +196,20 @@ def main():
                     help="only (re)write the CompressWithStats fixtures")
     ap.add_argument("--full-size-only", action="store_true",
                     help="only (re)write the full-size PSNR / per-block SSE fixtures")
+    ap.add_argument("--dxt-only", action="store_true",
+                    help="only (re)write the DXT1 / DXT5 fixtures")
     ap.add_argument("--workers", type=int, default=6)
     args = ap.parse_args()
     if not O.build_ref(args.reference):
         sys.exit("FasTC checkout not found; cannot regenerate fixtures")
     ref = O.Reference()
-    if args.stats_only or args.full_size_only:
+    if args.stats_only or args.full_size_only or args.dxt_only:
         with open(os.path.join(HERE, "manifest.json")) as f:
             manifest = json.load(f)
         if args.stats_only:
             make_stats(ref, manifest)
+        elif args.dxt_only:
+            make_dxt(ref, manifest)
         else:
             make_full_size(manifest, args.workers)
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
@@ -201,6 +246,7 @@ def main():
     o7, o6 = ref.tables()
     np.savez(os.path.join(HERE, "endpoint_tables.npz"), opt7=o7, opt6=o6)
     make_stats(ref, manifest)
+    make_dxt(ref, manifest)
     make_full_size(manifest, args.workers)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)

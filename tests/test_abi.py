@@ -13,7 +13,7 @@ from conftest import ROOT
 def declared_functions():
     src = open(os.path.join(ROOT, "include", "fastc_bc7.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(fastc_bc7_\w+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(fastc_(?:bc7|dxt)_\w+)\s*\(", src)))
 
 
 def test_header_and_binding_agree():
@@ -129,3 +129,37 @@ def test_no_device_fails_loudly(bc7lib):
 
     with pytest.raises(BC7Error):
         compress_image_data(np.zeros((8, 8, 4), np.uint8), 8, 8)
+
+
+def test_dxt_invalid_arguments_rejected(bc7lib):
+    from fastc_gb300._lib import Job
+
+    buf = (C.c_uint8 * 4096)()
+    addr = C.addressof(buf)
+    ok = Job(addr, addr, 8, 8, 0, 0, 8, 8)
+    assert bc7lib.fastc_dxt_compress(C.byref(ok), 3) == 1                      # no such format
+    assert bc7lib.fastc_dxt_compress(C.byref(Job(addr, addr, 6, 8, 0, 0, 6, 8)), 1) == 1
+    assert bc7lib.fastc_dxt_compress(C.byref(Job(addr + 2, addr, 8, 8, 0, 0, 8, 8)), 5) == 1
+    assert bc7lib.fastc_dxt_compress(C.byref(Job(0, addr, 8, 8, 0, 0, 8, 8)), 1) == 1
+    assert bc7lib.fastc_dxt_compress_device(None, 1, 1, None) == 1
+    assert bc7lib.fastc_dxt_decompress(None, C.cast(addr, C.POINTER(C.c_uint8)), 8, 8, 5) == 1
+    assert bc7lib.fastc_dxt_decompress_device(addr, addr, 0, 8, 1, None) == 1
+
+
+def test_dxt_job_output_sizes():
+    from fastc_gb300 import BC7Error, CompressionFormat, CompressionJob
+
+    img = np.zeros((8, 8, 4), np.uint8)
+    CompressionJob(img, np.zeros(32, np.uint8), 8, 8, format=CompressionFormat.DXT1)
+    with pytest.raises(BC7Error):
+        CompressionJob(img, np.zeros(32, np.uint8), 8, 8, format=CompressionFormat.DXT5)
+    with pytest.raises(BC7Error):
+        CompressionJob(img, np.zeros(32, np.uint8), 8, 8)
+
+
+def test_bptc_entry_rejects_dxt_jobs():
+    from fastc_gb300 import BC7Error, CompressionFormat, CompressionJob, compress
+
+    img = np.zeros((8, 8, 4), np.uint8)
+    with pytest.raises(BC7Error):
+        compress(CompressionJob(img, np.zeros(64, np.uint8), 8, 8, format=CompressionFormat.DXT5))

@@ -1,0 +1,167 @@
+"""DXT1 / DXT5 on the GPU (fastc_dxt_* through the C ABI) against FasTC's
+own blocks and decoded texels (tests/golden/dxt*.bin, made by the reference)
+and against the oracle (oracle/dxt_oracle.c) on larger seeded images, sub-
+jobs, many-job launches, unaligned buffers and random block bytes.
+Everything is compared bit for bit."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_blocks, make_image
+
+pytestmark = pytest.mark.gpu
+
+ENCODE = ["dxt1_tile", "dxt5_tile", "dxt1_gradient", "dxt5_radial", "dxt1_flat", "dxt5_flat"]
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def fmt_of(code):
+    from fastc_gb300 import CompressionFormat
+
+    return CompressionFormat(code)
+
+
+def bsz(code):
+    return 8 if code == 1 else 16
+
+
+def gpu_compress(img, code, rect=None):
+    from fastc_gb300 import CompressionJob, dxt
+
+    h, w = img.shape[:2]
+    out = np.zeros(w * h * bsz(code) // 16, np.uint8)
+    dxt.compress_dxt_jobs([CompressionJob(np.ascontiguousarray(img), out, w, h, *(rect or ()),
+                                          format=fmt_of(code))])
+    return out
+
+
+def gpu_compress_device(img, code, dev, in_off=0, out_off=0):
+    import torch
+
+    from fastc_gb300 import CompressionJob, dxt
+
+    h, w = img.shape[:2]
+    n = w * h * bsz(code) // 16
+    tin = torch.zeros(img.size + in_off, dtype=torch.uint8, device=dev)
+    tin[in_off:] = torch.from_numpy(img.reshape(-1)).to(dev)
+    tout = torch.zeros(n + out_off, dtype=torch.uint8, device=dev)
+    dxt.compress_dxt_jobs([CompressionJob(tin[in_off:], tout[out_off:], w, h, format=fmt_of(code))])
+    return tout[out_off:].cpu().numpy()
+
+
+@pytest.mark.parametrize("name", ENCODE)
+def test_blocks_equal_fasTC(gpu, manifest, name):
+    case = manifest["dxt"][name]
+    img = make_image(case["image"])
+    want = golden_blocks(name)
+    for got in (gpu_compress(img, case["format"]), gpu_compress_device(img, case["format"], gpu)):
+        b = bsz(case["format"])
+        bad = np.nonzero((got.reshape(-1, b) != want.reshape(-1, b)).any(1))[0]
+        assert bad.size == 0, (bad.size, bad[:8])
+
+
+@pytest.mark.parametrize("name", ENCODE)
+def test_decoder_equals_fasTC(gpu, manifest, name):
+    import torch
+
+    from fastc_gb300 import dxt
+
+    case = manifest["dxt"][name]
+    img = make_image(case["image"])
+    h, w = img.shape[:2]
+    blocks = golden_blocks(name)
+    assert sha(dxt.decompress(blocks, w, h, fmt_of(case["format"]))) == case["decoded_sha256"]
+    dev = dxt.decompress(torch.from_numpy(blocks).to(gpu), w, h, fmt_of(case["format"]))
+    assert sha(dev.cpu().numpy()) == case["decoded_sha256"]
+
+
+@pytest.mark.parametrize("name", ["dxt1_random_decode", "dxt5_random_decode"])
+def test_decoder_on_random_blocks_equals_fasTC(gpu, manifest, name):
+    import torch
+
+    from fastc_gb300 import dxt
+
+    case = manifest["dxt"][name]
+    w, h, code = case["width"], case["height"], case["format"]
+    n = ((w + 3) // 4) * ((h + 3) // 4) * bsz(code)
+    blocks = np.random.default_rng(case["rng_seed"]).integers(0, 256, n, dtype=np.uint8)
+    assert sha(dxt.decompress(blocks, w, h, fmt_of(code))) == case["decoded_sha256"]
+    dev = dxt.decompress(torch.from_numpy(blocks).to(gpu), w, h, fmt_of(code))
+    assert sha(dev.cpu().numpy()) == case["decoded_sha256"]
+
+
+@pytest.mark.parametrize("expr", [
+    "tile_mix(5, 1024, 512)",
+    "tile_mix_radial_alpha(6, 512, 512, 2000, 3000)",
+    "gradient_noise_alpha_ramp(4, 256, 768)",
+])
+@pytest.mark.parametrize("code", [1, 5])
+def test_larger_images_equal_oracle(gpu, port, expr, code):
+    img = make_image(expr)
+    want = port.dxt_compress(img, code == 5)
+    assert np.array_equal(gpu_compress(img, code), want)
+    assert np.array_equal(gpu_compress_device(img, code, gpu), want)
+
+
+@pytest.mark.parametrize("code", [1, 5])
+def test_unaligned_buffers(gpu, port, code):
+    img = make_image("tile_mix(8, 64, 32)")
+    want = port.dxt_compress(img, code == 5)
+    # 4-byte aligned but not 16 (input) or 8 / 16 (output): the narrow loads and stores
+    assert np.array_equal(gpu_compress_device(img, code, gpu, in_off=4, out_off=4), want)
+    assert np.array_equal(gpu_compress_device(img, code, gpu, in_off=8, out_off=8), want)
+
+
+@pytest.mark.parametrize("code", [1, 5])
+def test_sub_job_writes_its_range_only(gpu, port, code):
+    img = make_image("tile_mix(74, 64, 64)")
+    full = port.dxt_compress(img, code == 5)
+    got = gpu_compress(img, code, rect=(16, 8, 32, 40))
+    b = bsz(code)
+    first, last = 2 * 16 + 4, 10 * 16 + 8  # FasTC's raster walk, end exclusive
+    assert np.array_equal(got[b * first:b * last], full[b * first:b * last])
+    assert not got[:b * first].any() and not got[b * last:].any()
+
+
+@pytest.mark.parametrize("code", [1, 5])
+def test_many_device_jobs_in_one_call(gpu, port, code):
+    """70 textures of mixed sizes: three launches of up to 32 jobs."""
+    import torch
+
+    from fastc_gb300 import CompressionJob, dxt, synth
+
+    texs = synth.texture_set(seed=9, count=70, lo_log2=2, hi_log2=7)
+    jobs, outs = [], []
+    for t in texs:
+        h, w = t.shape[:2]
+        tin = torch.from_numpy(t.reshape(-1)).to(gpu)
+        tout = torch.zeros(w * h * bsz(code) // 16, dtype=torch.uint8, device=gpu)
+        jobs.append(CompressionJob(tin, tout, w, h, format=fmt_of(code)))
+        outs.append(tout)
+    dxt.compress_dxt_jobs(jobs)
+    for t, o in zip(texs, outs):
+        assert np.array_equal(o.cpu().numpy(), port.dxt_compress(t, code == 5))
+
+
+def test_compress_image_data_dispatches_on_format(gpu, port):
+    from fastc_gb300 import CompressionFormat, compress_image_data
+
+    img = make_image("tile_mix_radial_alpha(3, 128, 64, 300, 400)")
+    for f in (CompressionFormat.DXT1, CompressionFormat.DXT5):
+        got = compress_image_data(img, 128, 64, format=f)
+        assert np.array_equal(got, port.dxt_compress(img, f == CompressionFormat.DXT5))
+
+
+def test_round_trip_quality(gpu):
+    from fastc_gb300 import CompressionFormat, compress_image_data, dxt
+
+    img = make_image("tile_mix(12, 256, 256)")
+    for f in (CompressionFormat.DXT1, CompressionFormat.DXT5):
+        dec = dxt.decompress(compress_image_data(img, 256, 256, format=f), 256, 256, f)
+        err = dec[..., :3].astype(np.int64) - img[..., :3]
+        mse = float((err * err).mean())
+        assert 10 * np.log10(255.0 ** 2 / mse) > 28.0
