@@ -157,11 +157,20 @@ def test_compress_image_data_dispatches_on_format(gpu, port):
 
 
 def test_round_trip_quality(gpu):
+    """A smooth gradient survives the round trip at over 40 dB RGB PSNR
+    (43.8 dB with the oracle); DXT5 alpha within half a palette step
+    (1/14 of the block's alpha range) plus one of the original."""
     from fastc_gb300 import CompressionFormat, compress_image_data, dxt
 
-    img = make_image("tile_mix(12, 256, 256)")
+    img = make_image("gradient_noise_alpha_ramp(1, 256, 256)")
     for f in (CompressionFormat.DXT1, CompressionFormat.DXT5):
         dec = dxt.decompress(compress_image_data(img, 256, 256, format=f), 256, 256, f)
         err = dec[..., :3].astype(np.int64) - img[..., :3]
         mse = float((err * err).mean())
-        assert 10 * np.log10(255.0 ** 2 / mse) > 28.0
+        assert 10 * np.log10(255.0 ** 2 / mse) > 40.0
+        if f == CompressionFormat.DXT1:
+            assert (dec[..., 3] == 255).all()
+        else:
+            a = img[..., 3].reshape(64, 4, 64, 4).astype(int)
+            span = (a.max((1, 3)) - a.min((1, 3)))[:, None, :, None]
+            assert (np.abs(dec[..., 3].reshape(64, 4, 64, 4).astype(int) - a) <= span / 14 + 1).all()
