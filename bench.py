@@ -516,8 +516,8 @@ def dxt_bench(imgs, din, hin, c2_img, reps: int = 5):
     """DXT1 and DXT5 (FasTC's CompressImageDXT1 / DXT5) over the texture set:
     device-resident jobs through fastc_dxt_compress_device (launches of up
     to 32 jobs), timed by CUDA events over `reps` passes; the same set end
-    to end through the host-memory entry point (pinned inputs, one call per
-    texture, copies included); parity of every texture against the GPU's
+    to end through the batched host-memory entry point (pinned buffers,
+    copies included); parity of every texture against the GPU's
     own device path and of a band of the 2048x2048 tile mix against the
     oracle, which is also timed on one host core for the CPU figure."""
     import ctypes as C
@@ -559,17 +559,18 @@ def dxt_bench(imgs, din, hin, c2_img, reps: int = 5):
         e1.record(stream)
         torch.cuda.synchronize()
         dt = e0.elapsed_time(e1) / 1e3 / reps
-        # end to end: host buffers, one synchronous call per texture
-        houts = [np.zeros(im.shape[0] * im.shape[1] * bsz // 16, np.uint8) for im in imgs]
-        hj = [CompressionJob(a.numpy(), o, im.shape[1], im.shape[0], format=fmt).to_c()
-              for a, o, im in zip(hin, houts, imgs)]
-        for j in hj[:8]:
-            check(lib.fastc_dxt_compress(C.byref(j), int(fmt)), "fastc_dxt_compress")
+        # end to end: pinned host buffers, the whole set in one batched call
+        houts = [torch.zeros(im.shape[0] * im.shape[1] * bsz // 16, dtype=torch.uint8).pin_memory()
+                 for im in imgs]
+        hj = (Job * len(imgs))(*[CompressionJob(a.numpy(), o.numpy(), im.shape[1], im.shape[0],
+                                                format=fmt).to_c() for a, o, im in zip(hin, houts, imgs)])
+        check(lib.fastc_dxt_compress_batch(hj, len(imgs), int(fmt)), "fastc_dxt_compress_batch")
+        e2e_reps = 3
         t0 = time.perf_counter()
-        for j in hj:
-            check(lib.fastc_dxt_compress(C.byref(j), int(fmt)), "fastc_dxt_compress")
-        e2e_dt = time.perf_counter() - t0
-        same = all(np.array_equal(h, o.cpu().numpy()) for h, o in zip(houts, outs))
+        for _ in range(e2e_reps):
+            check(lib.fastc_dxt_compress_batch(hj, len(imgs), int(fmt)), "fastc_dxt_compress_batch")
+        e2e_dt = (time.perf_counter() - t0) / e2e_reps
+        same = all(np.array_equal(h.numpy(), o.cpu().numpy()) for h, o in zip(houts, outs))
         # the oracle on one core: a 2048x256 band of the 2048x2048 tile mix
         t0 = time.perf_counter()
         want = port.dxt_compress(band, fmt == CompressionFormat.DXT5)
@@ -584,7 +585,8 @@ def dxt_bench(imgs, din, hin, c2_img, reps: int = 5):
                          "frac": algo / dt / 1e9 / peak, "peak_source": peak_kind,
                          "algorithmic_bytes_per_block": 64 + bsz},
             "e2e": {"value": total_px / e2e_dt / 1e6, "unit": "MPix/s", "h2d_bytes_per_step": total_px * 4,
-                    "d2h_bytes_per_step": blocks * bsz, "calls": len(hj)},
+                    "d2h_bytes_per_step": blocks * bsz, "entry": "fastc_dxt_compress_batch, pinned buffers",
+                    "copy_gb_s": (total_px * 4 + blocks * bsz) / e2e_dt / 1e9},
             "host_equals_device": bool(same),
             "cpu_port_1core_mpix_s": band.shape[0] * band.shape[1] / cpu_dt / 1e6,
             "band_equals_oracle": bool(np.array_equal(got, want)),
@@ -615,22 +617,27 @@ def profile_case(args):
 
     from fastc_gb300 import CompressionJob, CompressionSettings, compress, set_launch_shape
 
-    from fastc_gb300 import set_engine
+    from fastc_gb300 import CompressionFormat, dxt, set_engine
 
     set_engine(args.case_engine)
     set_launch_shape(args.case_warps, 0)
+    fmt = CompressionFormat[args.case_format.upper()]
     din = torch.from_numpy(img).cuda()
-    dout = torch.zeros(n * n, dtype=torch.uint8, device="cuda")
+    dout = torch.zeros(n * n * (8 if fmt == CompressionFormat.DXT1 else 16) // 16, dtype=torch.uint8,
+                       device="cuda")
     s = CompressionSettings(num_simulated_annealing_steps=args.case_steps, seed=1)
-    job = CompressionJob(din, dout, n, n)
+    job = CompressionJob(din, dout, n, n, format=fmt)
+    what = f"q{args.case_steps}" if fmt == CompressionFormat.BPTC else fmt.name
     for _ in range(args.case_repeat):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        compress(job, s)
+        if fmt == CompressionFormat.BPTC:
+            compress(job, s)
+        else:
+            dxt.compress_dxt_jobs([job])
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        print(f"{args.case_kind} {n}x{n} q{args.case_steps}: {dt * 1e3:.2f} ms, "
-              f"{n * n / dt / 1e6:.2f} MPix/s")
+        print(f"{args.case_kind} {n}x{n} {what}: {dt * 1e3:.2f} ms, {n * n / dt / 1e6:.2f} MPix/s")
 
 
 def main():
@@ -656,6 +663,7 @@ def main():
     ap.add_argument("--case-kind", default="tile_mix", choices=["tile_mix", "radial", "gradient"])
     ap.add_argument("--case-size", type=int, default=4096)
     ap.add_argument("--case-steps", type=int, default=50)
+    ap.add_argument("--case-format", default="bptc", choices=["bptc", "dxt1", "dxt5"])
     ap.add_argument("--case-repeat", type=int, default=1)
     ap.add_argument("--case-engine", type=int, default=0,
                     help="0: pipeline engine, 1: warp-per-block engine")

@@ -139,6 +139,7 @@ SIGNATURES = {
     "fastc_bc7_block_error_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                                C.c_void_p, C.c_void_p, C.c_void_p]),
     "fastc_dxt_compress": (C.c_int, [C.POINTER(Job), C.c_int]),
+    "fastc_dxt_compress_batch": (C.c_int, [C.POINTER(Job), C.c_uint32, C.c_int]),
     "fastc_dxt_compress_device": (C.c_int, [C.POINTER(Job), C.c_uint32, C.c_int, C.c_void_p]),
     "fastc_dxt_decompress": (C.c_int, [u8p, u8p, C.c_uint32, C.c_uint32, C.c_int]),
     "fastc_dxt_decompress_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int,

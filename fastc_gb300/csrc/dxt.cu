@@ -25,49 +25,45 @@
 namespace fastc {
 namespace {
 
-// 565 expansion by bit replication; the best endpoint pair (high, low) whose
-// 1/3 interpolant reproduces each 8-bit value, with 3 % of the endpoints'
-// distance as a penalty; the 565 quantisers of the dither (offset by 8).
-struct DxtTables {
-  uint8_t exp5[32], exp6[64];
-  uint8_t match5[256][2], match6[256][2];
-  uint8_t quant_rb[256 + 16], quant_g[256 + 16];
-};
-__constant__ DxtTables c_dxt;
-
 __host__ __device__ inline int mul8bit(int a, int b) {
   const int t = a * b + 128;
   return (t + (t >> 8)) >> 8;
 }
 __host__ __device__ inline int lerp13(int a, int b) { return (2 * a + b) / 3; }
+// 565 expansion by bit replication
+__host__ __device__ inline int exp5(int q) { return (q << 3) | (q >> 2); }
+__host__ __device__ inline int exp6(int q) { return (q << 2) | (q >> 4); }
 
-void build_dxt_tables(DxtTables *t) {
-  for (int i = 0; i < 32; i++) t->exp5[i] = (uint8_t)((i << 3) | (i >> 2));
-  for (int i = 0; i < 64; i++) t->exp6[i] = (uint8_t)((i << 2) | (i >> 4));
-  for (int i = 0; i < 256 + 16; i++) {
-    const int v = i < 8 ? 0 : (i - 8 > 255 ? 255 : i - 8);
-    t->quant_rb[i] = t->exp5[mul8bit(v, 31)];
-    t->quant_g[i] = t->exp6[mul8bit(v, 63)];
-  }
+// Per 8-bit value, the best endpoint pair (high, low) of the single-colour
+// encoding: the pair whose 1/3 interpolant reproduces the value, with 3 % of
+// the endpoints' distance as a penalty; packed high | low << 8. In global
+// memory (read through the read-only cache: lanes index it divergently).
+__device__ uint16_t g_dxt_match[2][256];  // [0]: 5-bit channels, [1]: 6-bit
+
+void build_match_tables(uint16_t (*tab)[256]) {
   for (int pass = 0; pass < 2; pass++) {
-    const uint8_t *expand = pass ? t->exp6 : t->exp5;
     const int size = pass ? 64 : 32;
-    uint8_t(*tab)[2] = pass ? t->match6 : t->match5;
     for (int v = 0; v < 256; v++) {
       int best = 256;
       for (int lo = 0; lo < size; lo++)
         for (int hi = 0; hi < size; hi++) {
-          int err = std::abs(lerp13(expand[hi], expand[lo]) - v);
-          err += std::abs(expand[hi] - expand[lo]) * 3 / 100;
+          const int eh = pass ? exp6(hi) : exp5(hi), el = pass ? exp6(lo) : exp5(lo);
+          const int err = std::abs(lerp13(eh, el) - v) + std::abs(eh - el) * 3 / 100;
           if (err < best) {
-            tab[v][0] = (uint8_t)hi;
-            tab[v][1] = (uint8_t)lo;
+            tab[pass][v] = (uint16_t)(hi | (lo << 8));
             best = err;
           }
         }
     }
   }
 }
+
+// The dither's 565 quantisers: the channel value (clamped to 0..255, as
+// the reference's table indexed from -8 to 263 is) to its nearest 5- or
+// 6-bit level, expanded back to 8 bits. Arithmetic rather than a table, so
+// that divergent lanes do not serialise on a lookup.
+__device__ __forceinline__ int quant5(int v) { return exp5(mul8bit(min(max(v, 0), 255), 31)); }
+__device__ __forceinline__ int quant6(int v) { return exp6(mul8bit(min(max(v, 0), 255), 63)); }
 
 __device__ __forceinline__ int ch8(uint32_t p, int c) { return (int)((p >> (8 * c)) & 0xFF); }
 
@@ -77,12 +73,12 @@ __device__ __forceinline__ uint16_t as565(int r, int g, int b) {
 
 // The palette of endpoints c0, c1 as packed RGB (4-colour interpolation).
 __device__ __forceinline__ void dxt_palette(uint16_t c0, uint16_t c1, int col[4][3]) {
-  col[0][0] = c_dxt.exp5[(c0 >> 11) & 31];
-  col[0][1] = c_dxt.exp6[(c0 >> 5) & 63];
-  col[0][2] = c_dxt.exp5[c0 & 31];
-  col[1][0] = c_dxt.exp5[(c1 >> 11) & 31];
-  col[1][1] = c_dxt.exp6[(c1 >> 5) & 63];
-  col[1][2] = c_dxt.exp5[c1 & 31];
+  col[0][0] = exp5((c0 >> 11) & 31);
+  col[0][1] = exp6((c0 >> 5) & 63);
+  col[0][2] = exp5(c0 & 31);
+  col[1][0] = exp5((c1 >> 11) & 31);
+  col[1][1] = exp6((c1 >> 5) & 63);
+  col[1][2] = exp5(c1 & 31);
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     col[2][k] = lerp13(col[0][k], col[1][k]);
@@ -96,19 +92,19 @@ __device__ __forceinline__ void dxt_dither(const uint32_t (&px)[16], uint32_t (&
   for (int i = 0; i < 16; i++) out[i] = 0;
 #pragma unroll
   for (int ch = 0; ch < 3; ch++) {
-    const uint8_t *q = (ch == 1 ? c_dxt.quant_g : c_dxt.quant_rb) + 8;
+    auto q = [ch](int v) { return ch == 1 ? quant6(v) : quant5(v); };
     int p0 = 0, p1 = 0, p2 = 0, p3 = 0;  // the row above's errors
 #pragma unroll
     for (int y = 0; y < 4; y++) {
       const int s0 = ch8(px[4 * y], ch), s1 = ch8(px[4 * y + 1], ch);
       const int s2 = ch8(px[4 * y + 2], ch), s3 = ch8(px[4 * y + 3], ch);
-      const int d0 = q[s0 + ((3 * p1 + 5 * p0) >> 4)];
+      const int d0 = q(s0 + ((3 * p1 + 5 * p0) >> 4));
       const int e0 = s0 - d0;
-      const int d1 = q[s1 + ((7 * e0 + 3 * p2 + 5 * p1 + p0) >> 4)];
+      const int d1 = q(s1 + ((7 * e0 + 3 * p2 + 5 * p1 + p0) >> 4));
       const int e1 = s1 - d1;
-      const int d2 = q[s2 + ((7 * e1 + 3 * p3 + 5 * p2 + p1) >> 4)];
+      const int d2 = q(s2 + ((7 * e1 + 3 * p3 + 5 * p2 + p1) >> 4));
       const int e2 = s2 - d2;
-      const int d3 = q[s3 + ((7 * e2 + 5 * p3 + p2) >> 4)];
+      const int d3 = q(s3 + ((7 * e2 + 5 * p3 + p2) >> 4));
       const int e3 = s3 - d3;
       out[4 * y] |= (uint32_t)d0 << (8 * ch);
       out[4 * y + 1] |= (uint32_t)d1 << (8 * ch);
@@ -242,8 +238,10 @@ __device__ __forceinline__ int clamp_trunc(float y, int hi) {
 
 __device__ __forceinline__ void single_colour_pair(int r, int g, int b, uint16_t &max16,
                                                    uint16_t &min16) {
-  max16 = (uint16_t)((c_dxt.match5[r][0] << 11) | (c_dxt.match6[g][0] << 5) | c_dxt.match5[b][0]);
-  min16 = (uint16_t)((c_dxt.match5[r][1] << 11) | (c_dxt.match6[g][1] << 5) | c_dxt.match5[b][1]);
+  const uint32_t mr = __ldg(&g_dxt_match[0][r]), mg = __ldg(&g_dxt_match[1][g]),
+                 mb = __ldg(&g_dxt_match[0][b]);
+  max16 = (uint16_t)(((mr & 0xFF) << 11) | ((mg & 0xFF) << 5) | (mb & 0xFF));
+  min16 = (uint16_t)(((mr >> 8) << 11) | ((mg >> 8) << 5) | (mb >> 8));
 }
 
 // Least-squares endpoints for the indices in `mask` (normal equations,
@@ -309,20 +307,18 @@ __device__ __forceinline__ uint2 dxt_color_block(const uint32_t (&px)[16]) {
     uint32_t d[16];
     dxt_dither(px, d);
     dxt_axis(d, mx16, mn16);
-    int col[4][3];
-    if (mx16 != mn16) {
-      dxt_palette(mx16, mn16, col);
-      mask = dxt_match(px, col);
-    } else {
+    // match, refine, and match again when the refinement moved the
+    // endpoints (one copy of the match code: the kernel is instruction-
+    // cache bound when it is inlined twice)
+#pragma unroll 1
+    for (int pass = 0;; pass++) {
       mask = 0;
-    }
-    if (dxt_refine(d, mx16, mn16, mask)) {
       if (mx16 != mn16) {
+        int col[4][3];
         dxt_palette(mx16, mn16, col);
         mask = dxt_match(px, col);
-      } else {
-        mask = 0;
       }
+      if (pass == 1 || !dxt_refine(d, mx16, mn16, mask)) break;
     }
   }
   if (mx16 < mn16) {
@@ -373,8 +369,11 @@ struct DxtLaunch {
 };
 
 // One thread per block of up to 32 jobs (their blocks in one index space).
+#ifndef FASTC_DXT_MIN_BLOCKS
+#define FASTC_DXT_MIN_BLOCKS 4  // 128 registers: four CTAs of 128 threads per SM
+#endif
 template <bool kAlpha>
-__global__ void __launch_bounds__(128) dxt_encode_kernel(const DxtLaunch L, uint64_t total) {
+__global__ void __launch_bounds__(128, FASTC_DXT_MIN_BLOCKS) dxt_encode_kernel(const DxtLaunch L, uint64_t total) {
   const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= total) return;
   int j = 0;
@@ -477,9 +476,9 @@ cudaError_t dxt_setup(int dev) {
   std::lock_guard<std::mutex> lk(g_dxt_mu);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (g_dxt_ready[dev]) return cudaSuccess;
-  static DxtTables t;
-  build_dxt_tables(&t);
-  const cudaError_t e = cudaMemcpyToSymbol(c_dxt, &t, sizeof(t));
+  static uint16_t t[2][256];
+  build_match_tables(t);
+  const cudaError_t e = cudaMemcpyToSymbol(g_dxt_match, t, sizeof(t));
   if (e == cudaSuccess) g_dxt_ready[dev] = true;
   return e;
 }
@@ -513,10 +512,14 @@ bool dxt_jobs(const fastc_bc7_job *jobs, uint32_t n, std::vector<JobDev> *out) {
   return true;
 }
 
-struct DxtHostBuffers {
+// Host-memory calls: staging buffers, and three streams so that a group's
+// texel upload, the previous group's encode and the group before's block
+// download overlap (the copies, not the encode, bound these calls).
+struct DxtHostContext {
   void *in = nullptr, *out = nullptr;
   size_t in_cap = 0, out_cap = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t h2d = nullptr, comp = nullptr, d2h = nullptr;
+  std::vector<cudaEvent_t> ev;
   int device = -1;
 } g_dxt_host;
 
@@ -528,6 +531,36 @@ cudaError_t ensure(void **p, size_t *cap, size_t n) {
   const cudaError_t e = cudaMalloc(p, n);
   if (e == cudaSuccess) *cap = n;
   return e;
+}
+
+// The context of device `dev` (the current one); a previous device's
+// objects are released on that device.
+cudaError_t host_context(int dev, size_t events) {
+  DxtHostContext &h = g_dxt_host;
+  if (h.device != dev) {
+    if (h.device >= 0 && cudaSetDevice(h.device) == cudaSuccess) {
+      cudaFree(h.in);
+      cudaFree(h.out);
+      for (cudaEvent_t e : h.ev) cudaEventDestroy(e);
+      cudaStreamDestroy(h.h2d);
+      cudaStreamDestroy(h.comp);
+      cudaStreamDestroy(h.d2h);
+    }
+    h = DxtHostContext();
+    cudaError_t e = cudaSetDevice(dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h.h2d, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h.comp, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h.d2h, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    h.device = dev;
+  }
+  while (h.ev.size() < events) {
+    cudaEvent_t e;
+    const cudaError_t st = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (st != cudaSuccess) return st;
+    h.ev.push_back(e);
+  }
+  return cudaSuccess;
 }
 
 }  // namespace
@@ -564,44 +597,73 @@ fastc_bc7_status fastc_dxt_compress_device(const fastc_bc7_job *jobs, uint32_t n
   return FASTC_BC7_OK;
 }
 
-fastc_bc7_status fastc_dxt_compress(const fastc_bc7_job *job, int format) {
-  if (!job || (format != FASTC_DXT1 && format != FASTC_DXT5)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+fastc_bc7_status fastc_dxt_compress_batch(const fastc_bc7_job *jobs, uint32_t n, int format) {
+  if ((!jobs && n) || (format != FASTC_DXT1 && format != FASTC_DXT5)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
   std::vector<JobDev> dj;
-  if (!fastc::dxt_jobs(job, 1, &dj)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
-  JobDev &d = dj[0];
-  if (d.nblocks == 0) return FASTC_BC7_OK;
+  if (!fastc::dxt_jobs(jobs, n, &dj)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  const bool alpha = format == FASTC_DXT5;
+  const size_t bsz = alpha ? 16 : 8;
+  // per job: the texel rows its blocks cover, staged at 256-byte offsets
+  std::vector<size_t> in_off(n), in_bytes(n), out_off(n);
+  size_t in_total = 0, out_total = 0;
+  uint64_t total = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    JobDev &d = dj[i];
+    const uint32_t bw = jobs[i].width / 4;
+    const uint32_t r0 = d.nblocks ? d.first / bw : 0, r1 = d.nblocks ? (d.first + d.nblocks - 1) / bw : 0;
+    in_bytes[i] = d.nblocks ? (size_t)(r1 - r0 + 1) * 4 * jobs[i].width * 4 : 0;
+    d.row0 = r0 * 4;
+    d.out_first = d.first;
+    in_off[i] = in_total;
+    out_off[i] = out_total;
+    in_total += (in_bytes[i] + 255) & ~(size_t)255;
+    out_total += ((size_t)d.nblocks * bsz + 255) & ~(size_t)255;
+    total += d.nblocks;
+  }
+  if (total == 0) return FASTC_BC7_OK;
   const int dev = current_device();
   if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
   CK(fastc::dxt_setup(dev));
-  const bool alpha = format == FASTC_DXT5;
-  const size_t bsz = alpha ? 16 : 8;
+  const uint32_t groups = (n + fastc::kDxtJobsPerLaunch - 1) / fastc::kDxtJobsPerLaunch;
   std::lock_guard<std::mutex> lk(fastc::g_dxt_mu);
-  fastc::DxtHostBuffers &h = fastc::g_dxt_host;
-  if (h.device != dev) {
-    if (h.stream) cudaStreamDestroy(h.stream);
-    h = fastc::DxtHostBuffers();
-    CK(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
-    h.device = dev;
+  CK(fastc::host_context(dev, 2 * (size_t)groups));
+  fastc::DxtHostContext &h = fastc::g_dxt_host;
+  CK(fastc::ensure(&h.in, &h.in_cap, in_total));
+  CK(fastc::ensure(&h.out, &h.out_cap, out_total));
+  uint8_t *in = static_cast<uint8_t *>(h.in), *out = static_cast<uint8_t *>(h.out);
+  for (uint32_t g = 0; g < groups; g++) {
+    const uint32_t k0 = g * fastc::kDxtJobsPerLaunch;
+    const uint32_t m = std::min<uint32_t>(fastc::kDxtJobsPerLaunch, n - k0);
+    uint64_t begin = 0;
+    for (uint32_t k = k0; k < k0 + m; k++) {
+      JobDev &d = dj[k];
+      if (d.nblocks)
+        CK(cudaMemcpyAsync(in + in_off[k], jobs[k].in + (size_t)d.row0 * jobs[k].width * 4, in_bytes[k],
+                           cudaMemcpyHostToDevice, h.h2d));
+      d.in = in + in_off[k];
+      d.out = out + out_off[k];
+      d.flags = fastc::kJobIn16 | (alpha ? fastc::kJobOut16 : 0u);
+      d.begin = begin;
+      begin += d.nblocks;
+    }
+    CK(cudaEventRecord(h.ev[2 * g], h.h2d));
+    CK(cudaStreamWaitEvent(h.comp, h.ev[2 * g], 0));
+    CK(fastc::dxt_launch(dj.data() + k0, m, begin, alpha, h.comp));
+    CK(cudaEventRecord(h.ev[2 * g + 1], h.comp));
+    CK(cudaStreamWaitEvent(h.d2h, h.ev[2 * g + 1], 0));
+    for (uint32_t k = k0; k < k0 + m; k++)
+      if (dj[k].nblocks)
+        CK(cudaMemcpyAsync(jobs[k].out + (size_t)dj[k].first * bsz, out + out_off[k],
+                           (size_t)dj[k].nblocks * bsz, cudaMemcpyDeviceToHost, h.d2h));
   }
-  // the job's texel rows up, its blocks back
-  const uint32_t bw = job->width / 4;
-  const uint32_t r0 = d.first / bw, r1 = (d.first + d.nblocks - 1) / bw;
-  const size_t in_bytes = (size_t)(r1 - r0 + 1) * 4 * job->width * 4;
-  CK(fastc::ensure(&h.in, &h.in_cap, in_bytes));
-  CK(fastc::ensure(&h.out, &h.out_cap, (size_t)d.nblocks * bsz));
-  CK(cudaMemcpyAsync(h.in, job->in + (size_t)r0 * 4 * job->width * 4, in_bytes,
-                     cudaMemcpyHostToDevice, h.stream));
-  d.in = static_cast<const uint8_t *>(h.in);
-  d.out = static_cast<uint8_t *>(h.out);
-  d.row0 = r0 * 4;
-  d.out_first = d.first;
-  d.flags = fastc::kJobIn16 | (alpha ? fastc::kJobOut16 : 0u);
-  d.begin = 0;
-  CK(fastc::dxt_launch(&d, 1, d.nblocks, alpha, h.stream));
-  CK(cudaMemcpyAsync(job->out + (size_t)d.first * bsz, h.out, (size_t)d.nblocks * bsz,
-                     cudaMemcpyDeviceToHost, h.stream));
-  CK(cudaStreamSynchronize(h.stream));
+  // the last download waited on the last encode, which waited on the last upload
+  CK(cudaStreamSynchronize(h.d2h));
   return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_dxt_compress(const fastc_bc7_job *job, int format) {
+  if (!job) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  return fastc_dxt_compress_batch(job, 1, format);
 }
 
 fastc_bc7_status fastc_dxt_decompress_device(const uint8_t *blocks, uint8_t *rgba, uint32_t width,
@@ -631,26 +693,21 @@ fastc_bc7_status fastc_dxt_decompress(const uint8_t *blocks, uint8_t *rgba, uint
   const size_t nb = (size_t)((width + 3) / 4) * ((height + 3) / 4);
   const size_t bsz = format == FASTC_DXT5 ? 16 : 8, img = (size_t)width * height * 4;
   std::lock_guard<std::mutex> lk(fastc::g_dxt_mu);
-  fastc::DxtHostBuffers &h = fastc::g_dxt_host;
-  if (h.device != dev) {
-    if (h.stream) cudaStreamDestroy(h.stream);
-    h = fastc::DxtHostBuffers();
-    CK(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
-    h.device = dev;
-  }
+  CK(fastc::host_context(dev, 0));
+  fastc::DxtHostContext &h = fastc::g_dxt_host;
   CK(fastc::ensure(&h.in, &h.in_cap, nb * bsz));
   CK(fastc::ensure(&h.out, &h.out_cap, img));
-  CK(cudaMemcpyAsync(h.in, blocks, nb * bsz, cudaMemcpyHostToDevice, h.stream));
+  CK(cudaMemcpyAsync(h.in, blocks, nb * bsz, cudaMemcpyHostToDevice, h.comp));
   const unsigned grid = (unsigned)((nb + 127) / 128);
   if (format == FASTC_DXT5)
-    fastc::dxt_decode_kernel<true><<<grid, 128, 0, h.stream>>>(static_cast<const uint8_t *>(h.in),
+    fastc::dxt_decode_kernel<true><<<grid, 128, 0, h.comp>>>(static_cast<const uint8_t *>(h.in),
                                                                static_cast<uint8_t *>(h.out), width, height);
   else
-    fastc::dxt_decode_kernel<false><<<grid, 128, 0, h.stream>>>(static_cast<const uint8_t *>(h.in),
+    fastc::dxt_decode_kernel<false><<<grid, 128, 0, h.comp>>>(static_cast<const uint8_t *>(h.in),
                                                                 static_cast<uint8_t *>(h.out), width, height);
   CK(cudaPeekAtLastError());
-  CK(cudaMemcpyAsync(rgba, h.out, img, cudaMemcpyDeviceToHost, h.stream));
-  CK(cudaStreamSynchronize(h.stream));
+  CK(cudaMemcpyAsync(rgba, h.out, img, cudaMemcpyDeviceToHost, h.comp));
+  CK(cudaStreamSynchronize(h.comp));
   return FASTC_BC7_OK;
 }
 

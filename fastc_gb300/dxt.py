@@ -21,8 +21,9 @@ from .bptc import CompressionFormat, CompressionJob, _is_cuda, _stream_handle
 
 
 def compress_dxt_jobs(jobs: Sequence[CompressionJob], stream=None) -> None:
-    """Every job of one DXT format; device jobs go to the GPU in launches of
-    up to 32 jobs, host jobs one by one."""
+    """Every job of one DXT format in one call: device jobs are encoded in
+    place in launches of up to 32 jobs; host jobs go through the batched
+    host entry point (copies overlapped with the encode)."""
     if not jobs:
         return
     fmts = {j.format for j in jobs}
@@ -33,14 +34,12 @@ def compress_dxt_jobs(jobs: Sequence[CompressionJob], stream=None) -> None:
     if len(on_dev) != 1:
         raise BC7Error(_lib.ERR_INVALID_ARGUMENT, "compress_dxt_jobs", "mixed host and device jobs")
     lib = load()
+    jarr = (Job * len(jobs))(*[j.to_c() for j in jobs])
     if on_dev.pop():
-        jarr = (Job * len(jobs))(*[j.to_c() for j in jobs])
         check(lib.fastc_dxt_compress_device(jarr, len(jobs), fmt, C.c_void_p(_stream_handle(stream))),
               "fastc_dxt_compress_device")
-        return
-    for j in jobs:
-        cj = j.to_c()
-        check(lib.fastc_dxt_compress(C.byref(cj), fmt), "fastc_dxt_compress")
+    else:
+        check(lib.fastc_dxt_compress_batch(jarr, len(jobs), fmt), "fastc_dxt_compress_batch")
 
 
 def _with_format(job: CompressionJob, fmt: CompressionFormat) -> CompressionJob:

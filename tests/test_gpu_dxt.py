@@ -147,6 +147,30 @@ def test_many_device_jobs_in_one_call(gpu, port, code):
         assert np.array_equal(o.cpu().numpy(), port.dxt_compress(t, code == 5))
 
 
+@pytest.mark.parametrize("code", [1, 5])
+def test_many_host_jobs_in_one_call(gpu, port, code):
+    """70 host textures through the batched host entry point (three groups
+    of up to 32 jobs, copies overlapped), one of them a sub-job."""
+    from fastc_gb300 import CompressionJob, dxt, synth
+
+    texs = synth.texture_set(seed=10, count=70, lo_log2=2, hi_log2=7)
+    outs = [np.zeros(t.shape[0] * t.shape[1] * bsz(code) // 16, np.uint8) for t in texs]
+    jobs = [CompressionJob(t, o, t.shape[1], t.shape[0], format=fmt_of(code)) for t, o in zip(texs, outs)]
+    big = max(range(len(texs)), key=lambda i: texs[i].shape[0] * texs[i].shape[1])
+    t = texs[big]
+    jobs[big] = CompressionJob(t, outs[big], t.shape[1], t.shape[0], 4, 4, t.shape[1], 8, format=fmt_of(code))
+    dxt.compress_dxt_jobs(jobs)
+    for i, (t, o) in enumerate(zip(texs, outs)):
+        want = port.dxt_compress(t, code == 5)
+        if i == big:
+            bw, b = t.shape[1] // 4, bsz(code)
+            first, last = bw + 1, 3 * bw  # rest of block row 1, then row 2 up to x = width
+            assert np.array_equal(o[b * first:b * last], want[b * first:b * last])
+            assert not o[:b * first].any() and not o[b * last:].any()
+        else:
+            assert np.array_equal(o, want)
+
+
 def test_compress_image_data_dispatches_on_format(gpu, port):
     from fastc_gb300 import CompressionFormat, compress_image_data
 
