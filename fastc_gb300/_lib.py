@@ -144,6 +144,10 @@ SIGNATURES = {
     "fastc_dxt_decompress": (C.c_int, [u8p, u8p, C.c_uint32, C.c_uint32, C.c_int]),
     "fastc_dxt_decompress_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int,
                                               C.c_void_p]),
+    "fastc_dxt_psnr": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int,
+                                 C.POINTER(C.c_double), C.c_void_p]),
+    "fastc_dxt_block_error_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int,
+                                               C.c_void_p, C.c_void_p, C.c_void_p]),
     "fastc_bc7_set_engine": (C.c_int, [C.c_int]),
     "fastc_bc7_get_engine": (C.c_int, []),
     "fastc_bc7_set_launch_shape": (C.c_int, [C.c_int, C.c_int]),

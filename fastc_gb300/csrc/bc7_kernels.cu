@@ -791,6 +791,11 @@ int launch_range_error(const uint8_t *blocks, const uint8_t *rows, uint32_t widt
   return (int)cudaPeekAtLastError();
 }
 
+int launch_sum(const double *v, uint64_t n, double *out, void *stream) {
+  sum_kernel<<<1, 1024, 0, static_cast<cudaStream_t>(stream)>>>(v, n, out);
+  return (int)cudaPeekAtLastError();
+}
+
 int launch_block_error(const uint8_t *blocks, const uint8_t *rgba, uint32_t width,
                        uint32_t height, double *block_sse, double *total, void *stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -57,6 +57,8 @@ int device_sm_count(int device);
 // total is not null.
 int launch_block_error(const uint8_t *blocks, const uint8_t *rgba, uint32_t width,
                        uint32_t height, double *block_sse, double *total, void *stream);
+// Sum of n doubles in a fixed order (one CTA), into *out.
+int launch_sum(const double *v, uint64_t n, double *out, void *stream);
 // The same for the blocks [first, first + count) of a texture `width`
 // texels wide, `blocks` holding them from `first` on and `rows` its texels
 // from row `row0` on.

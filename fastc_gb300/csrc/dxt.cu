@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -419,16 +420,14 @@ __global__ void __launch_bounds__(128, FASTC_DXT_MIN_BLOCKS) dxt_encode_kernel(c
   }
 }
 
-// FasTC's decoder (DXTEncoder/src/Decompressor.cpp:26-155): one thread per
-// block, texels outside the image skipped.
+// FasTC's decoder (DXTEncoder/src/Decompressor.cpp:26-95) for one block:
+// 565 expanded by bit replication; 4 colours when the first endpoint word
+// is larger (always for DXT5's colour half), else 3 colours and black; DXT1
+// alpha 255; DXT5's 8-entry alpha palette (6 interpolants, or 4 with 0 and
+// 255 when the first alpha is not larger). out[i] = texel i, RGBA in bytes
+// 0..3.
 template <bool kAlpha>
-__global__ void dxt_decode_kernel(const uint8_t *__restrict__ blocks, uint8_t *__restrict__ rgba,
-                                  uint32_t width, uint32_t height) {
-  const uint32_t bw = (width + 3) / 4, bh = (height + 3) / 4;
-  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= (uint64_t)bw * bh) return;
-  const uint32_t bx = (uint32_t)(b % bw), by = (uint32_t)(b / bw);
-  const uint8_t *src = blocks + b * (kAlpha ? 16 : 8);
+__device__ __forceinline__ void dxt_decode_block(const uint8_t *__restrict__ src, uint32_t (&out)[16]) {
   uint32_t alpha[16];
   if (kAlpha) {
     const int a0 = src[0], a1 = src[1];
@@ -457,16 +456,74 @@ __global__ void dxt_decode_kernel(const uint8_t *__restrict__ blocks, uint8_t *_
   }
   const uint32_t m = (uint32_t)src[4] | ((uint32_t)src[5] << 8) | ((uint32_t)src[6] << 16) |
                      ((uint32_t)src[7] << 24);
+  for (int i = 0; i < 16; i++) {
+    const int *c = col[(m >> (2 * i)) & 3];
+    out[i] = alpha[i] | (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16);
+  }
+}
+
+// FasTC's DecompressDXT1 / DXT5 (Decompressor.cpp:98-155): one thread per
+// block, texels outside the image skipped.
+template <bool kAlpha>
+__global__ void dxt_decode_kernel(const uint8_t *__restrict__ blocks, uint8_t *__restrict__ rgba,
+                                  uint32_t width, uint32_t height) {
+  const uint32_t bw = (width + 3) / 4, bh = (height + 3) / 4;
+  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= (uint64_t)bw * bh) return;
+  const uint32_t bx = (uint32_t)(b % bw), by = (uint32_t)(b / bw);
+  uint32_t px[16];
+  dxt_decode_block<kAlpha>(blocks + b * (kAlpha ? 16 : 8), px);
   for (int y = 0; y < 4; y++) {
     if (by * 4 + y >= height) break;
     for (int x = 0; x < 4; x++) {
       if (bx * 4 + x >= width) break;
-      const int i = 4 * y + x;
-      const int *c = col[(m >> (2 * i)) & 3];
-      const uint32_t p = alpha[i] | (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16);
-      *reinterpret_cast<uint32_t *>(rgba + ((size_t)(by * 4 + y) * width + bx * 4 + x) * 4) = p;
+      *reinterpret_cast<uint32_t *>(rgba + ((size_t)(by * 4 + y) * width + bx * 4 + x) * 4) = px[4 * y + x];
     }
   }
+}
+
+// FasTC's Image::ComputePSNR metric (Base/src/Image.cpp:206-255) per 4x4
+// block of decoded DXT blocks against the original texels: per texel, RGB
+// premultiplied by alpha / 255 in double, the three squared differences
+// summed in channel order; per block, the texels in row order (texels
+// outside the image skipped).
+template <bool kAlpha>
+__global__ void dxt_error_kernel(const uint8_t *__restrict__ blocks, const uint8_t *__restrict__ rgba,
+                                 uint32_t width, uint32_t height, double *__restrict__ sse) {
+  const uint32_t bw = (width + 3) / 4, bh = (height + 3) / 4;
+  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= (uint64_t)bw * bh) return;
+  const uint32_t bx = (uint32_t)(b % bw), by = (uint32_t)(b / bw);
+  uint32_t dec[16];
+  dxt_decode_block<kAlpha>(blocks + b * (kAlpha ? 16 : 8), dec);
+  double s = 0.0;
+  for (int y = 0; y < 4; y++) {
+    if (by * 4 + y >= height) break;
+    for (int x = 0; x < 4; x++) {
+      if (bx * 4 + x >= width) break;
+      const uint8_t *p = rgba + ((size_t)(by * 4 + y) * width + bx * 4 + x) * 4;
+      const uint32_t d = dec[4 * y + x];
+      const double ra = (double)p[3] / 255.0, ua = (double)(d >> 24) / 255.0;
+      for (int c = 0; c < 3; c++) {
+        const double e = ra * (double)p[c] - ua * (double)((d >> (8 * c)) & 0xFF);
+        s += e * e;
+      }
+    }
+  }
+  sse[b] = s;
+}
+
+cudaError_t launch_dxt_error(const uint8_t *blocks, const uint8_t *rgba, uint32_t width, uint32_t height,
+                             bool alpha, double *block_sse, double *total, cudaStream_t st) {
+  const uint64_t nb = (uint64_t)((width + 3) / 4) * ((height + 3) / 4);
+  const unsigned grid = (unsigned)((nb + 127) / 128);
+  if (alpha) dxt_error_kernel<true><<<grid, 128, 0, st>>>(blocks, rgba, width, height, block_sse);
+  else dxt_error_kernel<false><<<grid, 128, 0, st>>>(blocks, rgba, width, height, block_sse);
+  if (total) {
+    const int e = launch_sum(block_sse, nb, total, st);
+    if (e) return (cudaError_t)e;
+  }
+  return cudaPeekAtLastError();
 }
 
 std::mutex g_dxt_mu;
@@ -664,6 +721,48 @@ fastc_bc7_status fastc_dxt_compress_batch(const fastc_bc7_job *jobs, uint32_t n,
 fastc_bc7_status fastc_dxt_compress(const fastc_bc7_job *job, int format) {
   if (!job) return FASTC_BC7_ERR_INVALID_ARGUMENT;
   return fastc_dxt_compress_batch(job, 1, format);
+}
+
+fastc_bc7_status fastc_dxt_block_error_device(const uint8_t *blocks, const uint8_t *rgba, uint32_t width,
+                                              uint32_t height, int format, double *block_sse, double *total,
+                                              void *stream) {
+  if (!blocks || !rgba || !block_sse || width == 0 || height == 0 ||
+      (format != FASTC_DXT1 && format != FASTC_DXT5))
+    return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  const int dev = current_device();
+  if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
+  CK(fastc::launch_dxt_error(blocks, rgba, width, height, format == FASTC_DXT5, block_sse, total,
+                             static_cast<cudaStream_t>(stream)));
+  return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_dxt_psnr(const uint8_t *blocks, const uint8_t *rgba, uint32_t width, uint32_t height,
+                                int format, double *psnr, double *block_sse) {
+  if (!blocks || !rgba || width == 0 || height == 0 || (format != FASTC_DXT1 && format != FASTC_DXT5))
+    return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  const int dev = current_device();
+  if (dev < 0) return FASTC_BC7_ERR_NO_DEVICE;
+  const size_t nb = (size_t)((width + 3) / 4) * ((height + 3) / 4);
+  const size_t bsz = format == FASTC_DXT5 ? 16 : 8, img = (size_t)width * height * 4;
+  std::lock_guard<std::mutex> lk(fastc::g_dxt_mu);
+  CK(fastc::host_context(dev, 0));
+  fastc::DxtHostContext &h = fastc::g_dxt_host;
+  // texels, then the blocks (byte loads), in the input buffer; the per-block
+  // errors after the total in the output buffer
+  CK(fastc::ensure(&h.in, &h.in_cap, img + nb * bsz));
+  CK(fastc::ensure(&h.out, &h.out_cap, (nb + 1) * sizeof(double)));
+  uint8_t *dimg = static_cast<uint8_t *>(h.in), *dblk = dimg + img;
+  double *dsse = static_cast<double *>(h.out);
+  CK(cudaMemcpyAsync(dimg, rgba, img, cudaMemcpyHostToDevice, h.comp));
+  CK(cudaMemcpyAsync(dblk, blocks, nb * bsz, cudaMemcpyHostToDevice, h.comp));
+  CK(fastc::launch_dxt_error(dblk, dimg, width, height, format == FASTC_DXT5, dsse + 1, dsse, h.comp));
+  double total = 0.0;
+  CK(cudaMemcpyAsync(&total, dsse, sizeof(double), cudaMemcpyDeviceToHost, h.comp));
+  if (block_sse)
+    CK(cudaMemcpyAsync(block_sse, dsse + 1, nb * sizeof(double), cudaMemcpyDeviceToHost, h.comp));
+  CK(cudaStreamSynchronize(h.comp));
+  if (psnr) *psnr = 10.0 * std::log10((3.0 * 255.0 * 255.0) / (total / ((double)width * height)));
+  return FASTC_BC7_OK;
 }
 
 fastc_bc7_status fastc_dxt_decompress_device(const uint8_t *blocks, uint8_t *rgba, uint32_t width,

@@ -96,3 +96,40 @@ def decompress_dxt1(blocks, width: int, height: int, out=None, stream=None):
 def decompress_dxt5(blocks, width: int, height: int, out=None, stream=None):
     """DXTC::DecompressDXT5 (DXTCompressor.h:28)."""
     return decompress(blocks, width, height, CompressionFormat.DXT5, out, stream)
+
+
+def psnr(blocks, rgba, width: int, height: int, format: CompressionFormat, block_sse: bool = False,
+         stream=None):
+    """Image::ComputePSNR (Base/src/Image.cpp:206-255) of DXT1 / DXT5
+    `blocks` against the original `rgba`, decoded and compared on the GPU:
+    the PSNR in dB, or (psnr, per-block SSE) with ``block_sse``. CUDA
+    tensors are read on `stream` (the result is copied back, which
+    synchronises it)."""
+    import math
+
+    format = CompressionFormat(format)
+    if format == CompressionFormat.BPTC:
+        raise BC7Error(_lib.ERR_INVALID_ARGUMENT, "dxt.psnr", "a DXT format")
+    lib = load()
+    nb = ((width + 3) // 4) * ((height + 3) // 4)
+    if _is_cuda(blocks):
+        import torch
+
+        sse = torch.empty(nb + 1, dtype=torch.float64, device=blocks.device)
+        check(lib.fastc_dxt_block_error_device(
+            C.c_void_p(blocks.data_ptr()), C.c_void_p(rgba.data_ptr()), width, height, int(format),
+            C.c_void_p(sse.data_ptr() + 8), C.c_void_p(sse.data_ptr()),
+            C.c_void_p(_stream_handle(stream))), "fastc_dxt_block_error_device")
+        host = sse.cpu().numpy()
+        total, per = float(host[0]), host[1:]
+        db = 10.0 * math.log10(3.0 * 255.0 * 255.0 / (total / (width * height))) if total > 0 else math.inf
+        return (db, per) if block_sse else db
+    blocks = np.ascontiguousarray(np.asarray(blocks, dtype=np.uint8))
+    rgba = np.ascontiguousarray(np.asarray(rgba, dtype=np.uint8))
+    if blocks.size < nb * (8 if format == CompressionFormat.DXT1 else 16) or rgba.size < width * height * 4:
+        raise BC7Error(_lib.ERR_INVALID_ARGUMENT, "dxt.psnr", "buffers smaller than the image")
+    out = C.c_double()
+    per = np.zeros(nb, dtype=np.float64) if block_sse else None
+    check(lib.fastc_dxt_psnr(blocks.ctypes.data, rgba.ctypes.data, width, height, int(format), C.byref(out),
+                             per.ctypes.data if per is not None else None), "fastc_dxt_psnr")
+    return (out.value, per) if block_sse else out.value

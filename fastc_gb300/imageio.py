@@ -1,6 +1,6 @@
 """Image files for the command-line tool: PNG (8-bit RGB/RGBA/grey, no
 interlace) read and written with zlib, raw RGBA8, numpy arrays, and the KTX
-container FasTC writes for compressed images.
+container FasTC writes for compressed images (BPTC, DXT1, DXT5).
 
 The KTX layout follows FasTC's ImageWriterKTX (IO/src/ImageWriterKTX.cpp:
 the 12-byte identifier, thirteen little-endian words, one key/value pair
@@ -15,39 +15,52 @@ import zlib
 import numpy as np
 
 KTX_IDENTIFIER = bytes([0xAB, 0x4B, 0x54, 0x58, 0x20, 0x31, 0x31, 0xBB, 0x0D, 0x0A, 0x1A, 0x0A])
+GL_RGB = 0x1907
 GL_RGBA = 0x1908
 GL_COMPRESSED_RGBA_BPTC_UNORM = 0x8E8C
+GL_COMPRESSED_RGB_S3TC_DXT1_EXT = 0x83F0
+GL_COMPRESSED_RGBA_S3TC_DXT5_EXT = 0x83F3
+# format -> (glInternalFormat, glBaseFormat, bytes per texel x 2), as
+# ImageWriterKTX writes them (IO/src/ImageWriterKTX.cpp:93-113, 140-151)
+_KTX_FORMATS = {
+    "BPTC": (GL_COMPRESSED_RGBA_BPTC_UNORM, GL_RGBA, 2),
+    "DXT1": (GL_COMPRESSED_RGB_S3TC_DXT1_EXT, GL_RGB, 1),
+    "DXT5": (GL_COMPRESSED_RGBA_S3TC_DXT5_EXT, GL_RGBA, 2),
+}
 _ORIENT_KEY = b"KTXorientation"
 _ORIENT_VALUE = b"S=r,T=d"
 
 
-def ktx_bytes(blocks: np.ndarray, width: int, height: int) -> bytes:
-    """A KTX file holding BC7 blocks (width*height bytes), as FasTC writes it."""
+def ktx_bytes(blocks: np.ndarray, width: int, height: int, format: str = "BPTC") -> bytes:
+    """A KTX file holding compressed blocks as FasTC writes it: BPTC and
+    DXT5 width*height bytes, DXT1 half that."""
+    internal, base, twice = _KTX_FORMATS[format]
     data = np.ascontiguousarray(blocks, dtype=np.uint8).tobytes()
-    if len(data) != width * height:
-        raise ValueError("BC7 data must be width*height bytes")
+    if len(data) != width * height * twice // 2:
+        raise ValueError(f"{format} data must be {width * height * twice // 2} bytes")
     kv = len(_ORIENT_KEY) + 1 + len(_ORIENT_VALUE) + 1
     total_kv = (kv + 4 + 3) & ~3
     head = KTX_IDENTIFIER + struct.pack(
-        "<13I", 0x04030201, 0, 1, 0, GL_COMPRESSED_RGBA_BPTC_UNORM, GL_RGBA, width, height, 0, 0, 1,
-        1, total_kv)
+        "<13I", 0x04030201, 0, 1, 0, internal, base, width, height, 0, 0, 1, 1, total_kv)
     pad = (_ORIENT_KEY * 2)[: total_kv - kv - 4]
     body = struct.pack("<I", kv) + _ORIENT_KEY + b"\0" + _ORIENT_VALUE + b"\0" + pad
     return head + body + struct.pack("<I", len(data)) + data
 
 
-def read_ktx(raw: bytes):
-    """(blocks, width, height) of a BC7 KTX file."""
+def read_ktx(raw: bytes, with_format: bool = False):
+    """(blocks, width, height) of a BPTC, DXT1 or DXT5 KTX file; with
+    ``with_format`` also the format name."""
     if raw[:12] != KTX_IDENTIFIER:
         raise ValueError("not a KTX file")
     words = struct.unpack("<13I", raw[12:64])
-    if words[0] != 0x04030201 or words[4] != GL_COMPRESSED_RGBA_BPTC_UNORM:
-        raise ValueError("not a little-endian BC7 KTX file")
+    fmt = [k for k, v in _KTX_FORMATS.items() if v[0] == words[4]]
+    if words[0] != 0x04030201 or not fmt:
+        raise ValueError("not a little-endian BPTC / DXT1 / DXT5 KTX file")
     width, height, kv = words[6], words[7], words[12]
     off = 64 + kv
     (size,) = struct.unpack("<I", raw[off:off + 4])
     blocks = np.frombuffer(raw[off + 4:off + 4 + size], dtype=np.uint8).copy()
-    return blocks, width, height
+    return (blocks, width, height, fmt[0]) if with_format else (blocks, width, height)
 
 
 def _paeth(a, b, c):

@@ -1,17 +1,20 @@
-"""tc-compatible command line: compress an image to BC7 on the GPU.
+"""tc-compatible command line: compress an image to BC7 (or DXT1 / DXT5) on
+the GPU.
 
-    python -m fastc_gb300.tc [-q N] [-n N] [-d OUT] [-nd] [-s WxH] IMAGE
+    python -m fastc_gb300.tc [-f BPTC|DXT1|DXT5] [-q N] [-n N] [-d OUT] [-nd] [-s WxH] IMAGE
 
 Mirrors FasTC's CLTool (CLTool/src/tc.cpp): BPTC at quality -q (annealing
-steps, default 50), the image zero-padded to whole blocks, "PSNR: %.3f"
+steps, default 50) or, with -f, DXT1 / DXT5 (quality has no effect, as in
+FasTC), the image zero-padded to whole blocks, "PSNR: %.3f"
 computed as FasTC's Image::ComputePSNR (alpha-premultiplied RGB, peak
 3*255^2) on the decoded blocks, and the output written to -d (or
-<basename>-bptc.png): a .ktx name stores the compressed blocks in FasTC's KTX
-layout, a .png name the decoded image. -nd writes nothing; -n N repeats the
+<basename>-bptc.png, -dxt1.png, -dxt5.png): a .ktx name stores the
+compressed blocks in FasTC's KTX layout, a .png name the decoded image. -nd writes nothing; -n N repeats the
 compression and reports the time. Options that choose host threading (-t,
 -j, -a, -simd) are accepted and have no effect: the work is distributed on
 the GPU. -l runs CompressWithStats with a log stream and writes FasTC's
-per-block log to <basename>.log; formats other than BPTC are refused.
+per-block log to <basename>.log (for DXT the log stays empty, as FasTC's
+does: it has no logging DXT encoder); ETC1 and PVRTC are refused.
 Inputs: PNG (8-bit), .npy RGBA8 arrays, raw RGBA (.rgba/.raw with -s WxH).
 """
 from __future__ import annotations
@@ -38,7 +41,7 @@ def main(argv=None) -> int:
     if not argv:
         usage()
         return 1
-    quality, repeats, out_name, write_out, save_log = 50, 1, "", True, False
+    quality, repeats, out_name, write_out, save_log, fmt = 50, 1, "", True, False, "BPTC"
     width = height = 0
     i = 0
     while i < len(argv) and argv[i].startswith("-"):
@@ -59,9 +62,12 @@ def main(argv=None) -> int:
                 width, height = (int(x) for x in val.lower().split("x"))
             elif opt == "-d":
                 out_name = val
-            elif opt == "-f" and val not in ("BPTC", "BPTCLib"):
-                print(f"format {val} is not supported: this build encodes BC7 (BPTC) only", file=sys.stderr)
-                return 1
+            elif opt == "-f":
+                if val not in ("BPTC", "BPTCLib", "DXT1", "DXT5"):
+                    print(f"format {val} is not supported: this build encodes BPTC, DXT1 and DXT5",
+                          file=sys.stderr)
+                    return 1
+                fmt = "BPTC" if val == "BPTCLib" else val
             i += 2
             continue
         if opt == "-nd":
@@ -77,36 +83,46 @@ def main(argv=None) -> int:
         return 1
     path = argv[i]
 
-    from . import imageio
-    from .bptc import CompressionJob, CompressionSettings, compress, compress_with_stats, decompress, psnr
+    from . import dxt, imageio
+    from .bptc import (CompressionFormat, CompressionJob, CompressionSettings, compress, compress_with_stats,
+                       decompress, psnr)
 
     img = imageio.pad_to_blocks(imageio.load_image(path, width, height))
     h, w = img.shape[:2]
-    blocks = np.zeros(w * h, dtype=np.uint8)
+    cf = CompressionFormat[fmt]
+    blocks = np.zeros(w * h // (2 if cf == CompressionFormat.DXT1 else 1), dtype=np.uint8)
     settings = CompressionSettings(num_simulated_annealing_steps=quality)
     logs = []
     t0 = time.perf_counter()
     for _ in range(repeats):
-        if save_log:  # the log stream sees every compression, as FasTC's does
-            logs.append(compress_with_stats(CompressionJob(img, blocks, w, h), settings))
+        job = CompressionJob(img, blocks, w, h, format=cf)
+        if cf != CompressionFormat.BPTC:
+            dxt.compress_dxt_jobs([job])
+        elif save_log:  # the log stream sees every compression, as FasTC's does
+            logs.append(compress_with_stats(job, settings))
         else:
-            compress(CompressionJob(img, blocks, w, h), settings)
+            compress(job, settings)
     dt = (time.perf_counter() - t0) / repeats
     if repeats > 1:
         print(f"Compression time: {dt * 1e3:.3f} ms")
     if save_log:
         with open(basename(path) + ".log", "w") as f:
             f.write("".join(logs))
-    print(f"PSNR: {psnr(blocks, img, w, h):.3f}")
+    if cf == CompressionFormat.BPTC:
+        db = psnr(blocks, img, w, h)
+    else:
+        db = dxt.psnr(blocks, img, w, h, cf)
+    print(f"PSNR: {db:.3f}")
     if write_out:
-        dec = decompress(blocks, w, h)
         if not out_name:
-            out_name = basename(path) + "-bptc.png"
+            out_name = basename(path) + ("-bptc.png" if cf == CompressionFormat.BPTC else f"-{fmt.lower()}.png")
         with open(out_name, "wb") as f:
             if out_name.endswith(".ktx"):
-                f.write(imageio.ktx_bytes(blocks, w, h))
+                f.write(imageio.ktx_bytes(blocks, w, h, fmt))
+            elif cf == CompressionFormat.BPTC:
+                f.write(imageio.png_bytes(decompress(blocks, w, h)))
             else:
-                f.write(imageio.png_bytes(dec))
+                f.write(imageio.png_bytes(dxt.decompress(blocks, w, h, cf)))
     return 0
 
 

@@ -406,6 +406,18 @@ FASTC_BC7_API fastc_bc7_status fastc_dxt_decompress(const uint8_t *blocks, uint8
 FASTC_BC7_API fastc_bc7_status fastc_dxt_decompress_device(const uint8_t *blocks, uint8_t *rgba,
                                                           uint32_t width, uint32_t height,
                                                           int format, void *stream);
+/* FasTC's Image::ComputePSNR (as fastc_bc7_psnr) of DXT1 / DXT5 blocks
+ * against the original texels, decoded on the GPU. Host buffers: *psnr (may
+ * be NULL) and, if not NULL, one double per block in block_sse. Device
+ * buffers: block_sse (one double per block) and, if not NULL, their
+ * fixed-order sum in *total, enqueued on `stream`. */
+FASTC_BC7_API fastc_bc7_status fastc_dxt_psnr(const uint8_t *blocks, const uint8_t *rgba, uint32_t width,
+                                             uint32_t height, int format, double *psnr,
+                                             double *block_sse);
+FASTC_BC7_API fastc_bc7_status fastc_dxt_block_error_device(const uint8_t *blocks, const uint8_t *rgba,
+                                                           uint32_t width, uint32_t height, int format,
+                                                           double *block_sse, double *total,
+                                                           void *stream);
 
 #ifdef __cplusplus
 }

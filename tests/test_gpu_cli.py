@@ -52,3 +52,28 @@ def test_tc_log_is_compress_with_stats(gpu, tmp_path, monkeypatch):
     assert (tmp_path / "logged.log").read_text() == log
     blocks, _, _ = imageio.read_ktx((tmp_path / "out.ktx").read_bytes())
     assert np.array_equal(blocks, want)
+
+
+@pytest.mark.parametrize("fmt", ["DXT1", "DXT5"])
+def test_tc_dxt_to_ktx_and_png(gpu, port, tmp_path, capsys, monkeypatch, fmt):
+    """-f DXT1 / DXT5: the blocks in FasTC's KTX layout are the oracle's
+    (FasTC's) blocks, the PSNR is FasTC's metric of their decode, the
+    default output is <basename>-dxt1.png / -dxt5.png, and -l leaves an
+    empty log (FasTC has no logging DXT encoder)."""
+    from fastc_gb300 import imageio, tc
+
+    img = make_image("tile_mix_radial_alpha(44, 48, 32, 100, 200)")
+    src = tmp_path / "dxt_in.png"
+    src.write_bytes(imageio.png_bytes(img))
+    out = tmp_path / "out.ktx"
+    assert tc.main(["-f", fmt, "-d", str(out), str(src)]) == 0
+    blocks, w, h, f = imageio.read_ktx(out.read_bytes(), with_format=True)
+    want = port.dxt_compress(img, fmt == "DXT5")
+    assert (w, h, f) == (48, 32, fmt) and np.array_equal(blocks, want)
+    dec = port.dxt_decompress(want, 48, 32, fmt == "DXT5")
+    line = [l for l in capsys.readouterr().out.splitlines() if l.startswith("PSNR: ")]
+    assert line and line[0] == f"PSNR: {port.psnr(img, dec):.3f}"
+    monkeypatch.chdir(tmp_path)
+    assert tc.main(["-f", fmt, "-l", str(src)]) == 0
+    assert np.array_equal(imageio.read_png((tmp_path / f"dxt_in-{fmt.lower()}.png").read_bytes()), dec)
+    assert (tmp_path / "dxt_in.log").read_text() == ""

@@ -65,6 +65,25 @@ def test_ktx_layout_matches_fastc_writer():
     assert (w, h) == (8, 8) and np.array_equal(b, blocks)
 
 
+@pytest.mark.parametrize("fmt,internal,base,size", [("DXT1", 0x83F0, 0x1907, 32), ("DXT5", 0x83F3, 0x1908, 64)])
+def test_ktx_layout_for_dxt(fmt, internal, base, size):
+    """ImageWriterKTX's DXT cases (IO/src/ImageWriterKTX.cpp:104-112,
+    140-151): the S3TC internal formats, RGB base for DXT1, half a byte per
+    texel for DXT1."""
+    from fastc_gb300 import imageio
+
+    blocks = np.arange(size, dtype=np.uint8)
+    raw = imageio.ktx_bytes(blocks, 8, 8, fmt)
+    assert len(raw) == 96 + size
+    words = struct.unpack("<13I", raw[12:64])
+    assert words[4:6] == (internal, base)
+    assert raw[92:96] == struct.pack("<I", size)
+    b, w, h, f = imageio.read_ktx(raw, with_format=True)
+    assert (w, h, f) == (8, 8, fmt) and np.array_equal(b, blocks)
+    with pytest.raises(ValueError):
+        imageio.ktx_bytes(blocks[:-1], 8, 8, fmt)
+
+
 def test_pad_to_blocks_and_basename():
     from fastc_gb300 import imageio, tc
 
@@ -79,6 +98,7 @@ def test_pad_to_blocks_and_basename():
 def test_cli_refuses_what_it_does_not_do(capsys):
     from fastc_gb300 import tc
 
-    assert tc.main(["-f", "DXT1", "x.png"]) == 1
+    assert tc.main(["-f", "ETC1", "x.png"]) == 1
+    assert tc.main(["-f", "PVRTC", "x.png"]) == 1
     assert tc.main(["-q"]) == 1
     assert tc.main([]) == 1
