@@ -504,10 +504,12 @@ __global__ void dxt_error_kernel(const uint8_t *__restrict__ blocks, const uint8
       const uint8_t *p = rgba + ((size_t)(by * 4 + y) * width + bx * 4 + x) * 4;
       const uint32_t d = dec[4 * y + x];
       const double ra = (double)p[3] / 255.0, ua = (double)(d >> 24) / 255.0;
+      double t = 0.0;  // the texel's three terms first, then the block's running sum
       for (int c = 0; c < 3; c++) {
         const double e = ra * (double)p[c] - ua * (double)((d >> (8 * c)) & 0xFF);
-        s += e * e;
+        t += e * e;
       }
+      s += t;
     }
   }
   sse[b] = s;
