@@ -3,6 +3,7 @@
 // the select stage and by the annealing loop (bc7_pipeline.cu).
 #pragma once
 
+#include <climits>
 #include <cstdint>
 
 namespace fastc {
@@ -116,19 +117,53 @@ __device__ __forceinline__ int pair_term(uint32_t e, const uint4 *pal, int j1, b
   return second ? t2 : t1;
 }
 
+// Ascending sort of 16 integers in registers (bitonic network, fixed
+// indices so that the array is never addressed dynamically).
+__device__ __forceinline__ void sort16(int (&v)[16]) {
+#pragma unroll
+  for (int k = 2; k <= 16; k <<= 1)
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+      for (int i = 0; i < 16; i++) {
+        const int l = i ^ j;
+        if (l > i) {
+          const int a = v[i], b = v[l];
+          const bool up = (i & k) == 0;
+          v[i] = up ? min(a, b) : max(a, b);
+          v[l] = up ? max(a, b) : min(a, b);
+        }
+      }
+}
+
 // A lower bound on the uniform-metric QuantizedError of n texels against
-// ANY pair of endpoints, for pruning fits that cannot win their block.
-// Every palette colour is the exact interpolation rounded per channel (at
-// most half a unit), so it lies within one unit of the line through the
-// endpoints; a texel at distance d from that line has error at least
-// max(0, d - 1)^2 >= d^2 - 2d. Summed: S - 2 sqrt(n S) (Cauchy-Schwarz),
-// with S = sum d^2 >= R, the scatter left after the best-fitting line
-// (trace minus largest eigenvalue of the scatter matrix); the bound grows
-// with S for S >= n, so R - 2 sqrt(n R) holds whenever R >= n. The largest
-// eigenvalue of the scatter A scaled to unit trace is at most
-// sqrt(|A^2|_F) (the fourth root of the sum of the eigenvalues' fourth
-// powers). The scatter is exact in integers; the float steps after it are
-// covered by a margin of 1e-5 of the trace.
+// ANY pair of endpoints with a kLevels-colour palette, for pruning fits
+// that cannot win their block; the larger of two bounds.
+//
+// Line term: every palette colour is the exact interpolation rounded per
+// channel (at most half a unit), so it lies within one unit of the line
+// through the endpoints; a texel at distance d from that line has error at
+// least max(0, d - 1)^2 >= d^2 - 2d. Summed: S - 2 sqrt(n S)
+// (Cauchy-Schwarz), with S = sum d^2 >= R, the scatter left after the
+// best-fitting line (trace minus largest eigenvalue of the scatter matrix);
+// the bound grows with S for S >= n, so R - 2 sqrt(n R) holds whenever
+// R >= n. The largest eigenvalue of the scatter A scaled to unit trace is
+// at most sqrt(|A^2|_F) (the fourth root of the sum of the eigenvalues'
+// fourth powers). The scatter is exact in integers; the float steps after
+// it are covered by a margin of 1e-5 of the trace.
+//
+// Palette-size term: on any unit direction u a texel's error is at least
+// (u.p - u.c)^2, so the error is at least the best kLevels-level
+// quantisation of the projections u.p (1-D k-means; its groups are runs of
+// the sorted projections). A run of span w costs at least w^2 / 2, and the
+// runs' spans add up to at least G, the n - kLevels smallest gaps between
+// sorted projections, so the error is at least G^2 / (2 kLevels). It is
+// computed for 4-colour palettes (where it prunes; with 8 or 16 colours the
+// clusters rarely have enough texels). u is the scatter's principal
+// direction (four power iterations), rounded to an integer
+// direction d with components in 1/64 of the largest, so the projections
+// d.p are exact integers and the term is G^2 / (2 kLevels |d|^2).
+template <int kLevels>
 __device__ __forceinline__ float qe_lower_bound(const uint32_t *pts, int stride, int n) {
   int s[4] = {0, 0, 0, 0}, q[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int k = 0; k < n; k++) {
@@ -173,7 +208,62 @@ __device__ __forceinline__ float qe_lower_bound(const uint32_t *pts, int stride,
   const float lam = sqrtf(sqrtf(f));
   const float R = fmaxf(0.0f, 1.0f - lam - 1e-5f) * ((float)tr / (float)n);
   const float fn = (float)n;
-  return R >= fn ? fmaxf(0.0f, R - 2.0f * sqrtf(fn * R) - 1e-3f * R) : 0.0f;
+  const float line = R >= fn ? fmaxf(0.0f, R - 2.0f * sqrtf(fn * R) - 1e-3f * R) : 0.0f;
+  // the palette-size term prunes in practice for 4-colour palettes only
+  if (kLevels != 4 || n <= kLevels) return line;
+  int d0 = 0;
+#pragma unroll
+  for (int c = 1; c < 4; c++)
+    if (A[c][c] > A[d0][d0]) d0 = c;
+  float u[4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) u[c] = d0 == 0 ? A[c][0] : d0 == 1 ? A[c][1] : d0 == 2 ? A[c][2] : A[c][3];
+#pragma unroll
+  for (int it = 0; it < 4; it++) {
+    float w[4], mx = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      w[a] = A[a][0] * u[0] + A[a][1] * u[1] + A[a][2] * u[2] + A[a][3] * u[3];
+      mx = fmaxf(mx, fabsf(w[a]));
+    }
+    if (!(mx > 0.0f)) return line;
+    const float r = 1.0f / mx;
+#pragma unroll
+    for (int a = 0; a < 4; a++) u[a] = w[a] * r;
+  }
+  const float um = fmaxf(fmaxf(fabsf(u[0]), fabsf(u[1])), fmaxf(fabsf(u[2]), fabsf(u[3])));
+  int d[4], dd = 0;
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    d[c] = __float2int_rn(u[c] * 64.0f / um);
+    dd += d[c] * d[c];
+  }
+  if (dd == 0) return line;
+  int sp[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) {
+    sp[k] = INT_MAX;
+    if (k < n) {
+      const uint32_t e = pts[k * stride];
+      sp[k] = d[0] * (int)(e & 0xFF) + d[1] * (int)((e >> 8) & 0xFF) + d[2] * (int)((e >> 16) & 0xFF) +
+              d[3] * (int)(e >> 24);
+    }
+  }
+  sort16(sp);
+  // G = the gaps' sum less the three largest gaps
+  int sum = 0, g1 = 0, g2 = 0, g3 = 0;
+#pragma unroll
+  for (int k = 0; k < 15; k++) {
+    const int g = k + 1 < n ? sp[k + 1] - sp[k] : 0;
+    sum += g;
+    const int a = max(g1, g), b = max(g2, min(g1, g)), c = max(g3, min(g2, g));
+    g1 = a;
+    g2 = b;
+    g3 = c;
+  }
+  const int G = sum - g1 - g2 - g3;
+  const float fg = (float)G;
+  return fmaxf(line, fg * fg / (float)(2 * kLevels * dd) * (1.0f - 1e-5f));
 }
 
 // Sixteen texels in registers (one-subset modes; texel k is point k).

@@ -983,7 +983,7 @@ __global__ void __launch_bounds__(kSetupThreads, (class_mode(C) == 6 ? 3 : 6)) s
     o.steps = (uint16_t)jb.steps;
     o.pbit = (uint8_t)st.pbit;
     o.flags = (uint8_t)((st.anneal ? kTaskAnneal : 0u) | (jb.metric ? kTaskNonuniform : 0u));
-    const float lb = st.anneal && !jb.metric ? qe_lower_bound(pts, kSetupThreads, c.n) : 0.0f;
+    const float lb = st.anneal && !jb.metric ? qe_lower_bound<kNB>(pts, kSetupThreads, c.n) : 0.0f;
     const uint64_t idx0 = o.idx;
 #pragma unroll 1
     for (int dup = 0; dup < (kPerBlock ? 2 : 1); dup++) {

@@ -1123,11 +1123,79 @@ static void init_ctx(mode_ctx *m, int mode, const block_ctx *b) {
   m->lcg = b->lcg;
 }
 
-/* The GPU pipeline's error lower bound for a fit of n texels (qe_lower_bound
- * in fastc_gb300/csrc/bc7_intqe.cuh), in the same float steps: the scatter
- * left after the best line, from an upper bound on the largest eigenvalue,
- * less the palette's rounding slack. */
-static float fit_lower_bound(const uint32_t *px, int n) {
+/* Whether the fit bound includes the palette-size term (diagnostic switch
+ * for comparing the pruning with and without it; on by default). */
+static int g_level_bound = 1;
+void bc7o_set_level_bound(int on) { g_level_bound = on; }
+
+static void sort_ints(int *v, int n) {
+  for (int i = 1; i < n; i++)
+    for (int j = i; j > 0 && v[j - 1] > v[j]; j--) {
+      const int t = v[j];
+      v[j] = v[j - 1];
+      v[j - 1] = t;
+    }
+}
+
+/* The palette-size term of the GPU pipeline's bound (qe_lower_bound in
+ * fastc_gb300/csrc/bc7_intqe.cuh), in the same steps. A palette has k
+ * colours, so on any unit direction u the error is at least the best
+ * k-level quantisation of the texels' projections (1-D k-means, whose
+ * groups are runs of the sorted projections); a run of span w costs at
+ * least w^2 / 2, and the spans add up to at least the n - k smallest gaps
+ * between sorted projections (G), so the error is at least G^2 / (2 k).
+ * u is the scatter's principal direction (power iteration on the
+ * unit-trace scatter A), rounded to an integer direction d (components in
+ * 1/64 of the largest), so the projections d.p are exact integers and the
+ * bound is G^2 / (2 k |d|^2). Like the GPU, it is computed for 4-colour
+ * palettes only, with four power iterations. */
+static float level_bound(const uint32_t *px, int n, int k, float A[4][4]) {
+  if (k != 4 || n <= k) return 0.0f; /* computed for 4-colour palettes only */
+  int d0 = 0;
+  for (int c = 1; c < 4; c++)
+    if (A[c][c] > A[d0][d0]) d0 = c;
+  float v[4];
+  for (int c = 0; c < 4; c++) v[c] = A[c][d0];
+  for (int it = 0; it < 4; it++) {
+    float w[4], m = 0.0f;
+    for (int a = 0; a < 4; a++) {
+      w[a] = A[a][0] * v[0] + A[a][1] * v[1] + A[a][2] * v[2] + A[a][3] * v[3];
+      const float x = fabsf(w[a]);
+      if (x > m) m = x;
+    }
+    if (!(m > 0.0f)) return 0.0f;
+    const float r = 1.0f / m;
+    for (int a = 0; a < 4; a++) v[a] = w[a] * r;
+  }
+  float m = 0.0f;
+  for (int c = 0; c < 4; c++)
+    if (fabsf(v[c]) > m) m = fabsf(v[c]);
+  int d[4], dd = 0;
+  for (int c = 0; c < 4; c++) {
+    d[c] = (int)rintf(v[c] * 64.0f / m);
+    dd += d[c] * d[c];
+  }
+  if (dd == 0) return 0.0f;
+  int sp[16], g[16];
+  for (int i = 0; i < n; i++) {
+    sp[i] = 0;
+    for (int c = 0; c < 4; c++) sp[i] += d[c] * (int)((px[i] >> (8 * c)) & 0xFF);
+  }
+  sort_ints(sp, n);
+  for (int i = 0; i + 1 < n; i++) g[i] = sp[i + 1] - sp[i];
+  sort_ints(g, n - 1);
+  int G = 0;
+  for (int i = 0; i < n - k; i++) G += g[i];
+  const float fg = (float)G;
+  return fg * fg / (float)(2 * k * dd) * (1.0f - 1e-5f);
+}
+
+/* The GPU pipeline's error lower bound for a fit of n texels and a k-colour
+ * palette (qe_lower_bound in fastc_gb300/csrc/bc7_intqe.cuh), in the same
+ * float steps: the larger of the scatter left after the best line (from an
+ * upper bound on the largest eigenvalue, less the palette's rounding slack)
+ * and the palette-size term above. */
+static float fit_lower_bound(const uint32_t *px, int n, int k) {
   int sm[4] = {0, 0, 0, 0}, q[10] = {0};
   for (int k = 0; k < n; k++) {
     int v[4];
@@ -1162,9 +1230,13 @@ static float fit_lower_bound(const uint32_t *px, int n) {
   if (one < 0.0f) one = 0.0f;
   const float R = one * ((float)tr / (float)n);
   const float fn = (float)n;
-  if (R < fn) return 0.0f;
-  const float lb = R - 2.0f * sqrtf(fn * R) - 1e-3f * R;
-  return lb > 0.0f ? lb : 0.0f;
+  float lb = 0.0f;
+  if (R >= fn) {
+    lb = R - 2.0f * sqrtf(fn * R) - 1e-3f * R;
+    if (lb < 0.0f) lb = 0.0f;
+  }
+  const float lv = g_level_bound ? level_bound(px, n, k, A) : 0.0f;
+  return lv > lb ? lv : lb;
 }
 
 /* Records one fit of the traced block. For a fit that took FasTC's
@@ -1183,7 +1255,8 @@ static void trace_fit(const mode_ctx *m, const cluster *c, int slot, int subset,
   t->final_err = final_err;
   if (note->annealed) {
     t->init_err = note->init + note->aerr;
-    t->lower_bound = (m->metric ? 0.0 : (double)fit_lower_bound(c->px, c->n)) + note->aerr;
+    t->lower_bound =
+        (m->metric ? 0.0 : (double)fit_lower_bound(c->px, c->n, 1 << bits_index(m, -1))) + note->aerr;
   } else {
     t->init_err = t->lower_bound = final_err;
   }

@@ -80,6 +80,10 @@ typedef struct {
 /* bc7o_compress_block, also listing the block's cluster fits (at most cap;
  * returns how many were recorded). Diagnostic: checks the pipeline's
  * pruning rule against the whole algorithm. */
+/* Diagnostic: leave the palette-size term out of the traced bounds (0) or
+ * put it back (1, the default). */
+void bc7o_set_level_bound(int on);
+
 int bc7o_trace_block(const uint32_t px[16], const bc7o_settings *s, uint32_t bx,
                      uint32_t by, uint32_t *wm, uint32_t *lcg, uint8_t out[16],
                      bc7o_fit_trace *fits, int cap);
