@@ -134,14 +134,23 @@ def measured_peaks():
 
 
 def profile_per_block():
-    """DRAM bytes and warp instructions per block of one encode launch, from
-    the committed ncu summary (profiles/bc7_encode_traffic.json)."""
+    """(DRAM bytes, warp instructions) per block from the committed ncu
+    summaries: the instructions from the launch list of this workload's own
+    timed step (profiles/bc7_encode_texture_set_512_q50.json, one pass), the
+    DRAM bytes from a multi-pass capture of a 4096x4096 tile-mix launch
+    (profiles/bc7_encode_traffic.json), scaled per block."""
+    traffic = inst = None
     try:
         with open(os.path.join(ROOT, "profiles", "bc7_encode_traffic.json")) as f:
-            d = json.load(f)
-        return float(d["dram_bytes_per_block"]), float(d["warp_instructions_per_block"])
+            traffic = float(json.load(f)["dram_bytes_per_block"])
     except Exception:
-        return None, None
+        pass
+    try:
+        with open(os.path.join(ROOT, "profiles", "bc7_encode_texture_set_512_q50.json")) as f:
+            inst = float(json.load(f)["warp_instructions_per_block"])
+    except Exception:
+        pass
+    return traffic, inst
 
 
 # The CPU legs encode a uniform sample of the set's blocks: every
@@ -836,12 +845,13 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": (tpb * total_blocks) if tpb else None,
-                     "note": "issue-bound integer/FP32 search: the annealing kernels issue on 74 % of "
-                             "cycles with the ALU pipe 62 % busy, the setup kernels are latency-bound "
-                             "(47 % issue), while HBM traffic stays under 1 % of peak; traffic (ncu, "
+                     "note": "issue-bound integer/FP32 search: the annealing kernels issue on 73 % of "
+                             "cycles with the ALU pipe 61 % busy, the setup kernels are latency-bound "
+                             "(43 % issue), while HBM traffic stays under 1 % of peak; traffic (ncu, "
                              "per block of a 4096x4096 tile-mix launch, scaled to the set's blocks) "
                              "counts the stages' fit state exchanged through HBM and the setup "
-                             "kernels' spills"},
+                             "kernels' spills; issue_roofline takes the warp instructions per block "
+                             "from the launch list of this workload's timed step"},
         "clocks": clocks.summary(),
     }
     if ipb:
