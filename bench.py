@@ -266,13 +266,21 @@ def band_texels(bands) -> int:
 
 
 def run_cpu_baseline(textures=None):
+    """The oracle port on all host cores over the row sample; also FasTC's
+    work on that sample in its own unit, texel-bucket evaluations of
+    QuantizedError (the port runs FasTC's search, so it counts them)."""
+    from oracle import oracle as O
+
     cores = os.cpu_count() or 1
     bands = band_sample()
     px = band_texels(bands)
+    O.Port().qe_counters(reset=True)
     dt, outs = encode_bands(bands, cores, "port", textures)
+    calls, evals = O.Port().qe_counters(reset=True)
     return {"value": px / dt / 1e6, "unit": "MPix/s", "cores": cores, "kind": "port",
             "sample": f"every {BAND_STRIDE}th block row of the set: {len(bands)} rows, {px} texels, "
-                      f"q50, one pass"}, bands, outs
+                      f"q50, one pass",
+            "qe_calls_per_block": calls / (px / 16), "qe_evaluations_per_block": evals / (px / 16)}, bands, outs
 
 
 def reference_impl(args):
@@ -873,6 +881,24 @@ def main():
             np.array_equal(o, dout[i][y0 * imgs[i].shape[1]:(y0 + 4) * imgs[i].shape[1]].cpu().numpy())
             for o, (i, y0, _) in zip(outs, bands))
         line["cpu_baseline"] = cb
+        # FasTC's work unit: QuantizedError texel-bucket evaluations (20
+        # ops each) per block, counted by the port on the sample, delivered
+        # at the GPU's block rate, against one op per lane per cycle
+        cs = line["clocks"]
+        mhz = cs.get("sm_mhz") or cs.get("sm_max_mhz") or 2070.0
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        ops = cb["qe_evaluations_per_block"] * 20.0 * total_blocks / step_s
+        peak_ops = sms * 128 * mhz * 1e6
+        line["work_roofline"] = {
+            "unit": "ops/s", "achieved": ops, "peak": peak_ops, "frac": ops / peak_ops,
+            "evaluations_per_block": cb["qe_evaluations_per_block"], "ops_per_evaluation": 20,
+            "note": "reference-equivalent work: FasTC's QuantizedError texel-bucket evaluations per "
+                    "block (counted by the oracle port, which runs FasTC's search, on the CPU sample) "
+                    "x 20 ops x the GPU's blocks/s, against SMs x 128 lanes x the SM clock; the GPU "
+                    "does fewer evaluations than this (pruned annealing, each distinct subset "
+                    "estimated once, integer candidate pairs), so the fraction reads the useful "
+                    "work rate in FasTC's units, not the GPU's own instruction rate "
+                    "(issue_roofline)"}
     plan.close()
     small_plan.close()
     if extras:

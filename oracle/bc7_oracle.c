@@ -389,11 +389,38 @@ static void make_cluster(const uint32_t block[16], int shape, int nsub,
 
 static int all_same_point(const cluster *c) { return eq4(c->mx, c->mn); }
 
+/* Work counters (diagnostic): QuantizedError calls and texel-bucket
+ * evaluations (one per palette entry tried for a texel), summed over all
+ * threads. */
+static uint64_t g_qe_calls, g_qe_evals;
+void bc7o_qe_counters(uint64_t out[2], int reset) {
+  out[0] = __atomic_load_n(&g_qe_calls, __ATOMIC_RELAXED);
+  out[1] = __atomic_load_n(&g_qe_evals, __ATOMIC_RELAXED);
+  if (reset) {
+    __atomic_store_n(&g_qe_calls, 0, __ATOMIC_RELAXED);
+    __atomic_store_n(&g_qe_evals, 0, __ATOMIC_RELAXED);
+  }
+}
+
+static float quantized_error_body(const cluster *c, const float *p1, const float *p2,
+                                  int nbuckets, uint32_t mask, const float *metric,
+                                  const int *pbits, uint8_t *indices, uint64_t *evals);
+
 /* RGBACluster::QuantizedError<nBuckets> (RE:190-310). */
 static float quantized_error(const cluster *c, const float *p1,
                              const float *p2, int nbuckets, uint32_t mask,
                              const float *metric, const int *pbits,
                              uint8_t *indices) {
+  uint64_t evals = 0;
+  const float e = quantized_error_body(c, p1, p2, nbuckets, mask, metric, pbits, indices, &evals);
+  __atomic_fetch_add(&g_qe_calls, 1, __ATOMIC_RELAXED);
+  __atomic_fetch_add(&g_qe_evals, evals, __ATOMIC_RELAXED);
+  return e;
+}
+
+static float quantized_error_body(const cluster *c, const float *p1, const float *p2,
+                                  int nbuckets, uint32_t mask, const float *metric,
+                                  const int *pbits, uint8_t *indices, uint64_t *evals) {
   const int prec = nbuckets == 4 ? 2 : (nbuckets == 8 ? 3 : 4);
   uint32_t qp1 = pbits ? to_pixel(p1, mask, pbits[0]) : to_pixel(p1, mask, -1);
   uint32_t qp2 = pbits ? to_pixel(p2, mask, pbits[1]) : to_pixel(p2, mask, -1);
@@ -418,6 +445,7 @@ static float quantized_error(const cluster *c, const float *p1,
       total += dot4(ev, ev);
       if (indices) indices[i] = 0;
     }
+    *evals += (uint64_t)c->n;
     return total;
   }
   for (int i = 0; i < c->n; i++) {
@@ -434,6 +462,7 @@ static float quantized_error(const cluster *c, const float *p1,
     uint8_t best = 0;
     int j = j1;
     do {
+      ++*evals;
       const uint32_t w1 = weight1(prec, j), w0 = 64 - w1;
       float ev[4];
       for (int k = 0; k < 4; k++) {

@@ -80,6 +80,12 @@ typedef struct {
 /* bc7o_compress_block, also listing the block's cluster fits (at most cap;
  * returns how many were recorded). Diagnostic: checks the pipeline's
  * pruning rule against the whole algorithm. */
+/* Diagnostic work counters summed over all threads since the last reset:
+ * out[0] = QuantizedError calls, out[1] = texel-bucket evaluations (one per
+ * palette entry a texel is compared with). reset != 0 zeroes them after
+ * reading. */
+void bc7o_qe_counters(uint64_t out[2], int reset);
+
 /* Diagnostic: leave the palette-size term out of the traced bounds (0) or
  * put it back (1, the default). */
 void bc7o_set_level_bound(int on);

@@ -128,6 +128,13 @@ class Port:
                                                   C.POINTER(BlockStats)]
         self.lib = lib
 
+    def qe_counters(self, reset: bool = False):
+        """(QuantizedError calls, texel-bucket evaluations) summed over all
+        threads since the last reset (diagnostic work counters)."""
+        out = np.zeros(2, dtype=np.uint64)
+        self.lib.bc7o_qe_counters(out.ctypes.data_as(C.POINTER(C.c_uint64)), int(reset))
+        return int(out[0]), int(out[1])
+
     def trace(self, img: np.ndarray, steps=0, modes=0xFF, metric=0, seed=0):
         """Every block's cluster fits (per-fit RNG), in raster block order:
         (blocks, [list of FitTrace per block])."""

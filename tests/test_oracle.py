@@ -157,3 +157,18 @@ def test_float_thresholds_equal_the_double_comparisons():
         assert (x < 1e-10) == (np.float32(x) < np.float32(1e-10))
     for x in neighbours(1e-8):
         assert (x < 1e-8) == (np.float32(x) <= np.float32(1e-8))
+
+
+def test_quantized_error_call_count_matches_reference_profile(port):
+    """The port runs FasTC's search: on the 256x256 gradient + noise + alpha
+    ramp image at q0, QuantizedError is called about 320 times per block,
+    the count a gprof profile of FasTC's own encoder gave on this content.
+    The bench's work roofline counts texel-bucket evaluations the same way."""
+    from conftest import make_image
+
+    img = make_image("gradient_noise_alpha_ramp(1, 256, 256)")
+    port.qe_counters(reset=True)
+    port.compress(img, steps=0)
+    calls, evals = port.qe_counters(reset=True)
+    assert abs(calls / 4096 - 320) < 3, calls / 4096
+    assert 10 * calls < evals < 16 * calls  # one to several palette entries per texel
