@@ -103,10 +103,6 @@ size_t scratch_bytes(uint64_t total, int engine, int task_bound) {
   return b;
 }
 
-size_t scratch_bytes_worst(uint64_t total, int engine) {
-  return std::max(scratch_bytes(total, engine, 16), scratch_bytes(total, engine, fastc::kMaxBlockTasks));
-}
-
 int task_bound_of(const fastc_bc7_settings *s, int per_job, uint32_t n) {
   if (!s) return fastc::block_task_bound(FASTC_BC7_ALL_MODES);
   int tb = 0;

@@ -39,8 +39,6 @@ LaunchShape pick_shape(uint64_t total);
 size_t rank_scratch_bytes(uint64_t total);
 // Scratch of a launch; task_bound: most cluster fits per block of its jobs.
 size_t scratch_bytes(uint64_t total, int engine, int task_bound);
-// Largest scratch any mask can need (admission bound).
-size_t scratch_bytes_worst(uint64_t total, int engine);
 // Most block_task_bound() over the jobs' settings.
 int task_bound_of(const fastc_bc7_settings *s, int per_job, uint32_t n);
 EncodeScratch carve_scratch(void *base, uint64_t total);

@@ -97,10 +97,11 @@ struct fastc_bc7_server_s {
   Clock::time_point t_last;
 
   // device bytes a batch needs, beyond the per-request texels and blocks
-  // (job table, the quality sums, encoder scratch)
-  size_t batch_overhead(uint64_t blocks, size_t njobs) const {
+  // (job table, the quality sums, encoder scratch for the most cluster fits
+  // per block that the batch's mode masks allow)
+  size_t batch_overhead(uint64_t blocks, size_t njobs, int task_bound) const {
     return round_up(njobs * sizeof(JobDev)) + round_up(njobs * sizeof(double)) +
-           round_up(blocks * sizeof(double)) + scratch_bytes_worst(blocks, engine);
+           round_up(blocks * sizeof(double)) + scratch_bytes(blocks, engine, task_bound);
   }
 
   void loop();
@@ -271,23 +272,32 @@ void fastc_bc7_server_s::loop() {
       std::vector<Request *> batch;
       uint64_t blocks = 0;
       size_t data = 0;
+      int tb = 0;
+      // A batch takes at most its share of the budget (budget / slots), so
+      // that when the queue is long, batches stay small enough for every
+      // slot to be in flight (a larger batch also needs the pipeline's
+      // second chunk buffer); a single request may use the whole budget.
+      const size_t share = cfg.memory_budget / cfg.max_inflight;
       while (!pending.empty() && batch.size() < cfg.max_batch_jobs) {
         Request *r = pending.front();
         const uint64_t nb = blocks + r->count;
         const size_t nd = data + round_up(r->in_bytes) + round_up(r->out_bytes);
-        const size_t need = nd + batch_overhead(nb, batch.size() + 1);
-        if ((!batch.empty() && nb > cfg.max_batch_blocks) || in_use + need > cfg.memory_budget) break;
+        const int ntb = std::max(tb, fastc::block_task_bound(r->settings.block_modes));
+        const size_t need = nd + batch_overhead(nb, batch.size() + 1, ntb);
+        if (!batch.empty() && (nb > cfg.max_batch_blocks || need > share)) break;
+        if (in_use + need > cfg.memory_budget) break;
         pending.pop_front();
         r->state = kRunning;
         batch.push_back(r);
         blocks = nb;
         data = nd;
+        tb = ntb;
       }
       if (!batch.empty()) {
         free_slot->busy = true;
         free_slot->finished = false;
         free_slot->reqs = batch;
-        free_slot->bytes = data + batch_overhead(blocks, batch.size());
+        free_slot->bytes = data + batch_overhead(blocks, batch.size(), tb);
         in_use += free_slot->bytes;
         peak = std::max(peak, in_use);
         batches++;
@@ -376,7 +386,8 @@ fastc_bc7_status fastc_bc7_server_submit(fastc_bc7_server s, const fastc_bc7_job
   r->out_bytes = (size_t)count * 16;
   r->t_submit = Clock::now();
   std::lock_guard<std::mutex> lk(s->mu);
-  const size_t alone = round_up(r->in_bytes) + round_up(r->out_bytes) + s->batch_overhead(count, 1);
+  const size_t alone = round_up(r->in_bytes) + round_up(r->out_bytes) +
+                       s->batch_overhead(count, 1, fastc::block_task_bound(r->settings.block_modes));
   s->submitted++;
   if (!s->started) {
     s->started = true;
