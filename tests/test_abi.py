@@ -163,3 +163,19 @@ def test_bptc_entry_rejects_dxt_jobs():
     img = np.zeros((8, 8, 4), np.uint8)
     with pytest.raises(BC7Error):
         compress(CompressionJob(img, np.zeros(64, np.uint8), 8, 8, format=CompressionFormat.DXT5))
+
+
+def test_dxt_empty_ranges_need_no_device(bc7lib):
+    """Jobs whose raster range holds no block (FasTC's walk writes nothing)
+    return OK at once, on host and device entry points, without a GPU."""
+    from fastc_gb300._lib import Job
+
+    buf = (C.c_uint8 * 4096)()
+    addr = C.addressof(buf)
+    for rect in [(4, 4, 4, 4), (8, 4, 4, 4)]:
+        j = Job(addr, addr, 16, 16, *rect)
+        assert bc7lib.fastc_bc7_job_blocks(C.byref(j)) == 0
+        for fmt in (1, 5):
+            assert bc7lib.fastc_dxt_compress(C.byref(j), fmt) == 0
+            assert bc7lib.fastc_dxt_compress_batch(C.byref(j), 1, fmt) == 0
+    assert bc7lib.fastc_dxt_compress_batch(None, 0, 1) == 0
