@@ -18,6 +18,12 @@
  *                             Core/include/FasTC/TexComp.h:81-88
  *   fastc_bc7_decompress      BPTCC::Decompress(const DecompressionJob&)
  *                             BPTCEncoder/include/FasTC/BPTCCompressor.h:216
+ *   fastc_dxt_compress        DXTC::CompressImageDXT1 / CompressImageDXT5
+ *                             (const CompressionJob&)
+ *                             DXTEncoder/include/FasTC/DXTCompressor.h:24-25
+ *                             (the Core plugin slot Core/src/TexComp.cpp:130-134)
+ *   fastc_dxt_decompress      DXTC::DecompressDXT1 / DecompressDXT5
+ *                             DXTEncoder/include/FasTC/DXTCompressor.h:27-28
  *
  * Differences a caller can observe:
  *   * steps > 0 draws annealing randomness from a per-fit stream seeded by
