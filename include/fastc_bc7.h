@@ -1,7 +1,9 @@
 /*
- * fastc_bc7.h -- C ABI of the GB300 BC7 (BPTC) encoder.
+ * fastc_bc7.h -- C ABI of the GB300 BC7 (BPTC) encoder, and of its DXT1 /
+ * DXT5 encoder and decoder.
  *
- * Drop-in boundary for FasTC's BPTC encode path. Every entry point takes
+ * Drop-in boundary for FasTC's BPTC encode path (and its DXT path, at the
+ * end of this header). Every entry point takes
  * plain pointers and sizes and returns a status code; none throws, none
  * keeps a pointer after it returns (plans excepted, see below).
  *
