@@ -687,6 +687,47 @@ fastc_bc7_status fastc_dxt_compress_batch(const fastc_bc7_job *jobs, uint32_t n,
   std::lock_guard<std::mutex> lk(fastc::g_dxt_mu);
   CK(fastc::host_context(dev, 2 * (size_t)groups));
   fastc::DxtHostContext &h = fastc::g_dxt_host;
+  // Page-locked host buffers (cudaHostAlloc, cudaHostRegister) are mapped
+  // into the device's address space: the kernel then reads the texels and
+  // writes the blocks across the host link itself, with no staging copies
+  // (on GB300 the NVLink-C2C link to the Grace CPU). Every job's buffers
+  // must be page-locked for this; otherwise the rows are staged below.
+  bool mapped = true;
+  std::vector<JobDev> zj(dj);
+  for (uint32_t i = 0; i < n && mapped; i++) {
+    if (!zj[i].nblocks) continue;
+    cudaPointerAttributes ai{}, ao{};
+    if (cudaPointerGetAttributes(&ai, jobs[i].in) != cudaSuccess ||
+        cudaPointerGetAttributes(&ao, jobs[i].out) != cudaSuccess) {
+      cudaGetLastError();
+      mapped = false;
+      break;
+    }
+    mapped = ai.type == cudaMemoryTypeHost && ao.type == cudaMemoryTypeHost && ai.devicePointer &&
+             ao.devicePointer;
+    if (mapped) {
+      zj[i].in = static_cast<const uint8_t *>(ai.devicePointer);
+      zj[i].out = static_cast<uint8_t *>(ao.devicePointer);
+      zj[i].row0 = 0;
+      zj[i].out_first = 0;
+    }
+  }
+  if (mapped) {
+    for (uint32_t k0 = 0; k0 < n; k0 += fastc::kDxtJobsPerLaunch) {
+      const uint32_t m = std::min<uint32_t>(fastc::kDxtJobsPerLaunch, n - k0);
+      uint64_t begin = 0;
+      for (uint32_t k = k0; k < k0 + m; k++) {
+        JobDev &d = zj[k];
+        d.flags = fastc::host::align_flags(d.in, d.out);
+        if (!alpha) d.flags &= ~fastc::kJobOut16;
+        d.begin = begin;
+        begin += d.nblocks;
+      }
+      CK(fastc::dxt_launch(zj.data() + k0, m, begin, alpha, h.comp));
+    }
+    CK(cudaStreamSynchronize(h.comp));
+    return FASTC_BC7_OK;
+  }
   CK(fastc::ensure(&h.in, &h.in_cap, in_total));
   CK(fastc::ensure(&h.out, &h.out_cap, out_total));
   uint8_t *in = static_cast<uint8_t *>(h.in), *out = static_cast<uint8_t *>(h.out);

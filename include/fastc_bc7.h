@@ -396,9 +396,11 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_get_launch_shape(int *warps_per_cta, in
 #define FASTC_DXT5 5
 /* Host buffers; returns when `out` holds the blocks. */
 FASTC_BC7_API fastc_bc7_status fastc_dxt_compress(const fastc_bc7_job *job, int format);
-/* n jobs of host buffers in one call: uploads, encodes and downloads of
- * groups of jobs overlap; returns when every `out` holds its blocks.
- * Page-locked buffers copy fastest. */
+/* n jobs of host buffers in one call; returns when every `out` holds its
+ * blocks. When every job's buffers are page-locked (cudaHostAlloc,
+ * cudaHostRegister), the encoder reads the texels and writes the blocks
+ * through the device's mapping of host memory, with no staging copies;
+ * otherwise uploads, encodes and downloads of groups of jobs overlap. */
 FASTC_BC7_API fastc_bc7_status fastc_dxt_compress_batch(const fastc_bc7_job *jobs, uint32_t n,
                                                        int format);
 /* Device buffers, enqueued on `stream` (NULL: the legacy default stream);

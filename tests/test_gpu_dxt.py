@@ -171,6 +171,43 @@ def test_many_host_jobs_in_one_call(gpu, port, code):
             assert np.array_equal(o, want)
 
 
+@pytest.mark.parametrize("code", [1, 5])
+def test_page_locked_host_jobs(gpu, port, code):
+    """Page-locked host buffers go through the device's mapping of host
+    memory (no staging); the blocks are the same, sub-jobs included, and
+    a mix with a pageable buffer falls back to the staged copies."""
+    import torch
+
+    from fastc_gb300 import CompressionJob, dxt, synth
+
+    texs = synth.texture_set(seed=11, count=40, lo_log2=2, hi_log2=8)
+    pin_in = [torch.from_numpy(t.reshape(-1)).pin_memory() for t in texs]
+    pin_out = [torch.zeros(t.shape[0] * t.shape[1] * bsz(code) // 16, dtype=torch.uint8).pin_memory()
+               for t in texs]
+    jobs = [CompressionJob(a.numpy(), o.numpy(), t.shape[1], t.shape[0], format=fmt_of(code))
+            for a, o, t in zip(pin_in, pin_out, texs)]
+    big = max(range(len(texs)), key=lambda i: texs[i].size)
+    t = texs[big]
+    jobs[big] = CompressionJob(pin_in[big].numpy(), pin_out[big].numpy(), t.shape[1], t.shape[0], 4, 4,
+                               t.shape[1], 8, format=fmt_of(code))
+    dxt.compress_dxt_jobs(jobs)
+    for i, (t, o) in enumerate(zip(texs, pin_out)):
+        want = port.dxt_compress(t, code == 5)
+        got = o.numpy()
+        if i == big:
+            bw, b = t.shape[1] // 4, bsz(code)
+            assert np.array_equal(got[b * (bw + 1):b * 3 * bw], want[b * (bw + 1):b * 3 * bw])
+            assert not got[:b * (bw + 1)].any() and not got[b * 3 * bw:].any()
+        else:
+            assert np.array_equal(got, want)
+    # one pageable output in the list: every job is staged
+    out0 = np.zeros_like(pin_out[0].numpy())
+    mixed = [CompressionJob(pin_in[0].numpy(), out0, texs[0].shape[1], texs[0].shape[0], format=fmt_of(code))]
+    mixed += jobs[1:4]
+    dxt.compress_dxt_jobs(mixed)
+    assert np.array_equal(out0, port.dxt_compress(texs[0], code == 5))
+
+
 def test_compress_image_data_dispatches_on_format(gpu, port):
     from fastc_gb300 import CompressionFormat, compress_image_data
 
