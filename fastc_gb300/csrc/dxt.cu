@@ -713,7 +713,11 @@ fastc_bc7_status fastc_dxt_compress_batch(const fastc_bc7_job *jobs, uint32_t n,
     }
   }
   if (mapped) {
-    for (uint32_t k0 = 0; k0 < n; k0 += fastc::kDxtJobsPerLaunch) {
+    // the groups' launches are independent: spread over the three streams
+    // so that small groups overlap while the link is busy
+    const cudaStream_t ss[3] = {h.comp, h.h2d, h.d2h};
+    uint32_t g = 0;
+    for (uint32_t k0 = 0; k0 < n; k0 += fastc::kDxtJobsPerLaunch, g++) {
       const uint32_t m = std::min<uint32_t>(fastc::kDxtJobsPerLaunch, n - k0);
       uint64_t begin = 0;
       for (uint32_t k = k0; k < k0 + m; k++) {
@@ -723,9 +727,9 @@ fastc_bc7_status fastc_dxt_compress_batch(const fastc_bc7_job *jobs, uint32_t n,
         d.begin = begin;
         begin += d.nblocks;
       }
-      CK(fastc::dxt_launch(zj.data() + k0, m, begin, alpha, h.comp));
+      CK(fastc::dxt_launch(zj.data() + k0, m, begin, alpha, ss[g % 3]));
     }
-    CK(cudaStreamSynchronize(h.comp));
+    for (cudaStream_t st : ss) CK(cudaStreamSynchronize(st));
     return FASTC_BC7_OK;
   }
   CK(fastc::ensure(&h.in, &h.in_cap, in_total));
