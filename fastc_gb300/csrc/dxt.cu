@@ -712,12 +712,23 @@ fastc_bc7_status fastc_dxt_compress_batch(const fastc_bc7_job *jobs, uint32_t n,
       zj[i].out_first = 0;
     }
   }
+  // Every stream of the call is drained before it returns, also after an
+  // error, so that no copy or kernel of the call still touches the caller's
+  // buffers afterwards; the first error is reported.
+  const cudaStream_t ss[3] = {h.comp, h.h2d, h.d2h};
+  auto drain = [&](cudaError_t e) -> fastc_bc7_status {
+    for (cudaStream_t st : ss) {
+      const cudaError_t se = cudaStreamSynchronize(st);
+      if (e == cudaSuccess) e = se;
+    }
+    return e == cudaSuccess ? FASTC_BC7_OK : fail_cuda(e);
+  };
+  cudaError_t e = cudaSuccess;
   if (mapped) {
     // the groups' launches are independent: spread over the three streams
     // so that small groups overlap while the link is busy
-    const cudaStream_t ss[3] = {h.comp, h.h2d, h.d2h};
     uint32_t g = 0;
-    for (uint32_t k0 = 0; k0 < n; k0 += fastc::kDxtJobsPerLaunch, g++) {
+    for (uint32_t k0 = 0; k0 < n && e == cudaSuccess; k0 += fastc::kDxtJobsPerLaunch, g++) {
       const uint32_t m = std::min<uint32_t>(fastc::kDxtJobsPerLaunch, n - k0);
       uint64_t begin = 0;
       for (uint32_t k = k0; k < k0 + m; k++) {
@@ -727,42 +738,39 @@ fastc_bc7_status fastc_dxt_compress_batch(const fastc_bc7_job *jobs, uint32_t n,
         d.begin = begin;
         begin += d.nblocks;
       }
-      CK(fastc::dxt_launch(zj.data() + k0, m, begin, alpha, ss[g % 3]));
+      e = fastc::dxt_launch(zj.data() + k0, m, begin, alpha, ss[g % 3]);
     }
-    for (cudaStream_t st : ss) CK(cudaStreamSynchronize(st));
-    return FASTC_BC7_OK;
+    return drain(e);
   }
   CK(fastc::ensure(&h.in, &h.in_cap, in_total));
   CK(fastc::ensure(&h.out, &h.out_cap, out_total));
   uint8_t *in = static_cast<uint8_t *>(h.in), *out = static_cast<uint8_t *>(h.out);
-  for (uint32_t g = 0; g < groups; g++) {
+  for (uint32_t g = 0; g < groups && e == cudaSuccess; g++) {
     const uint32_t k0 = g * fastc::kDxtJobsPerLaunch;
     const uint32_t m = std::min<uint32_t>(fastc::kDxtJobsPerLaunch, n - k0);
     uint64_t begin = 0;
-    for (uint32_t k = k0; k < k0 + m; k++) {
+    for (uint32_t k = k0; k < k0 + m && e == cudaSuccess; k++) {
       JobDev &d = dj[k];
       if (d.nblocks)
-        CK(cudaMemcpyAsync(in + in_off[k], jobs[k].in + (size_t)d.row0 * jobs[k].width * 4, in_bytes[k],
-                           cudaMemcpyHostToDevice, h.h2d));
+        e = cudaMemcpyAsync(in + in_off[k], jobs[k].in + (size_t)d.row0 * jobs[k].width * 4, in_bytes[k],
+                            cudaMemcpyHostToDevice, h.h2d);
       d.in = in + in_off[k];
       d.out = out + out_off[k];
       d.flags = fastc::kJobIn16 | (alpha ? fastc::kJobOut16 : 0u);
       d.begin = begin;
       begin += d.nblocks;
     }
-    CK(cudaEventRecord(h.ev[2 * g], h.h2d));
-    CK(cudaStreamWaitEvent(h.comp, h.ev[2 * g], 0));
-    CK(fastc::dxt_launch(dj.data() + k0, m, begin, alpha, h.comp));
-    CK(cudaEventRecord(h.ev[2 * g + 1], h.comp));
-    CK(cudaStreamWaitEvent(h.d2h, h.ev[2 * g + 1], 0));
-    for (uint32_t k = k0; k < k0 + m; k++)
+    if (e == cudaSuccess) e = cudaEventRecord(h.ev[2 * g], h.h2d);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h.comp, h.ev[2 * g], 0);
+    if (e == cudaSuccess) e = fastc::dxt_launch(dj.data() + k0, m, begin, alpha, h.comp);
+    if (e == cudaSuccess) e = cudaEventRecord(h.ev[2 * g + 1], h.comp);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h.d2h, h.ev[2 * g + 1], 0);
+    for (uint32_t k = k0; k < k0 + m && e == cudaSuccess; k++)
       if (dj[k].nblocks)
-        CK(cudaMemcpyAsync(jobs[k].out + (size_t)dj[k].first * bsz, out + out_off[k],
-                           (size_t)dj[k].nblocks * bsz, cudaMemcpyDeviceToHost, h.d2h));
+        e = cudaMemcpyAsync(jobs[k].out + (size_t)dj[k].first * bsz, out + out_off[k],
+                            (size_t)dj[k].nblocks * bsz, cudaMemcpyDeviceToHost, h.d2h);
   }
-  // the last download waited on the last encode, which waited on the last upload
-  CK(cudaStreamSynchronize(h.d2h));
-  return FASTC_BC7_OK;
+  return drain(e);
 }
 
 fastc_bc7_status fastc_dxt_compress(const fastc_bc7_job *job, int format) {
