@@ -1,12 +1,13 @@
 // DXT1 / DXT5 (BC1 / BC3) encoder and decoder for sm_103a, FasTC's second
-// compression path (DXTEncoder/src/Compressor.cpp:44-93): every 4x4 block
+// compression path (DXTEncoder/src/Compressor.cpp:47-93): every 4x4 block
 // of a job through the stb_dxt v1.06 block encoder that FasTC vendors
-// (DXTEncoder/src/stb_dxt.h), with dithering and one refinement pass; DXT5
-// adds the alpha block. The method, restated per step below from its
-// published description, keeps every integer step and the float and double
-// operation order (the file is compiled without contraction), so the
-// blocks are FasTC's bit for bit. One thread per block: the work per block
-// is a few hundred instructions, all in registers.
+// (DXTEncoder/src/stb_dxt.h, stb_compress_dxt_block :623), with dithering
+// and one refinement pass; DXT5 adds the alpha block. The method, restated
+// per step below from its published description (the stb_dxt.h lines each
+// step corresponds to are given with it), keeps every integer step and the
+// float and double operation order (the file is compiled without
+// contraction), so the blocks are FasTC's bit for bit. One thread per
+// block: about 3,400 instructions per block, all in registers.
 //
 // Jobs travel to the device inside kernel parameters (up to 32 per launch),
 // so the device entry point allocates nothing.
@@ -36,9 +37,10 @@ __host__ __device__ inline int exp5(int q) { return (q << 3) | (q >> 2); }
 __host__ __device__ inline int exp6(int q) { return (q << 2) | (q >> 4); }
 
 // Per 8-bit value, the best endpoint pair (high, low) of the single-colour
-// encoding: the pair whose 1/3 interpolant reproduces the value, with 3 % of
-// the endpoints' distance as a penalty; packed high | low << 8. In global
-// memory (read through the read-only cache: lanes index it divergently).
+// encoding (stb_dxt.h :121-147, built at :603-621): the pair whose 1/3
+// interpolant reproduces the value, with 3 % of the endpoints' distance as
+// a penalty; packed high | low << 8. In global memory (read through the
+// read-only cache: lanes index it divergently).
 __device__ uint16_t g_dxt_match[2][256];  // [0]: 5-bit channels, [1]: 6-bit
 
 void build_match_tables(uint16_t (*tab)[256]) {
@@ -59,9 +61,9 @@ void build_match_tables(uint16_t (*tab)[256]) {
   }
 }
 
-// The dither's 565 quantisers: the channel value (clamped to 0..255, as
-// the reference's table indexed from -8 to 263 is) to its nearest 5- or
-// 6-bit level, expanded back to 8 bits. Arithmetic rather than a table, so
+// The dither's 565 quantisers (the tables of stb_dxt.h :603-621): the
+// channel value (clamped to 0..255, as the table indexed from -8 to 263 is)
+// to its nearest 5- or 6-bit level, expanded back to 8 bits. Arithmetic rather than a table, so
 // that divergent lanes do not serialise on a lookup.
 __device__ __forceinline__ int quant5(int v) { return exp5(mul8bit(min(max(v, 0), 255), 31)); }
 __device__ __forceinline__ int quant6(int v) { return exp6(mul8bit(min(max(v, 0), 255), 63)); }
@@ -72,7 +74,8 @@ __device__ __forceinline__ uint16_t as565(int r, int g, int b) {
   return (uint16_t)((mul8bit(r, 31) << 11) + (mul8bit(g, 63) << 5) + mul8bit(b, 31));
 }
 
-// The palette of endpoints c0, c1 as packed RGB (4-colour interpolation).
+// The palette of endpoints c0, c1 as packed RGB (4-colour interpolation;
+// stb_dxt.h :149-157).
 __device__ __forceinline__ void dxt_palette(uint16_t c0, uint16_t c1, int col[4][3]) {
   col[0][0] = exp5((c0 >> 11) & 31);
   col[0][1] = exp6((c0 >> 5) & 63);
@@ -87,7 +90,8 @@ __device__ __forceinline__ void dxt_palette(uint16_t c0, uint16_t c1, int col[4]
   }
 }
 
-// Floyd-Steinberg dither of each RGB channel to its 565 grid, row by row.
+// Floyd-Steinberg dither of each RGB channel to its 565 grid, row by row
+// (stb_dxt.h :159-184).
 __device__ __forceinline__ void dxt_dither(const uint32_t (&px)[16], uint32_t (&out)[16]) {
 #pragma unroll
   for (int i = 0; i < 16; i++) out[i] = 0;
@@ -121,7 +125,7 @@ __device__ __forceinline__ void dxt_dither(const uint32_t (&px)[16], uint32_t (&
 
 // Indices: each texel's projection on the endpoint direction against the
 // midpoints of the palette's projections, with the projection error diffused
-// Floyd-Steinberg style.
+// Floyd-Steinberg style (stb_dxt.h :186-281, dithered branch).
 __device__ __forceinline__ uint32_t dxt_match(const uint32_t (&px)[16], const int (&col)[4][3]) {
   const int dr = col[0][0] - col[1][0], dg = col[0][1] - col[1][1], db = col[0][2] - col[1][2];
   int stops[4];
@@ -159,7 +163,7 @@ __device__ __forceinline__ uint32_t dxt_match(const uint32_t (&px)[16], const in
 // Endpoints from the principal axis of the (dithered) texels: four power
 // iterations on the RGB covariance from the bounding box's extent, the
 // axis scaled to 512 (or the luma weights when it is short), the texels
-// with the least and greatest projection.
+// with the least and greatest projection (stb_dxt.h :283-385).
 __device__ __forceinline__ void dxt_axis(const uint32_t (&px)[16], uint16_t &max16, uint16_t &min16) {
   int mu[3], mn[3], mx[3];
 #pragma unroll
@@ -247,7 +251,7 @@ __device__ __forceinline__ void single_colour_pair(int r, int g, int b, uint16_t
 
 // Least-squares endpoints for the indices in `mask` (normal equations,
 // Cramer's rule), or the mean's single-colour pair when every texel has the
-// same index; true when the endpoints changed.
+// same index; true when the endpoints changed (stb_dxt.h :387-475).
 __device__ __forceinline__ bool dxt_refine(const uint32_t (&px)[16], uint16_t &max16, uint16_t &min16,
                                            uint32_t mask) {
   const uint16_t old_min = min16, old_max = max16;
@@ -294,7 +298,9 @@ __device__ __forceinline__ bool dxt_refine(const uint32_t (&px)[16], uint16_t &m
   return old_min != mn16 || old_max != mx16;
 }
 
-// The 8-byte colour block: max16, min16, 32 index bits.
+// The 8-byte colour block: max16, min16, 32 index bits (stb_dxt.h
+// :477-549: the constant-block shortcut, dither, fit, match, one refinement,
+// the endpoint order swap).
 __device__ __forceinline__ uint2 dxt_color_block(const uint32_t (&px)[16]) {
   uint32_t mask;
   uint16_t mx16, mn16;
@@ -331,7 +337,8 @@ __device__ __forceinline__ uint2 dxt_color_block(const uint32_t (&px)[16]) {
   return make_uint2((uint32_t)mx16 | ((uint32_t)mn16 << 16), mask);
 }
 
-// The 8-byte alpha block: max, min, 16 3-bit indices by the bias rule.
+// The 8-byte alpha block: max, min, 16 3-bit indices by the bias rule
+// (stb_dxt.h :551-601).
 __device__ __forceinline__ uint2 dxt_alpha_block(const uint32_t (&px)[16]) {
   int mn = (int)(px[0] >> 24), mx = mn;
 #pragma unroll
