@@ -44,7 +44,8 @@ static int mul8bit(int a, int b) {
 static int lerp13(int a, int b) { return (2 * a + b) / 3; }
 
 /* the single-colour table: the endpoint pair whose 1/3 interpolant lands
- * closest to each value, with 3 % of the endpoint distance as a penalty */
+ * closest to each value, with 3 % of the endpoint distance as a penalty
+ * (stb_dxt.h:121-147) */
 static void match_table(uint8_t tab[256][2], const uint8_t *expand, int size) {
   for (int v = 0; v < 256; v++) {
     int best = 256;
@@ -62,6 +63,7 @@ static void match_table(uint8_t tab[256][2], const uint8_t *expand, int size) {
   }
 }
 
+/* stb_dxt.h:603-621 */
 static void init_tables(void) {
   if (gInit) return;
   for (int i = 0; i < 32; i++) gExp5[i] = (uint8_t)((i << 3) | (i >> 2));
@@ -86,7 +88,8 @@ static void from565(uint16_t v, int *c) {
   c[2] = gExp5[v & 31];
 }
 
-/* the four palette colours of endpoints c0, c1 (4-colour interpolation) */
+/* the four palette colours of endpoints c0, c1 (4-colour interpolation;
+ * stb_dxt.h:149-157) */
 static void palette(int col[4][3], uint16_t c0, uint16_t c1) {
   from565(c0, col[0]);
   from565(c1, col[1]);
@@ -97,7 +100,8 @@ static void palette(int col[4][3], uint16_t c0, uint16_t c1) {
 }
 
 /* Floyd-Steinberg dither of each RGB channel to its 565 grid, row by row;
- * px[i][c] are the block's texels, out the dithered ones (RGB only) */
+ * px[i][c] are the block's texels, out the dithered ones (RGB only)
+ * (stb_dxt.h:159-184) */
 static void dither(const uint8_t px[16][4], uint8_t out[16][4]) {
   for (int ch = 0; ch < 3; ch++) {
     const uint8_t *q = (ch == 1 ? gQuantG : gQuantRB) + 8;
@@ -123,7 +127,8 @@ static void dither(const uint8_t px[16][4], uint8_t out[16][4]) {
 }
 
 /* indices: projections onto the endpoint direction, split at the midpoints
- * of the palette's projections, with the projection error diffused */
+ * of the palette's projections, with the projection error diffused
+ * (stb_dxt.h:186-281) */
 static uint32_t match(const uint8_t px[16][4], int col[4][3]) {
   const int dr = col[0][0] - col[1][0], dg = col[0][1] - col[1][1], db = col[0][2] - col[1][2];
   int dots[16], stops[4];
@@ -156,7 +161,8 @@ static uint32_t match(const uint8_t px[16][4], int col[4][3]) {
   return mask;
 }
 
-/* endpoints from the principal axis of the (dithered) texels */
+/* endpoints from the principal axis of the (dithered) texels
+ * (stb_dxt.h:283-385) */
 static void axis_endpoints(const uint8_t px[16][4], uint16_t *max16, uint16_t *min16) {
   int mu[3], mn[3], mx[3];
   for (int ch = 0; ch < 3; ch++) {
@@ -226,7 +232,8 @@ static int clamp_trunc(float y, int hi) {
   return x < 0 ? 0 : (x > hi ? hi : x);
 }
 
-/* least-squares endpoints for the indices in `mask`; 1 when they changed */
+/* least-squares endpoints for the indices in `mask`; 1 when they changed
+ * (stb_dxt.h:387-475) */
 static int refine(const uint8_t px[16][4], uint16_t *max16, uint16_t *min16, uint32_t mask) {
   const uint16_t old_min = *min16, old_max = *max16;
   uint16_t mn16, mx16;
@@ -273,6 +280,7 @@ static int refine(const uint8_t px[16][4], uint16_t *max16, uint16_t *min16, uin
   return old_min != mn16 || old_max != mx16;
 }
 
+/* stb_dxt.h:477-549 */
 static void color_block(const uint8_t px[16][4], uint8_t out[8]) {
   uint32_t mask;
   uint16_t mx16, mn16;
@@ -319,6 +327,7 @@ static void color_block(const uint8_t px[16][4], uint8_t out[8]) {
   for (int k = 0; k < 4; k++) out[4 + k] = (uint8_t)(mask >> (8 * k));
 }
 
+/* stb_dxt.h:551-601 */
 static void alpha_block(const uint8_t px[16][4], uint8_t out[8]) {
   int mn = px[0][3], mx = px[0][3];
   for (int i = 1; i < 16; i++) {
@@ -349,6 +358,7 @@ static void alpha_block(const uint8_t px[16][4], uint8_t out[8]) {
   for (int k = 0; k < 6; k++) out[2 + k] = (uint8_t)(bits >> (8 * k));
 }
 
+/* stb_compress_dxt_block (stb_dxt.h:623-637) with STB_DXT_DITHER */
 void dxto_compress_block(const uint8_t rgba[64], int alpha, uint8_t *out) {
   init_tables();
   uint8_t px[16][4];
@@ -373,6 +383,7 @@ int dxto_compress(const uint8_t *rgba, uint8_t *out, uint32_t w, uint32_t h, int
   return 0;
 }
 
+/* DecompressDXT1Block (Decompressor.cpp:28-65) */
 static void decode_colors(const uint8_t *b, int four, uint32_t out[16], int keep_alpha) {
   const uint16_t c0 = (uint16_t)(b[0] | (b[1] << 8)), c1 = (uint16_t)(b[2] | (b[3] << 8));
   int col[4][3];
@@ -398,6 +409,7 @@ static void decode_colors(const uint8_t *b, int four, uint32_t out[16], int keep
   }
 }
 
+/* DecompressDXT5Block (Decompressor.cpp:67-96) */
 static void decode_alpha(const uint8_t *b, uint32_t out[16]) {
   const int a0 = b[0], a1 = b[1];
   int pal[8] = {a0, a1, 0, 0, 0, 0, 0, 0};
