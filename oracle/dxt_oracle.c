@@ -303,7 +303,6 @@ static void color_block(const uint8_t px[16][4], uint8_t out[8]) {
     } else {
       mask = 0;
     }
-    const uint32_t last = mask;
     if (refine((const uint8_t(*)[4])d, &mx16, &mn16, mask)) {
       if (mx16 != mn16) {
         palette(col, mx16, mn16);
@@ -312,7 +311,6 @@ static void color_block(const uint8_t px[16][4], uint8_t out[8]) {
         mask = 0;
       }
     }
-    (void)last;
   }
   if (mx16 < mn16) {
     const uint16_t t = mn16;
