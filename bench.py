@@ -225,6 +225,18 @@ def encode_bands(bands, threads: int, kind: str, textures=None, steps: int = STE
     outs = [np.zeros(b.shape[0] * b.shape[1], dtype=np.uint8) for _, _, b in bands]
     bufs = [np.ascontiguousarray(b) for _, _, b in bands]
     cursor = itertools.count()
+    # per thread, one whole-texture block buffer per texture, reused by the
+    # pieces of that texture (only each piece's blocks are written), so that
+    # the timing is the encoder's and not the allocation of large buffers
+    local = threading.local()
+
+    def texture_out(i, size):
+        cache = getattr(local, "cache", None)
+        if cache is None:
+            cache = local.cache = {}
+        if i not in cache:
+            cache[i] = np.empty(size, dtype=np.uint8)
+        return cache[i]
 
     def work(_):
         while True:
@@ -249,7 +261,8 @@ def encode_bands(bands, threads: int, kind: str, textures=None, steps: int = STE
                 w = tex.shape[1]
                 if y0 > 0:
                     o = enc.compress(tex, steps=steps, seed=ANNEAL_SEED, rect=(x0, y0, x1, y0),
-                                     state=np.array([0, prior[(k, x0)]], np.uint32))
+                                     state=np.array([0, prior[(k, x0)]], np.uint32),
+                                     out=texture_out(i, tex.shape[0] * w))
                     outs[k][x0 * 4:x1 * 4] = o[y0 * w + x0 * 4:y0 * w + x1 * 4]
                 else:  # the first block row, whole (a rect cannot end on row 0)
                     o = enc.compress(np.ascontiguousarray(tex[:4]), steps=steps, seed=ANNEAL_SEED)

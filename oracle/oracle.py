@@ -193,10 +193,15 @@ class Port:
         return Settings(steps, modes, metric, rng_mode, seed, exp_mode)
 
     def compress(self, img: np.ndarray, steps=0, modes=0xFF, metric=0, rng_mode=RNG_PER_FIT,
-                 seed=0, exp_mode=EXP_PORTABLE, rect=(0, 0, 0, 0), state=None) -> np.ndarray:
+                 seed=0, exp_mode=EXP_PORTABLE, rect=(0, 0, 0, 0), state=None,
+                 out=None) -> np.ndarray:
+        """`out`: a w*h-byte buffer to write into (only the rect's blocks are
+        written), e.g. reused across calls on sub-ranges of one image."""
         img = np.ascontiguousarray(img, dtype=np.uint8)
         h, w = img.shape[:2]
-        out = np.zeros(w * h, dtype=np.uint8)
+        if out is None:
+            out = np.zeros(w * h, dtype=np.uint8)
+        assert out.dtype == np.uint8 and out.size >= w * h and out.flags["C_CONTIGUOUS"]
         st = np.zeros(2, dtype=np.uint32) if state is None else state
         s = self.settings(steps, modes, metric, rng_mode, seed, exp_mode)
         rc = self.lib.bc7o_compress(_ptr(img), _ptr(out), w, h, *rect, C.byref(s), _ptr(st, _u32p))
