@@ -264,8 +264,13 @@ def encode_bands(bands, threads: int, kind: str, textures=None, steps: int = STE
                                      state=np.array([0, prior[(k, x0)]], np.uint32),
                                      out=texture_out(i, tex.shape[0] * w))
                     outs[k][x0 * 4:x1 * 4] = o[y0 * w + x0 * 4:y0 * w + x1 * 4]
-                else:  # the first block row, whole (a rect cannot end on row 0)
-                    o = enc.compress(np.ascontiguousarray(tex[:4]), steps=steps, seed=ANNEAL_SEED)
+                else:
+                    # the first block row: the texture cut to that row and to
+                    # x1 (a rect cannot end on row 0; the blocks keep their
+                    # coordinates, which seed the annealing)
+                    head = np.ascontiguousarray(tex[:4, :x1])
+                    o = enc.compress(head, steps=steps, seed=ANNEAL_SEED, rect=(x0, 0, 0, 0),
+                                     state=np.array([0, prior[(k, x0)]], np.uint32))
                     outs[k][x0 * 4:x1 * 4] = o[x0 * 4:x1 * 4]
 
     t0 = time.perf_counter()
