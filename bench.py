@@ -298,7 +298,25 @@ def run_cpu_baseline(textures=None):
     return {"value": px / dt / 1e6, "unit": "MPix/s", "cores": cores, "kind": "port",
             "sample": f"every {BAND_STRIDE}th block row of the set: {len(bands)} rows, {px} texels, "
                       f"q50, one pass",
+            "host_cpus": host_cpus(),
             "qe_calls_per_block": calls / (px / 16), "qe_evaluations_per_block": evals / (px / 16)}, bands, outs
+
+
+def host_cpus() -> dict:
+    """What the host grants this process: CPUs in its affinity mask and the
+    cgroup CPU quota, if any (the CPU legs' speed depends on both)."""
+    info = {"cpu_count": os.cpu_count()}
+    try:
+        info["affinity"] = len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        pass
+    try:
+        with open("/sys/fs/cgroup/cpu.max") as f:
+            quota, period = f.read().split()[:2]
+        info["cgroup_cpus"] = None if quota == "max" else int(quota) / int(period)
+    except (OSError, ValueError):
+        pass
+    return info
 
 
 def reference_impl(args):
