@@ -350,7 +350,7 @@ def reference_impl(args):
                    "steps_q": STEPS_Q},
         "cpu_baseline": {"value": v, "unit": "MPix/s", "cores": cores, "kind": kind,
                          "sample": f"every {BAND_STRIDE}th block row of the set: {len(bands)} rows, "
-                                   f"{px} texels per step"},
+                                   f"{px} texels per step", "host_cpus": host_cpus()},
         "e2e": {"value": v, "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
