@@ -2035,10 +2035,20 @@ static double px_sse(const uint8_t *a, const uint8_t *b) {
   return s;
 }
 
+/* Each channel's squared difference goes into the running sum on its own,
+   in FasTC's order (Image.cpp:244-247), so the sum is FasTC's to the last
+   bit. */
 double bc7o_psnr(const uint8_t *a, const uint8_t *b, uint32_t w, uint32_t h) {
   double mse = 0.0;
   const size_t n = (size_t)w * h;
-  for (size_t i = 0; i < n; i++) mse += px_sse(a + 4 * i, b + 4 * i);
+  for (size_t i = 0; i < n; i++) {
+    const uint8_t *pa = a + 4 * i, *pb = b + 4 * i;
+    const double ra = pa[3] / 255.0, ua = pb[3] / 255.0;
+    for (int c = 0; c < 3; c++) {
+      const double d = ra * (double)pa[c] - ua * (double)pb[c];
+      mse += d * d;
+    }
+  }
   mse /= (double)w * (double)h;
   return 10.0 * log10((3.0 * 255.0 * 255.0) / mse);
 }

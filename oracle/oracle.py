@@ -2,9 +2,9 @@
 
 * :class:`Port` -- the C restatement (oracle/bc7_oracle.c), built by
   ``make -C oracle port`` into ``oracle/_build/libbc7_oracle.so``.
-* :class:`Reference` -- FasTC's own encoder compiled in place by
-  ``make -C oracle ref`` into ``oracle/_ref/libfastc_ref.so`` (only where the
-  FasTC checkout is present).
+* :class:`Reference` -- FasTC's own encoders, decoders, PSNR and KTX writer
+  compiled in place by ``make -C oracle ref`` into
+  ``oracle/_ref/libfastc_ref.so`` (only where the FasTC checkout is present).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
 this module.
@@ -298,6 +298,10 @@ class Reference:
         lib.ref_compress_stats.restype = C.c_size_t
         lib.ref_dxt_compress.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32, C.c_int]
         lib.ref_dxt_decompress.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32, C.c_int]
+        lib.ref_tc_psnr.argtypes = [_u8p, _u8p, C.c_uint32, C.c_uint32, C.c_int]
+        lib.ref_tc_psnr.restype = C.c_double
+        lib.ref_ktx.argtypes = [_u8p, C.c_uint32, C.c_uint32, C.c_int, _u8p, C.c_uint64]
+        lib.ref_ktx.restype = C.c_int64
         self.lib = lib
 
     def dxt_compress(self, img: np.ndarray, alpha: bool) -> np.ndarray:
@@ -383,6 +387,26 @@ class Reference:
         out = np.zeros((h, w, 4), dtype=np.uint8)
         self.lib.ref_decompress(_ptr(blocks), _ptr(out), w, h)
         return out
+
+    def tc_psnr(self, img: np.ndarray, blocks: np.ndarray, fmt: int = 7) -> float:
+        """The PSNR FasTC's tc prints for these blocks of img (format code
+        1 = DXT1, 5 = DXT5, 7 = BPTC), from FasTC's own CompressedImage
+        decoder and Image::ComputePSNR."""
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+        h, w = img.shape[:2]
+        return float(self.lib.ref_tc_psnr(_ptr(img), _ptr(blocks), w, h, fmt))
+
+    def ktx(self, blocks: np.ndarray, w: int, h: int, fmt: int = 7) -> bytes:
+        """The KTX file FasTC's ImageWriterKTX writes for these blocks. Its
+        image size is a function-local static, so only the first call per
+        format group in a process gives the file one tc run writes."""
+        blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+        out = np.zeros(len(blocks) + 4096, dtype=np.uint8)
+        n = self.lib.ref_ktx(_ptr(blocks), w, h, fmt, _ptr(out), out.size)
+        if n <= 0:
+            raise RuntimeError(f"ImageWriterKTX refused ({n})")
+        return out[:n].tobytes()
 
     def box_selection(self, px: np.ndarray, metric=0):
         px = np.ascontiguousarray(px, dtype=np.uint32)

@@ -81,6 +81,17 @@ DXT_DECODE = {
 }
 
 
+# The KTX files FasTC's tc writes (`-d out.ktx`) for fixture blocks: name ->
+# (blocks fixture, format code). ImageWriterKTX keeps the image size in a
+# function-local static, so each file is written by a fresh process, as by
+# one run of tc.
+KTX = {
+    "ktx_bptc_tile_q0": ("tile_q0", 7),
+    "ktx_dxt1_tile": ("dxt1_tile", 1),
+    "ktx_dxt5_tile": ("dxt5_tile", 5),
+}
+
+
 def dxt_random_blocks(w: int, h: int, fmt: int, seed: int) -> np.ndarray:
     n = ((w + 3) // 4) * ((h + 3) // 4) * (8 if fmt == 1 else 16)
     return np.random.default_rng(seed).integers(0, 256, n, dtype=np.uint8)
@@ -189,6 +200,42 @@ def make_dxt(ref, manifest):
         print(name)
 
 
+def _ktx_one(args):
+    """One KTX fixture, in a fresh worker process."""
+    name, blocks, w, h, fmt = args
+    return name, O.Reference().ktx(blocks, w, h, fmt)
+
+
+def make_tc(ref, manifest):
+    """What FasTC's tc prints and writes after the encode: its PSNR line for
+    every fixture with an image (Image::ComputePSNR over FasTC's decoder),
+    and the KTX files of KTX."""
+    import multiprocessing as mp
+
+    for group, fmt_of in (("cases", lambda e: 7), ("dxt", lambda e: e["format"])):
+        for name, e in manifest[group].items():
+            if "image" not in e:
+                continue
+            img = make(e["image"])
+            blocks = np.fromfile(os.path.join(HERE, name + ".bin"), np.uint8)
+            e["tc_psnr"] = ref.tc_psnr(img, blocks, fmt_of(e))
+            print(name, "tc PSNR", e["tc_psnr"])
+    work = []
+    for name, (src, fmt) in KTX.items():
+        e = manifest["cases" if fmt == 7 else "dxt"][src]
+        h, w = make(e["image"]).shape[:2]
+        work.append((name, np.fromfile(os.path.join(HERE, src + ".bin"), np.uint8), w, h, fmt))
+    with mp.get_context("spawn").Pool(1, maxtasksperchild=1) as pool:
+        files = dict(pool.map(_ktx_one, work, chunksize=1))
+    manifest["ktx"] = {}
+    for (name, _, w, h, fmt), (src, _) in zip(work, KTX.values()):
+        raw = files[name]
+        manifest["ktx"][name] = {"blocks": src, "format": fmt, "width": w, "height": h,
+                                 "bytes": len(raw), "header_hex": raw[:96].hex(),
+                                 "sha256": hashlib.sha256(raw).hexdigest()}
+        print(name, len(raw), "bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=O.DEFAULT_REFERENCE)
@@ -198,18 +245,23 @@ def main():
                     help="only (re)write the full-size PSNR / per-block SSE fixtures")
     ap.add_argument("--dxt-only", action="store_true",
                     help="only (re)write the DXT1 / DXT5 fixtures")
+    ap.add_argument("--tc-only", action="store_true",
+                    help="only (re)write tc's PSNR values and the KTX fixtures")
     ap.add_argument("--workers", type=int, default=6)
     args = ap.parse_args()
     if not O.build_ref(args.reference):
         sys.exit("FasTC checkout not found; cannot regenerate fixtures")
     ref = O.Reference()
-    if args.stats_only or args.full_size_only or args.dxt_only:
+    if args.stats_only or args.full_size_only or args.dxt_only or args.tc_only:
         with open(os.path.join(HERE, "manifest.json")) as f:
             manifest = json.load(f)
         if args.stats_only:
             make_stats(ref, manifest)
         elif args.dxt_only:
             make_dxt(ref, manifest)
+            make_tc(ref, manifest)
+        elif args.tc_only:
+            make_tc(ref, manifest)
         else:
             make_full_size(manifest, args.workers)
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
@@ -247,6 +299,7 @@ def main():
     np.savez(os.path.join(HERE, "endpoint_tables.npz"), opt7=o7, opt6=o6)
     make_stats(ref, manifest)
     make_dxt(ref, manifest)
+    make_tc(ref, manifest)
     make_full_size(manifest, args.workers)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)

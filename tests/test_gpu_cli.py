@@ -1,5 +1,7 @@
 """The tc-compatible command line on the GPU: PNG in, KTX out, the blocks
 those of the library call, PSNR printed as FasTC's tc prints it."""
+import hashlib
+
 import numpy as np
 import pytest
 
@@ -22,6 +24,27 @@ def test_tc_png_to_ktx(gpu, tmp_path, capsys):
     assert (w, h) == (40, 24) and np.array_equal(blocks, want)
     line = [l for l in capsys.readouterr().out.splitlines() if l.startswith("PSNR: ")]
     assert line and float(line[0].split()[1]) > 20.0
+
+
+@pytest.mark.parametrize("fmt,ktx", [("BPTC", "ktx_bptc_tile_q0"), ("DXT1", "ktx_dxt1_tile"),
+                                     ("DXT5", "ktx_dxt5_tile")])
+def test_tc_writes_fasTC_file_and_psnr_line(gpu, manifest, tmp_path, capsys, fmt, ktx):
+    """`tc -q 0 -f FMT -d out.ktx` on a fixture image writes the very file
+    FasTC's tc writes (its blocks, through its ImageWriterKTX) and prints
+    FasTC's PSNR line (its Image::ComputePSNR of its decoder's texels)."""
+    from fastc_gb300 import imageio, tc
+
+    e = manifest["ktx"][ktx]
+    src_case = manifest["cases" if fmt == "BPTC" else "dxt"][e["blocks"]]
+    img = make_image(src_case["image"])
+    src = tmp_path / "fixture.png"
+    src.write_bytes(imageio.png_bytes(img))
+    out = tmp_path / "out.ktx"
+    assert tc.main(["-q", "0", "-f", fmt, "-d", str(out), str(src)]) == 0
+    raw = out.read_bytes()
+    assert len(raw) == e["bytes"] and hashlib.sha256(raw).hexdigest() == e["sha256"]
+    line = [l for l in capsys.readouterr().out.splitlines() if l.startswith("PSNR: ")]
+    assert line == [f"PSNR: {src_case['tc_psnr']:.3f}"]
 
 
 def test_tc_pads_odd_sizes_and_writes_decoded_png(gpu, tmp_path):
