@@ -332,7 +332,6 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
     dj[i].out = dout + out_off[i];
     dj[i].flags |= fastc::kJobIn16 | fastc::kJobOut16;
   }
-  CK(cudaMemcpyAsync(g_host.jobs.p, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs));
   // Texels go up on the copy stream in job order, chunk by chunk of the
   // pipeline, so that chunk k starts once its own jobs are in while later
   // ones are still copying; blocks come back the same way as each chunk is
@@ -345,58 +344,69 @@ fastc_bc7_status run_host(const fastc_bc7_job *jobs, uint32_t n, const fastc_bc7
                                : total;
   const size_t nchunk = (size_t)((total + cap - 1) / cap);
   CK(ensure_chunk_events(nchunk));
-  auto copy_in = [&](uint32_t i) -> cudaError_t {
-    if (!dj[i].nblocks) return cudaSuccess;
-    const uint8_t *src = jobs[i].in + (size_t)dj[i].row0 * jobs[i].width * 4;
-    return cudaMemcpyAsync(din + in_off[i], src, in_bytes[i], cudaMemcpyHostToDevice, g_host.copy);
-  };
-  auto copy_out = [&](uint32_t i) -> cudaError_t {
-    if (!dj[i].nblocks) return cudaSuccess;
-    return cudaMemcpyAsync(jobs[i].out + (size_t)dj[i].first * 16, dout + out_off[i],
-                           (size_t)dj[i].nblocks * 16, cudaMemcpyDeviceToHost, g_host.copy);
-  };
-  {
-    uint32_t next = 0;
-    for (size_t k = 0; k < nchunk; k++) {
-      const uint64_t end = (k + 1) * cap;
-      while (next < n && dj[next].begin < end) CK(copy_in(next++));
-      CK(cudaEventRecord(g_host.in_ev[k], g_host.copy));
-    }
-  }
-  if (!chunked) CK(cudaStreamWaitEvent(cs, g_host.in_ev[nchunk - 1], 0));
-  const EncodeScratch sc = carve_scratch(g_host.scratch.p, total);
-  fastc_bc7_block_stats *dstats =
-      static_cast<fastc_bc7_block_stats *>(stats ? g_host.stats.p : nullptr);
-  fastc::ChunkEvents ev;
-  ev.in_ready = g_host.in_ev.data();
-  ev.packed = g_host.out_ev.data();
-  ev.count = (int)nchunk;
-  const int le = launch_engine(static_cast<const JobDev *>(g_host.jobs.p), (int)n, total,
-                               g_host.scratch.p, engine, pick_shape(total), tb, g_host.cls,
-                               fastc::PipelineTuning{}, cs, dstats, chunked ? &ev : nullptr);
-  if (le) return fail_cuda((cudaError_t)le);
-  if (chunked) {
-    uint32_t next = 0;
-    for (size_t k = 0; k < nchunk; k++) {
-      const uint64_t end = k + 1 == nchunk ? total : (k + 1) * cap;
-      CK(cudaStreamWaitEvent(g_host.copy, g_host.out_ev[k], 0));
-      while (next < n && dj[next].begin + dj[next].nblocks <= end) CK(copy_out(next++));
-    }
-  } else {
-    CK(cudaEventRecord(g_host.out_ev[0], cs));
-    CK(cudaStreamWaitEvent(g_host.copy, g_host.out_ev[0], 0));
-    for (uint32_t i = 0; i < n; i++) CK(copy_out(i));
-  }
-  CK(cudaEventRecord(g_host.copied, g_host.copy));
-  CK(cudaStreamWaitEvent(cs, g_host.copied, 0));
-  if (stats)
-    CK(cudaMemcpyAsync(stats, dstats, total * sizeof(fastc_bc7_block_stats),
-                       cudaMemcpyDeviceToHost, cs));
   uint32_t singles = 0, status = 0;
-  if (any_continue)
-    CK(cudaMemcpyAsync(&singles, sc.singles, sizeof(singles), cudaMemcpyDeviceToHost, cs));
-  CK(cudaMemcpyAsync(&status, sc.status, sizeof(status), cudaMemcpyDeviceToHost, cs));
-  CK(cudaStreamSynchronize(cs));
+  // Everything the call enqueues on its two streams. Both are drained
+  // afterwards, also after an error, so that no copy of the call still
+  // touches the caller's buffers once it has returned.
+  auto enqueue = [&]() -> cudaError_t {
+    CK_RT(cudaMemcpyAsync(g_host.jobs.p, dj.data(), n * sizeof(JobDev), cudaMemcpyHostToDevice, cs));
+    auto copy_in = [&](uint32_t i) -> cudaError_t {
+      if (!dj[i].nblocks) return cudaSuccess;
+      const uint8_t *src = jobs[i].in + (size_t)dj[i].row0 * jobs[i].width * 4;
+      return cudaMemcpyAsync(din + in_off[i], src, in_bytes[i], cudaMemcpyHostToDevice, g_host.copy);
+    };
+    auto copy_out = [&](uint32_t i) -> cudaError_t {
+      if (!dj[i].nblocks) return cudaSuccess;
+      return cudaMemcpyAsync(jobs[i].out + (size_t)dj[i].first * 16, dout + out_off[i],
+                             (size_t)dj[i].nblocks * 16, cudaMemcpyDeviceToHost, g_host.copy);
+    };
+    {
+      uint32_t next = 0;
+      for (size_t k = 0; k < nchunk; k++) {
+        const uint64_t end = (k + 1) * cap;
+        while (next < n && dj[next].begin < end) CK_RT(copy_in(next++));
+        CK_RT(cudaEventRecord(g_host.in_ev[k], g_host.copy));
+      }
+    }
+    if (!chunked) CK_RT(cudaStreamWaitEvent(cs, g_host.in_ev[nchunk - 1], 0));
+    const EncodeScratch sc = carve_scratch(g_host.scratch.p, total);
+    fastc_bc7_block_stats *dstats =
+        static_cast<fastc_bc7_block_stats *>(stats ? g_host.stats.p : nullptr);
+    fastc::ChunkEvents ev;
+    ev.in_ready = g_host.in_ev.data();
+    ev.packed = g_host.out_ev.data();
+    ev.count = (int)nchunk;
+    const int le = launch_engine(static_cast<const JobDev *>(g_host.jobs.p), (int)n, total,
+                                 g_host.scratch.p, engine, pick_shape(total), tb, g_host.cls,
+                                 fastc::PipelineTuning{}, cs, dstats, chunked ? &ev : nullptr);
+    CK_RT((cudaError_t)le);
+    if (chunked) {
+      uint32_t next = 0;
+      for (size_t k = 0; k < nchunk; k++) {
+        const uint64_t end = k + 1 == nchunk ? total : (k + 1) * cap;
+        CK_RT(cudaStreamWaitEvent(g_host.copy, g_host.out_ev[k], 0));
+        while (next < n && dj[next].begin + dj[next].nblocks <= end) CK_RT(copy_out(next++));
+      }
+    } else {
+      CK_RT(cudaEventRecord(g_host.out_ev[0], cs));
+      CK_RT(cudaStreamWaitEvent(g_host.copy, g_host.out_ev[0], 0));
+      for (uint32_t i = 0; i < n; i++) CK_RT(copy_out(i));
+    }
+    CK_RT(cudaEventRecord(g_host.copied, g_host.copy));
+    CK_RT(cudaStreamWaitEvent(cs, g_host.copied, 0));
+    if (stats)
+      CK_RT(cudaMemcpyAsync(stats, dstats, total * sizeof(fastc_bc7_block_stats),
+                            cudaMemcpyDeviceToHost, cs));
+    if (any_continue)
+      CK_RT(cudaMemcpyAsync(&singles, sc.singles, sizeof(singles), cudaMemcpyDeviceToHost, cs));
+    CK_RT(cudaMemcpyAsync(&status, sc.status, sizeof(status), cudaMemcpyDeviceToHost, cs));
+    return cudaSuccess;
+  };
+  cudaError_t e = enqueue();
+  const cudaError_t se_copy = cudaStreamSynchronize(g_host.copy);
+  const cudaError_t se_comp = cudaStreamSynchronize(cs);
+  if (e == cudaSuccess) e = se_copy != cudaSuccess ? se_copy : se_comp;
+  if (e != cudaSuccess) return fail_cuda(e);
   if (status & 2u) {  // the task-overflow status bit (bc7_block.cuh)
     // a block needed more cluster fits than the scratch was sized for; its
     // bytes are not FasTC's (never expected: the bound is computed above)
@@ -614,13 +624,15 @@ fastc_bc7_status fastc_bc7_decompress(const uint8_t *blocks, uint8_t *rgba, uint
   CK(g_host.in.ensure(nb * 16));
   CK(g_host.out.ensure(img));
   cudaStream_t cs = g_host.stream;
-  CK(cudaMemcpyAsync(g_host.in.p, blocks, nb * 16, cudaMemcpyHostToDevice, cs));
-  const int le = fastc::launch_decode(static_cast<const uint8_t *>(g_host.in.p),
-                                      static_cast<uint8_t *>(g_host.out.p), width, height, spec, cs);
-  if (le) return fail_cuda((cudaError_t)le);
-  CK(cudaMemcpyAsync(rgba, g_host.out.p, img, cudaMemcpyDeviceToHost, cs));
-  CK(cudaStreamSynchronize(cs));
-  return FASTC_BC7_OK;
+  cudaError_t e = cudaMemcpyAsync(g_host.in.p, blocks, nb * 16, cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess)
+    e = (cudaError_t)fastc::launch_decode(static_cast<const uint8_t *>(g_host.in.p),
+                                          static_cast<uint8_t *>(g_host.out.p), width, height, spec, cs);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rgba, g_host.out.p, img, cudaMemcpyDeviceToHost, cs);
+  // drained also after an error: no copy of the call outlives it
+  const cudaError_t se = cudaStreamSynchronize(cs);
+  if (e == cudaSuccess) e = se;
+  return e == cudaSuccess ? FASTC_BC7_OK : fail_cuda(e);
 }
 
 fastc_bc7_status fastc_bc7_block_error_device(const uint8_t *blocks, const uint8_t *rgba,
@@ -647,15 +659,18 @@ fastc_bc7_status fastc_bc7_psnr(const uint8_t *blocks, const uint8_t *rgba, uint
   uint8_t *dimg = static_cast<uint8_t *>(g_host.in.p);
   uint8_t *dblk = dimg + img;  // byte loads only, so no alignment is needed
   double *dsse = static_cast<double *>(g_host.out.p);
-  CK(cudaMemcpyAsync(dimg, rgba, img, cudaMemcpyHostToDevice, cs));
-  CK(cudaMemcpyAsync(dblk, blocks, nb * 16, cudaMemcpyHostToDevice, cs));
-  const int le = fastc::launch_block_error(dblk, dimg, width, height, dsse + 1, dsse, cs);
-  if (le) return fail_cuda((cudaError_t)le);
   double total = 0.0;
-  CK(cudaMemcpyAsync(&total, dsse, sizeof(double), cudaMemcpyDeviceToHost, cs));
-  if (block_sse)
-    CK(cudaMemcpyAsync(block_sse, dsse + 1, nb * sizeof(double), cudaMemcpyDeviceToHost, cs));
-  CK(cudaStreamSynchronize(cs));
+  cudaError_t e = cudaMemcpyAsync(dimg, rgba, img, cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dblk, blocks, nb * 16, cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess)
+    e = (cudaError_t)fastc::launch_block_error(dblk, dimg, width, height, dsse + 1, dsse, cs);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&total, dsse, sizeof(double), cudaMemcpyDeviceToHost, cs);
+  if (e == cudaSuccess && block_sse)
+    e = cudaMemcpyAsync(block_sse, dsse + 1, nb * sizeof(double), cudaMemcpyDeviceToHost, cs);
+  // drained also after an error: no copy of the call outlives it
+  const cudaError_t se = cudaStreamSynchronize(cs);
+  if (e == cudaSuccess) e = se;
+  if (e != cudaSuccess) return fail_cuda(e);
   if (psnr) *psnr = 10.0 * std::log10((3.0 * 255.0 * 255.0) / (total / ((double)width * height)));
   return FASTC_BC7_OK;
 }

@@ -31,6 +31,14 @@ fastc_bc7_status fail_cuda(cudaError_t e);
     if (e_ != cudaSuccess) return ::fastc::host::fail_cuda(e_); \
   } while (0)
 
+// The same inside a helper that returns the cudaError_t itself (a sequence
+// of enqueues whose caller drains the streams before it reports).
+#define CK_RT(expr)                          \
+  do {                                       \
+    const cudaError_t e_ = (expr);           \
+    if (e_ != cudaSuccess) return e_;        \
+  } while (0)
+
 bool settings_ok(const fastc_bc7_settings &s, fastc_bc7_status *why);
 // Raster block range of a job (FasTC's BPTCC::Compress walk), or false.
 bool job_range(const fastc_bc7_job &j, uint32_t *first, uint32_t *count);

@@ -206,6 +206,9 @@ void fastc_bc7_server_s::launch(Slot &s) {
     if (e != cudaSuccess) delete arg;
   }
   if (e != cudaSuccess) {
+    // drain what was enqueued before the error: no upload may still read a
+    // request's texels once the request is reported failed
+    cudaStreamSynchronize(s.stream);
     std::lock_guard<std::mutex> lk(mu);
     s.error = e;
     s.finished = true;

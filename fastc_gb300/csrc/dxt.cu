@@ -815,14 +815,18 @@ fastc_bc7_status fastc_dxt_psnr(const uint8_t *blocks, const uint8_t *rgba, uint
   CK(fastc::ensure(&h.out, &h.out_cap, (nb + 1) * sizeof(double)));
   uint8_t *dimg = static_cast<uint8_t *>(h.in), *dblk = dimg + img;
   double *dsse = static_cast<double *>(h.out);
-  CK(cudaMemcpyAsync(dimg, rgba, img, cudaMemcpyHostToDevice, h.comp));
-  CK(cudaMemcpyAsync(dblk, blocks, nb * bsz, cudaMemcpyHostToDevice, h.comp));
-  CK(fastc::launch_dxt_error(dblk, dimg, width, height, format == FASTC_DXT5, dsse + 1, dsse, h.comp));
   double total = 0.0;
-  CK(cudaMemcpyAsync(&total, dsse, sizeof(double), cudaMemcpyDeviceToHost, h.comp));
-  if (block_sse)
-    CK(cudaMemcpyAsync(block_sse, dsse + 1, nb * sizeof(double), cudaMemcpyDeviceToHost, h.comp));
-  CK(cudaStreamSynchronize(h.comp));
+  cudaError_t e = cudaMemcpyAsync(dimg, rgba, img, cudaMemcpyHostToDevice, h.comp);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dblk, blocks, nb * bsz, cudaMemcpyHostToDevice, h.comp);
+  if (e == cudaSuccess)
+    e = fastc::launch_dxt_error(dblk, dimg, width, height, format == FASTC_DXT5, dsse + 1, dsse, h.comp);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&total, dsse, sizeof(double), cudaMemcpyDeviceToHost, h.comp);
+  if (e == cudaSuccess && block_sse)
+    e = cudaMemcpyAsync(block_sse, dsse + 1, nb * sizeof(double), cudaMemcpyDeviceToHost, h.comp);
+  // drained also after an error: no copy of the call outlives it
+  const cudaError_t se = cudaStreamSynchronize(h.comp);
+  if (e == cudaSuccess) e = se;
+  if (e != cudaSuccess) return fail_cuda(e);
   if (psnr) *psnr = 10.0 * std::log10((3.0 * 255.0 * 255.0) / (total / ((double)width * height)));
   return FASTC_BC7_OK;
 }
@@ -858,18 +862,20 @@ fastc_bc7_status fastc_dxt_decompress(const uint8_t *blocks, uint8_t *rgba, uint
   fastc::DxtHostContext &h = fastc::g_dxt_host;
   CK(fastc::ensure(&h.in, &h.in_cap, nb * bsz));
   CK(fastc::ensure(&h.out, &h.out_cap, img));
-  CK(cudaMemcpyAsync(h.in, blocks, nb * bsz, cudaMemcpyHostToDevice, h.comp));
-  const unsigned grid = (unsigned)((nb + 127) / 128);
-  if (format == FASTC_DXT5)
-    fastc::dxt_decode_kernel<true><<<grid, 128, 0, h.comp>>>(static_cast<const uint8_t *>(h.in),
-                                                               static_cast<uint8_t *>(h.out), width, height);
-  else
-    fastc::dxt_decode_kernel<false><<<grid, 128, 0, h.comp>>>(static_cast<const uint8_t *>(h.in),
-                                                                static_cast<uint8_t *>(h.out), width, height);
-  CK(cudaPeekAtLastError());
-  CK(cudaMemcpyAsync(rgba, h.out, img, cudaMemcpyDeviceToHost, h.comp));
-  CK(cudaStreamSynchronize(h.comp));
-  return FASTC_BC7_OK;
+  cudaError_t e = cudaMemcpyAsync(h.in, blocks, nb * bsz, cudaMemcpyHostToDevice, h.comp);
+  if (e == cudaSuccess) {
+    const unsigned grid = (unsigned)((nb + 127) / 128);
+    const uint8_t *din = static_cast<const uint8_t *>(h.in);
+    uint8_t *dout = static_cast<uint8_t *>(h.out);
+    if (format == FASTC_DXT5) fastc::dxt_decode_kernel<true><<<grid, 128, 0, h.comp>>>(din, dout, width, height);
+    else fastc::dxt_decode_kernel<false><<<grid, 128, 0, h.comp>>>(din, dout, width, height);
+    e = cudaPeekAtLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rgba, h.out, img, cudaMemcpyDeviceToHost, h.comp);
+  // drained also after an error: no copy of the call outlives it
+  const cudaError_t se = cudaStreamSynchronize(h.comp);
+  if (e == cudaSuccess) e = se;
+  return e == cudaSuccess ? FASTC_BC7_OK : fail_cuda(e);
 }
 
 }  // extern "C"
