@@ -1,6 +1,7 @@
 """Image files for the command-line tool: PNG (8-bit RGB/RGBA/grey, no
-interlace) read and written with zlib, raw RGBA8, numpy arrays, and the KTX
-container FasTC writes for compressed images (BPTC, DXT1, DXT5).
+interlace) read and written with zlib, TGA read as FasTC's loader reads it,
+raw RGBA8, numpy arrays, and the KTX container FasTC writes for compressed
+images (BPTC, DXT1, DXT5).
 
 The KTX layout follows FasTC's ImageWriterKTX (IO/src/ImageWriterKTX.cpp:
 the 12-byte identifier, thirteen little-endian words, one key/value pair
@@ -144,14 +145,98 @@ def png_bytes(rgba: np.ndarray) -> bytes:
             chunk(b"IDAT", zlib.compress(rows.tobytes(), 6)) + chunk(b"IEND", b""))
 
 
+def read_tga(raw: bytes) -> np.ndarray:
+    """RGBA8 (h, w, 4) from a TGA file, read as FasTC's loader reads it
+    (ImageLoaderTGA::ReadData, IO/src/ImageLoaderTGA.cpp:35-48, over
+    targa_loadFromData, IO/third_party/tga/targa.c:262-571):
+
+    * no colour maps; image types 0, 1 and 9 are refused, types 2 and 3 are
+      read as uncompressed BGR(A) (type 3 too), every other type as
+      run-length packets (targa.c:323-329, 436, 480);
+    * 24- and 32-bit texels (alpha 255 at 24 bits), and 16-bit texels in
+      uncompressed files only, red from the low five bits and blue from the
+      high five, each shifted up by three, alpha 255 (targa.c:387-399,
+      453-458); 8-bit files are refused;
+    * the image descriptor is ignored: the rows are always taken bottom-up
+      (ImageLoader::LoadFromPixelBuffer with flipY, IO/src/ImageLoader.cpp:
+      122-149).
+
+    Truncated files raise ValueError (FasTC refuses them too, apart from
+    reading a few bytes past the end of a run-length file)."""
+    if len(raw) < 18:
+        raise ValueError("TGA: file shorter than its header")
+    id_len, cmap, itype = raw[0], raw[1], raw[2]
+    if cmap != 0:
+        raise ValueError("TGA: colour-mapped files are not supported")
+    if itype in (0, 1, 9):
+        raise ValueError(f"TGA: unsupported image type {itype}")
+    w, h = struct.unpack("<hh", raw[12:16])
+    if w < 1 or h < 1:
+        raise ValueError(f"TGA: invalid size {w}x{h}")
+    depth = raw[16]
+    if depth not in (16, 24, 32):
+        raise ValueError(f"TGA: unsupported pixel depth of {depth} bits")
+    rle = itype not in (2, 3)
+    if depth == 16 and rle:
+        raise ValueError("TGA: run-length files of 16-bit texels are not supported")
+    pos = 18 + id_len
+    if pos > len(raw):
+        raise ValueError("TGA: truncated image ID")
+    n = w * h
+    out = np.empty((n, 4), dtype=np.uint8)
+    if not rle:
+        cm = 2 if depth == 16 else depth // 8
+        if pos + n * cm > len(raw):
+            raise ValueError("TGA: truncated pixel data")
+        if depth == 16:
+            v = np.frombuffer(raw, dtype="<u2", count=n, offset=pos)
+            out[:, 0] = (v & 31) << 3
+            out[:, 1] = ((v >> 5) & 31) << 3
+            out[:, 2] = ((v >> 10) & 31) << 3
+            out[:, 3] = 255
+        else:
+            px = np.frombuffer(raw, dtype=np.uint8, count=n * cm, offset=pos).reshape(n, cm)
+            out[:, :3] = px[:, 2::-1]
+            out[:, 3] = px[:, 3] if cm == 4 else 255
+    else:
+        cm = depth // 8
+        buf = np.frombuffer(raw, dtype=np.uint8)
+        k = 0
+        while k < n:
+            if pos >= len(raw):
+                raise ValueError("TGA: truncated run-length data")
+            hdr = raw[pos]
+            pos += 1
+            if hdr < 128:  # a packet of hdr + 1 literal texels
+                cnt = min(hdr + 1, n - k)
+                if pos + cnt * cm > len(raw):
+                    raise ValueError("TGA: truncated run-length data")
+                px = buf[pos:pos + cnt * cm].reshape(cnt, cm)
+                pos += (hdr + 1) * cm
+            else:  # a run of hdr - 127 copies of one texel
+                cnt = min(hdr - 127, n - k)
+                if pos + cm > len(raw):
+                    raise ValueError("TGA: truncated run-length data")
+                px = np.broadcast_to(buf[pos:pos + cm], (cnt, cm))
+                pos += cm
+            out[k:k + cnt, :3] = px[:, 2::-1]
+            out[k:k + cnt, 3] = px[:, 3] if cm == 4 else 255
+            k += cnt
+    return np.ascontiguousarray(out.reshape(h, w, 4)[::-1])
+
+
 def load_image(path: str, width: int = 0, height: int = 0) -> np.ndarray:
-    """RGBA8 (h, w, 4) from .png, .npy or raw RGBA (.rgba, needs width/height)."""
+    """RGBA8 (h, w, 4) from .png, .tga, .npy or raw RGBA (.rgba, needs
+    width/height)."""
     if path.endswith(".npy"):
         img = np.load(path)
     elif path.endswith(".rgba") or path.endswith(".raw"):
         if not (width and height):
             raise ValueError("raw RGBA input needs its size (-s WxH)")
         img = np.fromfile(path, dtype=np.uint8).reshape(height, width, 4)
+    elif path.endswith(".tga"):
+        with open(path, "rb") as f:
+            img = read_tga(f.read())
     else:
         with open(path, "rb") as f:
             img = read_png(f.read())

@@ -7,7 +7,8 @@ Mirrors FasTC's CLTool (CLTool/src/tc.cpp): BPTC at quality -q (annealing
 steps, default 50) or, with -f, DXT1 / DXT5 (quality has no effect, as in
 FasTC), the image zero-padded to whole blocks, "PSNR: %.3f"
 computed as FasTC's Image::ComputePSNR (alpha-premultiplied RGB, peak
-3*255^2) on the decoded blocks, and the output written to -d (or
+3*255^2) on the decoded blocks (for a padded image, FasTC's message that
+the sizes differ instead), and the output written to -d (or
 <basename>-bptc.png, -dxt1.png, -dxt5.png): a .ktx name stores the
 compressed blocks in FasTC's KTX layout, a .png name the decoded image. -nd writes nothing; -n N repeats the
 compression and reports the time. Options that choose host threading (-t,
@@ -15,7 +16,8 @@ compression and reports the time. Options that choose host threading (-t,
 the GPU. -l runs CompressWithStats with a log stream and writes FasTC's
 per-block log to <basename>.log (for DXT the log stays empty, as FasTC's
 does: it has no logging DXT encoder); ETC1 and PVRTC are refused.
-Inputs: PNG (8-bit), .npy RGBA8 arrays, raw RGBA (.rgba/.raw with -s WxH).
+Inputs: PNG (8-bit), TGA (as FasTC's loader reads it), .npy RGBA8 arrays, raw
+RGBA (.rgba/.raw with -s WxH).
 """
 from __future__ import annotations
 
@@ -87,8 +89,13 @@ def main(argv=None) -> int:
     from .bptc import (CompressionFormat, CompressionJob, CompressionSettings, compress, compress_with_stats,
                        decompress, psnr)
 
-    img = imageio.pad_to_blocks(imageio.load_image(path, width, height))
+    src = imageio.load_image(path, width, height)
+    img = imageio.pad_to_blocks(src)
     h, w = img.shape[:2]
+    padded = img.shape != src.shape
+    if padded:  # CompressImage's warning (Core/src/TexComp.cpp:157-158, 383)
+        print("TexComp -- WARNING - Image size is not a multiple of block size. Padding with zeros...",
+              file=sys.stderr)
     cf = CompressionFormat[fmt]
     blocks = np.zeros(w * h // (2 if cf == CompressionFormat.DXT1 else 1), dtype=np.uint8)
     settings = CompressionSettings(num_simulated_annealing_steps=quality)
@@ -108,11 +115,17 @@ def main(argv=None) -> int:
     if save_log:
         with open(basename(path) + ".log", "w") as f:
             f.write("".join(logs))
-    if cf == CompressionFormat.BPTC:
-        db = psnr(blocks, img, w, h)
+    if padded:
+        # the compressed image has the padded size, so tc compares nothing
+        # (CLTool/src/tc.cpp:297-299)
+        print("Cannot compute image metrics: compressed and uncompressed dimensions differ.",
+              file=sys.stderr)
     else:
-        db = dxt.psnr(blocks, img, w, h, cf)
-    print(f"PSNR: {db:.3f}")
+        if cf == CompressionFormat.BPTC:
+            db = psnr(blocks, img, w, h)
+        else:
+            db = dxt.psnr(blocks, img, w, h, cf)
+        print(f"PSNR: {db:.3f}")
     if write_out:
         if not out_name:
             out_name = basename(path) + ("-bptc.png" if cf == CompressionFormat.BPTC else f"-{fmt.lower()}.png")

@@ -12,6 +12,10 @@
 //   * ref_ktx     -> the KTX file tc writes for `-d out.ktx`
 //                    (CLTool/src/tc.cpp:336-337 -> IO/src/ImageFile.cpp:132-160
 //                    -> ImageWriterKTX::WriteImage, IO/src/ImageWriterKTX.cpp:69-161)
+//   * ref_load_tga -> the texels tc compresses for a .tga input
+//                    (ImageLoaderTGA::ReadData, IO/src/ImageLoaderTGA.cpp:35-48,
+//                    over IO/third_party/tga/targa.c, then ImageLoader::LoadImage,
+//                    IO/src/ImageLoader.cpp:151-215)
 //
 // ImageWriterKTX keeps the image size in a function-local static
 // (ImageWriterKTX.cpp:143,149,153), so only the first file a process writes per
@@ -29,9 +33,11 @@
 
 #include "FasTC/CompressedImage.h"
 #include "FasTC/Image.h"
+#include "FasTC/Pixel.h"
 #include "FasTC/ASTCCompressor.h"
 #include "FasTC/ETCCompressor.h"
 #include "FasTC/PVRTCCompressor.h"
+#include "ImageLoaderTGA.h"
 #include "ImageWriterKTX.h"
 
 namespace {
@@ -73,6 +79,26 @@ int64_t ref_ktx(const uint8_t *blocks, uint32_t w, uint32_t h, int format,
   if (n > cap) return -static_cast<int64_t>(n);
   memcpy(out, writer.GetRawFileData(), n);
   return static_cast<int64_t>(n);
+}
+
+// Loads a TGA file with FasTC's loader: returns the texel count with *w, *h
+// set (RGBA8 texels written to out when cap holds them), or 0 when the
+// loader refuses the file.
+int64_t ref_load_tga(const uint8_t *data, int32_t n, uint8_t *out, uint64_t cap, uint32_t *w,
+                     uint32_t *h) {
+  ImageLoaderTGA loader(data, n);
+  FasTC::Image<> *img = loader.LoadImage();
+  if (!img) return 0;
+  *w = img->GetWidth();
+  *h = img->GetHeight();
+  const uint64_t texels = (uint64_t)*w * *h;
+  if (4 * texels <= cap)
+    for (uint64_t i = 0; i < texels; i++) {
+      const uint32 p = img->GetPixels()[i].Pack();
+      memcpy(out + 4 * i, &p, 4);
+    }
+  delete img;
+  return static_cast<int64_t>(texels);
 }
 
 }  // extern "C"

@@ -15,6 +15,7 @@ import argparse
 import hashlib
 import json
 import os
+import struct
 import sys
 
 import numpy as np
@@ -90,6 +91,105 @@ KTX = {
     "ktx_dxt1_tile": ("dxt1_tile", 1),
     "ktx_dxt5_tile": ("dxt5_tile", 5),
 }
+
+
+# TGA inputs as FasTC's tc loads them (ImageLoaderTGA over the vendored
+# targa reader): name -> (image, depth, image type, image ID, descriptor
+# byte). The files are written here (rows bottom-up, run-length packets where
+# the type asks for them) and FasTC's decoded texels recorded; the ones marked
+# None are files FasTC refuses (a colour map, 8-bit texels, run-length 16-bit
+# texels, image type 1, truncated texels).
+TGA = {
+    "tga32_raw": ("tile_mix_radial_alpha(6, 24, 20, 5, 3)[:17, :23]", 32, 2, b"fastc", 0x28),
+    "tga24_raw": ("tile_mix(7, 20, 12)", 24, 2, b"", 0x00),
+    "tga32_rle": ("flat_blocks(8, 40, 24)", 32, 10, b"", 0x08),
+    "tga24_rle": ("tile_mix(9, 40, 12)[:9, :37]", 24, 10, b"id", 0x20),
+    "tga32_bw_rle": ("flat_blocks(10, 16, 12)", 32, 11, b"", 0x08),
+    "tga24_bw": ("tile_mix(11, 12, 8)", 24, 3, b"", 0x00),
+    "tga16_raw": ("rng16(12, 16, 8)", 16, 2, b"", 0x00),
+}
+TGA_REFUSED = ["tga_colormap", "tga8_bw", "tga16_rle", "tga_type1", "tga32_truncated"]
+
+
+def tga_file(img: np.ndarray, depth: int, itype: int, ident: bytes = b"", desc: int = 0) -> bytes:
+    """A TGA file of img (RGBA8, or 16-bit words for depth 16), rows stored
+    bottom-up; types 9-11 as run-length packets (runs of 2-128 equal texels,
+    literal packets of up to 128)."""
+    h, w = img.shape[:2]
+    head = struct.pack("<BBBHHBHHHHBB", len(ident), 0, itype, 0, 0, 0, 0, 0, w, h, depth, desc)
+    rows = img[::-1].reshape(h * w, -1)
+    if depth == 16:
+        texels = [int(v).to_bytes(2, "little") for v in rows[:, 0]]
+    else:
+        cm = depth // 8
+        texels = [bytes(p[[2, 1, 0, 3][:cm]]) for p in rows]
+    if itype in (2, 3):
+        return head + ident + b"".join(texels)
+    out, k = bytearray(), 0
+    while k < len(texels):
+        run = 1
+        while k + run < len(texels) and run < 128 and texels[k + run] == texels[k]:
+            run += 1
+        if run >= 2:
+            out += bytes([127 + run]) + texels[k]
+            k += run
+            continue
+        lit = 1
+        while (k + lit < len(texels) and lit < 128 and
+               not (k + lit + 1 < len(texels) and texels[k + lit] == texels[k + lit + 1])):
+            lit += 1
+        out += bytes([lit - 1]) + b"".join(texels[k:k + lit])
+        k += lit
+    return head + ident + bytes(out)
+
+
+def tga_refused(name: str) -> bytes:
+    img = make("tile_mix(13, 8, 8)")
+    raw = bytearray(tga_file(img, 32, 2))
+    if name == "tga_colormap":
+        raw[1] = 1
+    elif name == "tga8_bw":
+        raw = bytearray(tga_file(img, 32, 3))
+        raw[16] = 8
+    elif name == "tga16_rle":
+        raw = bytearray(tga_file(np.zeros((8, 8, 1), np.uint16), 16, 10))
+    elif name == "tga_type1":
+        raw[2] = 1
+    elif name == "tga32_truncated":
+        raw = raw[:-5]
+    return bytes(raw)
+
+
+def rng16(seed: int, w: int, h: int) -> np.ndarray:
+    """Random 16-bit texel words (h, w, 1)."""
+    return np.random.default_rng(seed).integers(0, 1 << 16, (h, w, 1), dtype=np.uint16)
+
+
+def make_tga(ref, manifest):
+    manifest["tga"] = {}
+    for name, (expr, depth, itype, ident, desc) in TGA.items():
+        img = eval(expr, {"rng16": rng16}) if expr.startswith("rng16") else make(expr)
+        raw = tga_file(np.ascontiguousarray(img), depth, itype, ident, desc)
+        with open(os.path.join(HERE, name + ".tga"), "wb") as f:
+            f.write(raw)
+        dec = ref.load_tga(raw)
+        e = manifest["tga"][name] = {"image": expr, "depth": depth, "type": itype,
+                                     "file_sha256": hashlib.sha256(raw).hexdigest(),
+                                     "width": int(dec.shape[1]), "height": int(dec.shape[0]),
+                                     "decoded_sha256": sha(dec)}
+        if dec.shape[0] % 4 == 0 and dec.shape[1] % 4 == 0:
+            # what `tc -q 0` makes of the file: FasTC's blocks and PSNR line
+            blocks = ref.compress(dec, steps=0)
+            e["q0_blocks_sha256"] = sha(blocks)
+            e["q0_tc_psnr"] = ref.tc_psnr(dec, blocks, 7)
+        print(name, dec.shape, len(raw), "bytes")
+    for name in TGA_REFUSED:
+        raw = tga_refused(name)
+        with open(os.path.join(HERE, name + ".tga"), "wb") as f:
+            f.write(raw)
+        assert ref.load_tga(raw) is None, name
+        manifest["tga"][name] = {"file_sha256": hashlib.sha256(raw).hexdigest(), "refused": True}
+        print(name, "refused")
 
 
 def dxt_random_blocks(w: int, h: int, fmt: int, seed: int) -> np.ndarray:
@@ -246,7 +346,7 @@ def main():
     ap.add_argument("--dxt-only", action="store_true",
                     help="only (re)write the DXT1 / DXT5 fixtures")
     ap.add_argument("--tc-only", action="store_true",
-                    help="only (re)write tc's PSNR values and the KTX fixtures")
+                    help="only (re)write tc's PSNR values, the KTX and the TGA fixtures")
     ap.add_argument("--workers", type=int, default=6)
     args = ap.parse_args()
     if not O.build_ref(args.reference):
@@ -262,6 +362,7 @@ def main():
             make_tc(ref, manifest)
         elif args.tc_only:
             make_tc(ref, manifest)
+            make_tga(ref, manifest)
         else:
             make_full_size(manifest, args.workers)
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
@@ -300,6 +401,7 @@ def main():
     make_stats(ref, manifest)
     make_dxt(ref, manifest)
     make_tc(ref, manifest)
+    make_tga(ref, manifest)
     make_full_size(manifest, args.workers)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)

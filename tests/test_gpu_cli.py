@@ -47,7 +47,10 @@ def test_tc_writes_fasTC_file_and_psnr_line(gpu, manifest, tmp_path, capsys, fmt
     assert line == [f"PSNR: {src_case['tc_psnr']:.3f}"]
 
 
-def test_tc_pads_odd_sizes_and_writes_decoded_png(gpu, tmp_path):
+def test_tc_pads_odd_sizes_and_writes_decoded_png(gpu, tmp_path, capsys):
+    """An image that is not whole blocks is zero-padded with FasTC's warning;
+    the compressed image then has the padded size, so, as FasTC's tc, no
+    PSNR is printed but the message that the sizes differ."""
     from fastc_gb300 import imageio, tc
 
     img = make_image("tile_mix(42, 16, 16)")[:14, :9].copy()
@@ -57,6 +60,11 @@ def test_tc_pads_odd_sizes_and_writes_decoded_png(gpu, tmp_path):
     assert tc.main(["-q", "0", "-d", str(out), str(src)]) == 0
     dec = imageio.read_png(out.read_bytes())
     assert dec.shape == (16, 12, 4)
+    cap = capsys.readouterr()
+    assert "PSNR" not in cap.out
+    assert cap.err.splitlines() == [
+        "TexComp -- WARNING - Image size is not a multiple of block size. Padding with zeros...",
+        "Cannot compute image metrics: compressed and uncompressed dimensions differ."]
 
 
 def test_tc_log_is_compress_with_stats(gpu, tmp_path, monkeypatch):
@@ -100,3 +108,24 @@ def test_tc_dxt_to_ktx_and_png(gpu, port, tmp_path, capsys, monkeypatch, fmt):
     assert tc.main(["-f", fmt, "-l", str(src)]) == 0
     assert np.array_equal(imageio.read_png((tmp_path / f"dxt_in-{fmt.lower()}.png").read_bytes()), dec)
     assert (tmp_path / "dxt_in.log").read_text() == ""
+
+
+@pytest.mark.parametrize("name", ["tga24_raw", "tga32_rle", "tga16_raw"])
+def test_tc_tga_input_gives_fasTC_output(gpu, manifest, tmp_path, capsys, name):
+    """`tc -q 0 -d out.ktx file.tga`: the blocks FasTC's tc writes for the
+    texels its loader reads, and its PSNR line."""
+    import os
+    import shutil
+
+    from fastc_gb300 import imageio, tc
+
+    e = manifest["tga"][name]
+    src = tmp_path / (name + ".tga")
+    shutil.copy(os.path.join(os.path.dirname(__file__), "golden", name + ".tga"), src)
+    out = tmp_path / "out.ktx"
+    assert tc.main(["-q", "0", "-d", str(out), str(src)]) == 0
+    blocks, w, h = imageio.read_ktx(out.read_bytes())
+    assert (w, h) == (e["width"], e["height"])
+    assert hashlib.sha256(blocks.tobytes()).hexdigest() == e["q0_blocks_sha256"]
+    line = [l for l in capsys.readouterr().out.splitlines() if l.startswith("PSNR: ")]
+    assert line == [f"PSNR: {e['q0_tc_psnr']:.3f}"]

@@ -102,3 +102,36 @@ def test_cli_refuses_what_it_does_not_do(capsys):
     assert tc.main(["-f", "PVRTC", "x.png"]) == 1
     assert tc.main(["-q"]) == 1
     assert tc.main([]) == 1
+
+
+def _tga_names():
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(__file__), "golden", "manifest.json")) as f:
+        return sorted(json.load(f)["tga"])
+
+
+@pytest.mark.parametrize("name", _tga_names())
+def test_tga_reads_as_fasTC_loader(manifest, name):
+    """TGA inputs decode to the texels FasTC's tc loads from them
+    (ImageLoaderTGA over its targa reader, rows bottom-up whatever the
+    descriptor says), and the files FasTC refuses are refused."""
+    import hashlib
+    import os
+
+    from fastc_gb300 import imageio
+
+    e = manifest["tga"][name]
+    path = os.path.join(os.path.dirname(__file__), "golden", name + ".tga")
+    with open(path, "rb") as f:
+        raw = f.read()
+    assert hashlib.sha256(raw).hexdigest() == e["file_sha256"]
+    if e.get("refused"):
+        with pytest.raises(ValueError):
+            imageio.read_tga(raw)
+        return
+    img = imageio.read_tga(raw)
+    assert img.shape == (e["height"], e["width"], 4) and img.dtype == np.uint8
+    assert hashlib.sha256(img.tobytes()).hexdigest() == e["decoded_sha256"]
+    assert np.array_equal(imageio.load_image(path), img)
