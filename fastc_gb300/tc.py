@@ -65,11 +65,16 @@ def main(argv=None) -> int:
             elif opt == "-d":
                 out_name = val
             elif opt == "-f":
-                if val not in ("BPTC", "BPTCLib", "DXT1", "DXT5"):
+                # FasTC's names (CLTool/src/tc.cpp:121-148); a name it does
+                # not know leaves the format as it was
+                if val in ("PVRTC", "PVRTCLib", "ETC1"):
                     print(f"format {val} is not supported: this build encodes BPTC, DXT1 and DXT5",
                           file=sys.stderr)
                     return 1
-                fmt = "BPTC" if val == "BPTCLib" else val
+                if val in ("DXT1", "DXT5"):
+                    fmt = val
+                elif val == "BPTCLib":
+                    fmt = "BPTC"
             i += 2
             continue
         if opt == "-nd":

@@ -100,6 +100,7 @@ def test_cli_refuses_what_it_does_not_do(capsys):
 
     assert tc.main(["-f", "ETC1", "x.png"]) == 1
     assert tc.main(["-f", "PVRTC", "x.png"]) == 1
+    assert tc.main(["-f", "PVRTCLib", "x.png"]) == 1
     assert tc.main(["-q"]) == 1
     assert tc.main([]) == 1
 
