@@ -572,7 +572,7 @@ def single_launch(img, steps: int, warmup: int, reps: int):
     return w * h / dt / 1e6, dt, din, dout, psnr(dout, din, w, h)
 
 
-def dxt_bench(imgs, din, hin, c2_img, reps: int = 5):
+def dxt_bench(imgs, din, hin, c2_img, reps: int = 5, clocks=None):
     """DXT1 and DXT5 (FasTC's CompressImageDXT1 / DXT5) over the texture set:
     device-resident jobs through fastc_dxt_compress_device (launches of up
     to 32 jobs), timed by CUDA events over `reps` passes; the same set end
@@ -594,6 +594,15 @@ def dxt_bench(imgs, din, hin, c2_img, reps: int = 5):
     total_px = sum(im.shape[0] * im.shape[1] for im in imgs)
     blocks = total_px // 16
     peak, peak_kind = measured_peaks()
+    # warp instructions per block of each format's encode kernel, from the
+    # committed launch list of this workload (one ncu pass)
+    try:
+        with open(os.path.join(ROOT, "profiles", "dxt_encode_texture_set_512.json")) as f:
+            dxt_ipb = {k: float(v["warp_instructions_per_block"]) for k, v in json.load(f)["formats"].items()}
+    except Exception:
+        dxt_ipb = {}
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
     port = O.Port()
     band = np.ascontiguousarray(c2_img[:256])
     res = {"workload": "texture_set_512", "texels": total_px, "blocks": blocks,
@@ -651,6 +660,15 @@ def dxt_bench(imgs, din, hin, c2_img, reps: int = 5):
             "cpu_port_1core_mpix_s": band.shape[0] * band.shape[1] / cpu_dt / 1e6,
             "band_equals_oracle": bool(np.array_equal(got, want)),
         }
+        ipb = dxt_ipb.get(fmt.name.lower())
+        if ipb:
+            # the encoder is issue-bound: warp instructions per block x
+            # blocks/s against 4 schedulers x SMs x the SM clock
+            issued = ipb * blocks / dt
+            res[fmt.name.lower()]["issue_roofline"] = {
+                "achieved": issued, "peak": 4.0 * sms * mhz * 1e6, "unit": "warp-inst/s",
+                "frac": issued / (4.0 * sms * mhz * 1e6), "instructions_per_block": ipb,
+                "sms": sms, "sm_mhz": mhz}
         del outs
     return res
 
@@ -662,8 +680,41 @@ def fasTC_full_size_psnr(name: str):
     return sum(case["psnr"]) / len(case["psnr"])
 
 
+def profile_set(args):
+    """The 512-texture set, device-resident, encoded `case_repeat` times per
+    format (DXT1 then DXT5 for --case-format dxt): the bench's own DXT
+    launches, for ncu captures of that workload."""
+    import torch
+
+    from fastc_gb300 import CompressionFormat, CompressionJob, dxt
+
+    imgs = make_texture_set(min(16, os.cpu_count() or 1))
+    fmts = ["dxt1", "dxt5"] if args.case_format == "dxt" else [args.case_format]
+    if "bptc" in fmts:
+        raise SystemExit("the texture-set case covers DXT1 / DXT5 (the BC7 step is bench.py itself)")
+    din = [torch.from_numpy(im).cuda() for im in imgs]
+    px = sum(im.shape[0] * im.shape[1] for im in imgs)
+    for name in fmts:
+        fmt = CompressionFormat[name.upper()]
+        bsz = 8 if fmt == CompressionFormat.DXT1 else 16
+        outs = [torch.zeros(im.shape[0] * im.shape[1] * bsz // 16, dtype=torch.uint8, device="cuda")
+                for im in imgs]
+        jobs = [CompressionJob(a, o, im.shape[1], im.shape[0], format=fmt) for a, o, im in zip(din, outs, imgs)]
+        for _ in range(args.case_repeat):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            dxt.compress_dxt_jobs(jobs)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            print(f"texture_set_512 {fmt.name}: {dt * 1e3:.3f} ms, {px / dt / 1e6:.1f} MPix/s")
+        del outs
+
+
 def profile_case(args):
     """One seeded texture encoded `case_repeat` times (for ncu captures)."""
+    if args.case_kind == "texture_set":
+        profile_set(args)
+        return
     n = args.case_size
     from fastc_gb300 import synth
 
@@ -681,6 +732,8 @@ def profile_case(args):
 
     set_engine(args.case_engine)
     set_launch_shape(args.case_warps, 0)
+    if args.case_format == "dxt":
+        raise SystemExit("--case-format dxt (both formats) is for --case-kind texture_set")
     fmt = CompressionFormat[args.case_format.upper()]
     din = torch.from_numpy(img).cuda()
     dout = torch.zeros(n * n * (8 if fmt == CompressionFormat.DXT1 else 16) // 16, dtype=torch.uint8,
@@ -720,10 +773,11 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--profile-case", action="store_true",
                     help="encode one texture --case-repeat times (for ncu captures)")
-    ap.add_argument("--case-kind", default="tile_mix", choices=["tile_mix", "radial", "gradient"])
+    ap.add_argument("--case-kind", default="tile_mix",
+                    choices=["tile_mix", "radial", "gradient", "texture_set"])
     ap.add_argument("--case-size", type=int, default=4096)
     ap.add_argument("--case-steps", type=int, default=50)
-    ap.add_argument("--case-format", default="bptc", choices=["bptc", "dxt1", "dxt5"])
+    ap.add_argument("--case-format", default="bptc", choices=["bptc", "dxt1", "dxt5", "dxt"])
     ap.add_argument("--case-repeat", type=int, default=1)
     ap.add_argument("--case-engine", type=int, default=0,
                     help="0: pipeline engine, 1: warp-per-block engine")
@@ -945,7 +999,7 @@ def main():
     plan.close()
     small_plan.close()
     if extras:
-        line["dxt"] = dxt_bench(imgs, din, hin, c2_img)
+        line["dxt"] = dxt_bench(imgs, din, hin, c2_img, clocks=line["clocks"])
         del din, dout, hin, hout
         torch.cuda.empty_cache()
         # config 2: one 2048x2048 tile-mix texture at q50 in one launch
