@@ -880,6 +880,7 @@ def main():
     small = [i for i, im in enumerate(imgs) if im.shape[0] * im.shape[1] <= SMALL_PIXELS]
     small_px = sum(imgs[i].shape[0] * imgs[i].shape[1] for i in small)
     small_plan = Plan([jobs[i] for i in small], settings)
+    small_tuning = small_plan.autotune(stream, launches=3)  # outside the timed region
     for _ in range(3):
         small_plan.launch()
     barrier()
@@ -890,6 +891,7 @@ def main():
     e1.record(stream)
     barrier()
     small_batched = small_px * reps / (e0.elapsed_time(e1) / 1e3) / 1e6
+    small_identical = all(torch.equal(dout[i], ref_blocks[i]) for i in small)
     plain_pass([jobs[i] for i in small])
     barrier()
     e0.record(stream)
@@ -941,8 +943,10 @@ def main():
                    "l2": "inputs 462 MB > L2, no flush", "parallelism": f"replica x{world}",
                    "autotuned": tuning},
         "plain_mpix_s": plain_value, "batched_over_plain": value / world / plain_value,
-        "small_textures": {"count": len(small), "texels": small_px, "batched_mpix_s": small_batched,
-                           "plain_mpix_s": small_plain, "batched_over_plain": small_batched / small_plain},
+        "small_textures": {"count": len(small), "texels": small_px, "autotuned": small_tuning,
+                           "batched_mpix_s": small_batched,
+                           "plain_mpix_s": small_plain, "batched_over_plain": small_batched / small_plain,
+                           "batched_equals_plain": bool(small_identical)},
         "batched_equals_plain": bool(identical), "psnr_db": psnr, "device_flags": flags,
         "e2e": {"value": e2e_value, "unit": "MPix/s", "h2d_bytes_per_step": total_px * 4,
                 "d2h_bytes_per_step": total_blocks * 16, "identical_to_device_path": bool(e2e_identical)},
