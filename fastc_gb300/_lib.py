@@ -124,6 +124,7 @@ SIGNATURES = {
     "fastc_bc7_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     "fastc_bc7_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Job), C.POINTER(Settings),
                                           C.POINTER(C.c_uint64)]),
+    "fastc_dxt_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Job), C.c_int, C.POINTER(C.c_uint64)]),
     "fastc_bc7_server_poll": (C.c_int, [C.c_void_p, C.c_uint64]),
     "fastc_bc7_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int64]),
     "fastc_bc7_server_request_psnr": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_double)]),

@@ -14,7 +14,10 @@
 // its texture, position and settings, so a request gives the same bytes
 // alone or in any mix. After the encode each request's blocks are decoded
 // and compared with its texels on the device (FasTC's PSNR metric), so the
-// server reports every request's quality beside its latency.
+// server reports every request's quality beside its latency. DXT1 / DXT5
+// requests (fastc_dxt_server_submit) share the queue, the budget and the
+// batches: a batch's BC7 requests go through the BC7 encoder, its DXT ones
+// through the DXT kernel, on the same stream.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -31,6 +34,7 @@
 
 #include "bc7_host.h"
 #include "bc7_kernels.cuh"
+#include "dxt.cuh"
 #include "fastc_bc7.h"
 
 using fastc::JobDev;
@@ -46,6 +50,7 @@ struct Request {
   uint64_t id = 0;
   fastc_bc7_job job{};
   fastc_bc7_settings settings{};
+  int format = 0;                 // 0: BC7, FASTC_DXT1, FASTC_DXT5
   uint32_t first = 0, count = 0;  // raster block range
   uint32_t row0 = 0;              // first texel row uploaded
   size_t in_bytes = 0, out_bytes = 0;
@@ -97,11 +102,12 @@ struct fastc_bc7_server_s {
   Clock::time_point t_last;
 
   // device bytes a batch needs, beyond the per-request texels and blocks
-  // (job table, the quality sums, encoder scratch for the most cluster fits
-  // per block that the batch's mode masks allow)
-  size_t batch_overhead(uint64_t blocks, size_t njobs, int task_bound) const {
+  // (job table, the quality sums, BC7 encoder scratch for the most cluster
+  // fits per block that the batch's mode masks allow; DXT needs none)
+  size_t batch_overhead(uint64_t bc7_blocks, uint64_t blocks, size_t njobs, int task_bound) const {
     return round_up(njobs * sizeof(JobDev)) + round_up(njobs * sizeof(double)) +
-           round_up(blocks * sizeof(double)) + scratch_bytes(blocks, engine, task_bound);
+           round_up(blocks * sizeof(double)) +
+           (bc7_blocks ? scratch_bytes(bc7_blocks, engine, task_bound) : 0);
   }
 
   void loop();
@@ -126,23 +132,28 @@ void CUDART_CB on_batch_done(void *arg) {
 void fastc_bc7_server_s::launch(Slot &s) {
   // Called by the worker without the lock; s.reqs/out_off/bytes are set.
   cudaError_t e = cudaSuccess;
-  uint64_t total = 0;
+  uint64_t total = 0, bc7_total = 0;
   size_t in_total = 0, out_total = 0;
   std::vector<size_t> in_off(s.reqs.size());
   s.out_off.assign(s.reqs.size(), 0);
+  int tb = 0;
   for (size_t i = 0; i < s.reqs.size(); i++) {
+    const Request &r = *s.reqs[i];
     in_off[i] = in_total;
     s.out_off[i] = out_total;
-    in_total += round_up(s.reqs[i]->in_bytes);
-    out_total += round_up(s.reqs[i]->out_bytes);
-    total += s.reqs[i]->count;
+    in_total += round_up(r.in_bytes);
+    out_total += round_up(r.out_bytes);
+    total += r.count;
+    if (r.format == 0) {
+      bc7_total += r.count;
+      tb = std::max(tb, fastc::block_task_bound(r.settings.block_modes));
+    }
   }
   const size_t table = round_up(s.reqs.size() * sizeof(JobDev));
   const size_t sums = round_up(s.reqs.size() * sizeof(double));  // per-request error
   const size_t errs = round_up(total * sizeof(double));          // per-block error
-  int tb = 0;
-  for (Request *r : s.reqs) tb = std::max(tb, fastc::block_task_bound(r->settings.block_modes));
-  const size_t need = in_total + out_total + table + sums + errs + scratch_bytes(total, engine, tb);
+  const size_t need = in_total + out_total + table + sums + errs +
+                      (bc7_total ? scratch_bytes(bc7_total, engine, tb) : 0);
   if (s.pinned_cap < out_total + sums) {
     if (s.pinned) cudaFreeHost(s.pinned);
     s.pinned = nullptr;
@@ -158,38 +169,53 @@ void fastc_bc7_server_s::launch(Slot &s) {
     double *dsum = reinterpret_cast<double *>(reinterpret_cast<uint8_t *>(dtab) + table);
     double *derr = reinterpret_cast<double *>(reinterpret_cast<uint8_t *>(dsum) + sums);
     void *scratch = reinterpret_cast<uint8_t *>(derr) + errs;
-    std::vector<JobDev> dj(s.reqs.size());
+    // BC7 requests: the encoder's job table; DXT1 / DXT5 requests: the DXT
+    // kernel's launch parameters
+    std::vector<JobDev> dj, dxt[2];
     uint64_t begin = 0;
     for (size_t i = 0; i < s.reqs.size() && e == cudaSuccess; i++) {
       Request &r = *s.reqs[i];
-      dj[i] = make_job(r.job, r.settings, r.first, r.count, begin);
-      dj[i].in = din + in_off[i];
-      dj[i].out = dout + s.out_off[i];
-      dj[i].row0 = r.row0;
-      dj[i].out_first = r.first;
-      dj[i].flags = fastc::kJobIn16 | fastc::kJobOut16;
-      begin += r.count;
+      JobDev d = make_job(r.job, r.settings, r.first, r.count, r.format == 0 ? begin : 0);
+      d.in = din + in_off[i];
+      d.out = dout + s.out_off[i];
+      d.row0 = r.row0;
+      d.out_first = r.first;
+      if (r.format == 0) {
+        d.flags = fastc::kJobIn16 | fastc::kJobOut16;
+        dj.push_back(d);
+        begin += r.count;
+      } else {
+        d.flags = fastc::kJobIn16 | (r.format == FASTC_DXT5 ? fastc::kJobOut16 : 0u);
+        dxt[r.format == FASTC_DXT5].push_back(d);
+      }
       const uint8_t *src = r.job.in + (size_t)r.row0 * r.job.width * 4;
       e = cudaMemcpyAsync(din + in_off[i], src, r.in_bytes, cudaMemcpyHostToDevice, s.stream);
     }
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && !dj.empty())
       e = cudaMemcpyAsync(dtab, dj.data(), dj.size() * sizeof(JobDev), cudaMemcpyHostToDevice,
                           s.stream);
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && !dj.empty()) {
       fastc::LaunchShape shape;
       {
         std::lock_guard<std::mutex> lk(g_mu);
-        shape = pick_shape(total);
+        shape = pick_shape(bc7_total);
       }
-      e = (cudaError_t)launch_engine(dtab, (int)dj.size(), total, scratch, engine, shape, tb, s.cls,
-                                     s.stream);
+      e = (cudaError_t)launch_engine(dtab, (int)dj.size(), bc7_total, scratch, engine, shape, tb,
+                                     s.cls, s.stream);
     }
+    for (int a = 0; a < 2 && e == cudaSuccess; a++)
+      if (!dxt[a].empty())
+        e = fastc::dxt_encode_jobs(dxt[a].data(), (uint32_t)dxt[a].size(), a == 1, s.stream);
     uint64_t at = 0;  // each request's quality, from its uploaded texels and its blocks
     for (size_t i = 0; i < s.reqs.size() && e == cudaSuccess; i++) {
       const Request &r = *s.reqs[i];
-      e = (cudaError_t)fastc::launch_range_error(dout + s.out_off[i], din + in_off[i], r.job.width,
-                                                 r.row0, r.first, r.count, derr + at, dsum + i,
-                                                 s.stream);
+      if (r.format == 0)
+        e = (cudaError_t)fastc::launch_range_error(dout + s.out_off[i], din + in_off[i], r.job.width,
+                                                   r.row0, r.first, r.count, derr + at, dsum + i,
+                                                   s.stream);
+      else
+        e = fastc::dxt_range_error(dout + s.out_off[i], din + in_off[i], r.job.width, r.row0, r.first,
+                                   r.count, r.format == FASTC_DXT5, derr + at, dsum + i, s.stream);
       at += r.count;
     }
     if (e == cudaSuccess)
@@ -222,7 +248,8 @@ void fastc_bc7_server_s::retire(Slot &s) {
     for (size_t i = 0; i < s.reqs.size(); i++) out_total += round_up(s.reqs[i]->out_bytes);
     for (size_t i = 0; i < s.reqs.size(); i++) {
       Request &r = *s.reqs[i];
-      std::memcpy(r.job.out + (size_t)r.first * 16, s.pinned + s.out_off[i], r.out_bytes);
+      std::memcpy(r.job.out + (size_t)r.first * (r.out_bytes / std::max<uint32_t>(r.count, 1)),
+                s.pinned + s.out_off[i], r.out_bytes);
       std::memcpy(&r.sse, s.pinned + out_total + i * sizeof(double), sizeof(double));
     }
   }
@@ -273,7 +300,7 @@ void fastc_bc7_server_s::loop() {
       }
     if (free_slot && !pending.empty()) {
       std::vector<Request *> batch;
-      uint64_t blocks = 0;
+      uint64_t blocks = 0, bc7_blocks = 0;
       size_t data = 0;
       int tb = 0;
       // A batch takes at most its share of the budget (budget / slots), so
@@ -284,15 +311,18 @@ void fastc_bc7_server_s::loop() {
       while (!pending.empty() && batch.size() < cfg.max_batch_jobs) {
         Request *r = pending.front();
         const uint64_t nb = blocks + r->count;
+        const uint64_t nb7 = bc7_blocks + (r->format == 0 ? r->count : 0);
         const size_t nd = data + round_up(r->in_bytes) + round_up(r->out_bytes);
-        const int ntb = std::max(tb, fastc::block_task_bound(r->settings.block_modes));
-        const size_t need = nd + batch_overhead(nb, batch.size() + 1, ntb);
+        const int ntb =
+            r->format == 0 ? std::max(tb, fastc::block_task_bound(r->settings.block_modes)) : tb;
+        const size_t need = nd + batch_overhead(nb7, nb, batch.size() + 1, ntb);
         if (!batch.empty() && (nb > cfg.max_batch_blocks || need > share)) break;
         if (in_use + need > cfg.memory_budget) break;
         pending.pop_front();
         r->state = kRunning;
         batch.push_back(r);
         blocks = nb;
+        bc7_blocks = nb7;
         data = nd;
         tb = ntb;
       }
@@ -300,7 +330,7 @@ void fastc_bc7_server_s::loop() {
         free_slot->busy = true;
         free_slot->finished = false;
         free_slot->reqs = batch;
-        free_slot->bytes = data + batch_overhead(blocks, batch.size(), tb);
+        free_slot->bytes = data + batch_overhead(bc7_blocks, blocks, batch.size(), tb);
         in_use += free_slot->bytes;
         peak = std::max(peak, in_use);
         batches++;
@@ -343,6 +373,10 @@ fastc_bc7_status fastc_bc7_server_create(const fastc_bc7_server_config *cfg,
     std::lock_guard<std::mutex> lk(g_mu);
     fastc::upload_tables(dev);
   }
+  {
+    const cudaError_t e = fastc::dxt_prepare(dev);
+    if (e != cudaSuccess) return fail_cuda(e);
+  }
   auto *s = new fastc_bc7_server_s();
   s->cfg = c;
   s->device = dev;
@@ -366,31 +400,28 @@ fastc_bc7_status fastc_bc7_server_create(const fastc_bc7_server_config *cfg,
   return FASTC_BC7_OK;
 }
 
-fastc_bc7_status fastc_bc7_server_submit(fastc_bc7_server s, const fastc_bc7_job *job,
-                                         const fastc_bc7_settings *settings, uint64_t *id) {
-  if (!s || !job || !id) return FASTC_BC7_ERR_INVALID_ARGUMENT;
-  fastc_bc7_settings st;
-  fastc_bc7_settings_default(&st);
-  if (settings) st = *settings;
-  fastc_bc7_status why;
-  if (!settings_ok(st, &why)) return why;
-  if (st.watermark_start == FASTC_BC7_WATERMARK_CONTINUE) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+// Queues a request of format 0 (BC7, with settings st) or FASTC_DXT1 / DXT5.
+static fastc_bc7_status submit_request(fastc_bc7_server s, const fastc_bc7_job *job,
+                                       const fastc_bc7_settings &st, int format, uint64_t *id) {
   uint32_t first, count;
   if (!job->in || !job->out || !job_range(*job, &first, &count)) return FASTC_BC7_ERR_INVALID_ARGUMENT;
   auto r = std::make_unique<Request>();
   r->job = *job;
   r->settings = st;
+  r->format = format;
   r->first = first;
   r->count = count;
   const uint32_t bw = job->width / 4;
   const uint32_t r0 = count ? first / bw : 0, r1 = count ? (first + count - 1) / bw : 0;
   r->row0 = r0 * 4;
   r->in_bytes = count ? (size_t)(r1 - r0 + 1) * 4 * job->width * 4 : 0;
-  r->out_bytes = (size_t)count * 16;
+  r->out_bytes = (size_t)count * (format == FASTC_DXT1 ? 8 : 16);
   r->t_submit = Clock::now();
   std::lock_guard<std::mutex> lk(s->mu);
-  const size_t alone = round_up(r->in_bytes) + round_up(r->out_bytes) +
-                       s->batch_overhead(count, 1, fastc::block_task_bound(r->settings.block_modes));
+  const size_t alone =
+      round_up(r->in_bytes) + round_up(r->out_bytes) +
+      s->batch_overhead(format == 0 ? count : 0, count, 1,
+                        format == 0 ? fastc::block_task_bound(r->settings.block_modes) : 0);
   s->submitted++;
   if (!s->started) {
     s->started = true;
@@ -417,6 +448,27 @@ fastc_bc7_status fastc_bc7_server_submit(fastc_bc7_server s, const fastc_bc7_job
   s->reqs.emplace(r->id, std::move(r));
   s->cv_work.notify_all();
   return FASTC_BC7_OK;
+}
+
+fastc_bc7_status fastc_bc7_server_submit(fastc_bc7_server s, const fastc_bc7_job *job,
+                                         const fastc_bc7_settings *settings, uint64_t *id) {
+  if (!s || !job || !id) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  fastc_bc7_settings st;
+  fastc_bc7_settings_default(&st);
+  if (settings) st = *settings;
+  fastc_bc7_status why;
+  if (!settings_ok(st, &why)) return why;
+  if (st.watermark_start == FASTC_BC7_WATERMARK_CONTINUE) return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  return submit_request(s, job, st, 0, id);
+}
+
+fastc_bc7_status fastc_dxt_server_submit(fastc_bc7_server s, const fastc_bc7_job *job, int format,
+                                         uint64_t *id) {
+  if (!s || !job || !id || (format != FASTC_DXT1 && format != FASTC_DXT5))
+    return FASTC_BC7_ERR_INVALID_ARGUMENT;
+  fastc_bc7_settings st;
+  fastc_bc7_settings_default(&st);
+  return submit_request(s, job, st, format, id);
 }
 
 // FasTC's Image::ComputePSNR from a summed error (Base/src/Image.cpp:206-255):

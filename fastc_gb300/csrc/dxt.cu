@@ -22,6 +22,7 @@
 
 #include "bc7_host.h"
 #include "bc7_kernels.cuh"
+#include "dxt.cuh"
 #include "fastc_bc7.h"
 
 namespace fastc {
@@ -522,6 +523,34 @@ __global__ void dxt_error_kernel(const uint8_t *__restrict__ blocks, const uint8
   sse[b] = s;
 }
 
+// The same error for count consecutive blocks of an image (raster block
+// first on), the texels given from row row0 on.
+template <bool kAlpha>
+__global__ void dxt_range_error_kernel(const uint8_t *__restrict__ blocks,
+                                       const uint8_t *__restrict__ rows, uint32_t width, uint32_t row0,
+                                       uint32_t first, uint32_t count, double *__restrict__ sse) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const uint32_t bw = width / 4, b = first + k;
+  const uint32_t bx = b % bw, by = b / bw;
+  uint32_t dec[16];
+  dxt_decode_block<kAlpha>(blocks + (size_t)k * (kAlpha ? 16 : 8), dec);
+  double s = 0.0;
+  for (int y = 0; y < 4; y++)
+    for (int x = 0; x < 4; x++) {
+      const uint8_t *p = rows + ((size_t)(by * 4 + y - row0) * width + bx * 4 + x) * 4;
+      const uint32_t d = dec[4 * y + x];
+      const double ra = (double)p[3] / 255.0, ua = (double)(d >> 24) / 255.0;
+      double t = 0.0;
+      for (int c = 0; c < 3; c++) {
+        const double e = ra * (double)p[c] - ua * (double)((d >> (8 * c)) & 0xFF);
+        t += e * e;
+      }
+      s += t;
+    }
+  sse[k] = s;
+}
+
 cudaError_t launch_dxt_error(const uint8_t *blocks, const uint8_t *rgba, uint32_t width, uint32_t height,
                              bool alpha, double *block_sse, double *total, cudaStream_t st) {
   const uint64_t nb = (uint64_t)((width + 3) / 4) * ((height + 3) / 4);
@@ -630,6 +659,35 @@ cudaError_t host_context(int dev, size_t events) {
 }
 
 }  // namespace
+
+cudaError_t dxt_prepare(int dev) { return dxt_setup(dev); }
+
+cudaError_t dxt_encode_jobs(JobDev *jobs, uint32_t n, bool alpha, cudaStream_t st) {
+  for (uint32_t k0 = 0; k0 < n; k0 += kDxtJobsPerLaunch) {
+    const uint32_t m = std::min<uint32_t>(kDxtJobsPerLaunch, n - k0);
+    uint64_t begin = 0;
+    for (uint32_t k = k0; k < k0 + m; k++) {
+      jobs[k].begin = begin;
+      begin += jobs[k].nblocks;
+    }
+    const cudaError_t e = dxt_launch(jobs + k0, m, begin, alpha, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t dxt_range_error(const uint8_t *blocks, const uint8_t *rows, uint32_t width, uint32_t row0,
+                            uint32_t first, uint32_t count, bool alpha, double *block_sse,
+                            double *total, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  const unsigned grid = (count + 127) / 128;
+  if (alpha) dxt_range_error_kernel<true><<<grid, 128, 0, st>>>(blocks, rows, width, row0, first, count, block_sse);
+  else dxt_range_error_kernel<false><<<grid, 128, 0, st>>>(blocks, rows, width, row0, first, count, block_sse);
+  const int e = launch_sum(block_sse, count, total, st);
+  if (e) return (cudaError_t)e;
+  return cudaPeekAtLastError();
+}
+
 }  // namespace fastc
 
 using fastc::JobDev;

@@ -1,4 +1,5 @@
-"""Python front end of the continuous-batching BC7 request server.
+"""Python front end of the continuous-batching BC7 (and DXT1 / DXT5)
+request server.
 
 The server itself (admission by device-memory budget, batches on several
 streams, completion callbacks) is native code in the library; this module
@@ -7,6 +8,7 @@ keeps the request buffers alive and converts results and statistics.
     with Server(memory_budget=8 << 30) as srv:
         req = srv.submit(rgba, CompressionSettings(num_simulated_annealing_steps=16))
         blocks = srv.wait(req)          # numpy uint8, width*height bytes
+        dxt = srv.submit(rgba, format=CompressionFormat.DXT1)  # same queue and batches
 """
 from __future__ import annotations
 
@@ -18,7 +20,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import BC7Error, Job, ServerConfig, ServerStats, check, load
-from .bptc import CompressionSettings
+from .bptc import FORMAT_BLOCK_BYTES, CompressionFormat, CompressionSettings
 
 
 @dataclass
@@ -50,17 +52,26 @@ class Server:
         self._lib = lib
 
     def submit(self, rgba: np.ndarray, settings: Optional[CompressionSettings] = None,
-               out: Optional[np.ndarray] = None) -> Request:
+               out: Optional[np.ndarray] = None,
+               format: CompressionFormat = CompressionFormat.BPTC) -> Request:
+        """Queue one texture: BC7 with `settings`, or DXT1 / DXT5 (settings
+        do not apply) through fastc_dxt_server_submit."""
         rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
         h, w = rgba.shape[:2]
+        fmt = CompressionFormat(format)
         if out is None:
-            out = np.zeros(w * h, dtype=np.uint8)
+            out = np.zeros(w * h * FORMAT_BLOCK_BYTES[fmt] // 16, dtype=np.uint8)
         job = Job(rgba.ctypes.data, out.ctypes.data, w, h, 0, 0, w, h)
-        s = (settings or CompressionSettings()).to_c()
         rid = C.c_uint64()
-        st = self._lib.fastc_bc7_server_submit(self._h, C.byref(job), C.byref(s), C.byref(rid))
+        if fmt == CompressionFormat.BPTC:
+            s = (settings or CompressionSettings()).to_c()
+            st = self._lib.fastc_bc7_server_submit(self._h, C.byref(job), C.byref(s), C.byref(rid))
+            name = "fastc_bc7_server_submit"
+        else:
+            st = self._lib.fastc_dxt_server_submit(self._h, C.byref(job), int(fmt), C.byref(rid))
+            name = "fastc_dxt_server_submit"
         if st != _lib.OK:
-            raise BC7Error(st, "fastc_bc7_server_submit")
+            raise BC7Error(st, name)
         return Request(int(rid.value), rgba, out, w, h)
 
     def poll(self, req: Request) -> bool:

@@ -347,6 +347,16 @@ FASTC_BC7_API fastc_bc7_status fastc_bc7_server_create(const fastc_bc7_server_co
 FASTC_BC7_API fastc_bc7_status fastc_bc7_server_submit(fastc_bc7_server s, const fastc_bc7_job *job,
                                                        const fastc_bc7_settings *settings,
                                                        uint64_t *request_id);
+/* Queue one DXT1 / DXT5 job (format FASTC_DXT1 or FASTC_DXT5; the output
+ * holds 8 or 16 bytes per block) on the same server: DXT requests share the
+ * queue, the budget and the batches with BC7 requests (a batch runs its BC7
+ * requests through the BC7 encoder and its DXT requests through the DXT
+ * encoder on the same stream), and poll / wait / request_psnr / cancel /
+ * release and the statistics cover them alike. The second compression
+ * function of FasTC's plugin slot (DXTC::CompressImageDXT1 / DXT5,
+ * DXTEncoder/include/FasTC/DXTCompressor.h:24-25) on the serving runtime. */
+FASTC_BC7_API fastc_bc7_status fastc_dxt_server_submit(fastc_bc7_server s, const fastc_bc7_job *job,
+                                                       int format, uint64_t *request_id);
 /* OK when finished, TIMEOUT while queued or running, else the failure. */
 FASTC_BC7_API fastc_bc7_status fastc_bc7_server_poll(fastc_bc7_server s, uint64_t request_id);
 /* Wait up to timeout_ms (negative: forever). */

@@ -136,3 +136,58 @@ def test_wait_timeout_and_poll(gpu):
             srv.poll(h)
         assert e.value.status == 7
     assert finished_early in (True, False)
+
+
+def test_dxt_requests_share_the_server(gpu, port):
+    """DXT1 / DXT5 requests (fastc_dxt_server_submit) in the same queue and
+    batches as BC7 requests: each gives FasTC's DXT blocks (the oracle's,
+    pinned to FasTC's) alone and in the mix, the BC7 requests among them are
+    unchanged, and each request's PSNR is measured on the device."""
+    from fastc_gb300 import CompressionFormat
+    from fastc_gb300.serve import Server
+
+    rng = np.random.default_rng(9)
+    reqs = []
+    for i in range(18):
+        w, h = (int(x) for x in 4 * rng.integers(2, 30, 2))
+        fmt = [CompressionFormat.BPTC, CompressionFormat.DXT1, CompressionFormat.DXT5][i % 3]
+        reqs.append((make_image(f"tile_mix_radial_alpha({500 + i}, {w}, {h}, 3, 5)"), fmt))
+    alone = []
+    with Server(max_inflight=1) as srv:
+        for img, fmt in reqs:
+            alone.append(srv.wait(srv.submit(img, settings(8), format=fmt)).copy())
+    with Server(max_inflight=3, max_batch_blocks=1024) as srv:
+        handles = [srv.submit(img, settings(8), format=fmt) for img, fmt in reqs]
+        mixed = [srv.wait(hd) for hd in handles]
+        psnrs = [srv.psnr(hd) for hd in handles]
+        st = srv.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0 and st["batches"] >= 2
+    for (img, fmt), a, m, db in zip(reqs, alone, mixed, psnrs):
+        assert np.array_equal(a, m)
+        h, w = img.shape[:2]
+        if fmt == CompressionFormat.BPTC:
+            assert np.array_equal(m, port.compress(img, steps=8, seed=11))
+            dec = port.decompress(m, w, h)
+        else:
+            alpha = fmt == CompressionFormat.DXT5
+            assert len(m) == w * h // (1 if alpha else 2)
+            assert np.array_equal(m, port.dxt_compress(img, alpha))
+            dec = port.dxt_decompress(m, w, h, alpha)
+        assert abs(db - port.psnr(img, dec)) <= 1e-9
+
+
+def test_dxt_submit_rejects_other_formats(gpu):
+    import ctypes as C
+
+    from fastc_gb300 import _lib
+    from fastc_gb300.serve import Server
+
+    img = make_image("tile_mix(5, 16, 16)")
+    out = np.zeros(16 * 16, np.uint8)
+    job = _lib.Job(img.ctypes.data, out.ctypes.data, 16, 16, 0, 0, 16, 16)
+    rid = C.c_uint64()
+    with Server() as srv:
+        for fmt in (0, 3, 7):
+            assert srv._lib.fastc_dxt_server_submit(srv._h, C.byref(job), fmt, C.byref(rid)) == \
+                _lib.ERR_INVALID_ARGUMENT
+        assert srv.stats()["submitted"] == 0
