@@ -53,15 +53,20 @@ class Server:
 
     def submit(self, rgba: np.ndarray, settings: Optional[CompressionSettings] = None,
                out: Optional[np.ndarray] = None,
-               format: CompressionFormat = CompressionFormat.BPTC) -> Request:
+               format: CompressionFormat = CompressionFormat.BPTC,
+               rect: Optional[tuple] = None) -> Request:
         """Queue one texture: BC7 with `settings`, or DXT1 / DXT5 (settings
-        do not apply) through fastc_dxt_server_submit."""
+        do not apply) through fastc_dxt_server_submit. `rect` = (x_start,
+        y_start, x_end, y_end) limits the request to a sub-job in FasTC's
+        sense (blocks from (x_start, y_start) in raster order up to x_end on
+        row y_end); its blocks go to their places in `out`."""
         rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
         h, w = rgba.shape[:2]
         fmt = CompressionFormat(format)
         if out is None:
             out = np.zeros(w * h * FORMAT_BLOCK_BYTES[fmt] // 16, dtype=np.uint8)
-        job = Job(rgba.ctypes.data, out.ctypes.data, w, h, 0, 0, w, h)
+        x0, y0, x1, y1 = rect if rect is not None else (0, 0, w, h)
+        job = Job(rgba.ctypes.data, out.ctypes.data, w, h, x0, y0, x1, y1)
         rid = C.c_uint64()
         if fmt == CompressionFormat.BPTC:
             s = (settings or CompressionSettings()).to_c()

@@ -191,3 +191,34 @@ def test_dxt_submit_rejects_other_formats(gpu):
             assert srv._lib.fastc_dxt_server_submit(srv._h, C.byref(job), fmt, C.byref(rid)) == \
                 _lib.ERR_INVALID_ARGUMENT
         assert srv.stats()["submitted"] == 0
+
+
+@pytest.mark.parametrize("fmt_name", ["BPTC", "DXT1", "DXT5"])
+def test_sub_job_requests(gpu, port, fmt_name):
+    """A request for a sub-job (FasTC's job rectangle: raster blocks from
+    (x_start, y_start) to x_end on row y_end) writes exactly those blocks,
+    equal to the whole image's, and its PSNR covers exactly those texels."""
+    from fastc_gb300 import CompressionFormat
+    from fastc_gb300.serve import Server
+
+    fmt = CompressionFormat[fmt_name]
+    img = make_image("tile_mix_radial_alpha(77, 48, 40, 9, 2)")
+    bsz = 8 if fmt == CompressionFormat.DXT1 else 16
+    if fmt == CompressionFormat.BPTC:
+        whole = port.compress(img, steps=8, seed=11)
+        dec = port.decompress(whole, 48, 40)
+    else:
+        whole = port.dxt_compress(img, fmt == CompressionFormat.DXT5)
+        dec = port.dxt_decompress(whole, 48, 40, fmt == CompressionFormat.DXT5)
+    sse = port.block_sse(img, dec).reshape(-1)
+    rect = (8, 12, 20, 28)  # blocks 3 * 12 + 2 .. 7 * 12 + 5 (exclusive)
+    first, end = 3 * 12 + 2, 7 * 12 + 5
+    with Server(max_inflight=2) as srv:
+        out = np.zeros(48 * 40 * bsz // 16, np.uint8)
+        req = srv.submit(img, settings(8), out=out, format=fmt, rect=rect)
+        srv.wait(req)
+        db = srv.psnr(req)
+    assert np.array_equal(out[first * bsz:end * bsz], whole[first * bsz:end * bsz])
+    assert not out[:first * bsz].any() and not out[end * bsz:].any()
+    want = 10 * np.log10(3 * 255.0 ** 2 / (float(sse[first:end].sum()) / ((end - first) * 16)))
+    assert abs(db - want) <= 1e-9
