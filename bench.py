@@ -603,10 +603,30 @@ def dxt_bench(imgs, din, hin, c2_img, reps: int = 5, clocks=None):
         dxt_ipb = {}
     mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
     sms = torch.cuda.get_device_properties(0).multi_processor_count
+    # the host link's own rates (one 256 MB page-locked buffer copied up and
+    # down by cudaMemcpyAsync, 3 times each): the end-to-end figures below
+    # move the texels up and the blocks down across this link
+    link = {}
+    hbuf = torch.empty(256 << 20, dtype=torch.uint8).pin_memory()
+    dbuf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for name, fn in (("h2d_gb_s", lambda: dbuf.copy_(hbuf, non_blocking=True)),
+                     ("d2h_gb_s", lambda: hbuf.copy_(dbuf, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(3):
+            fn()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        link[name] = 3 * hbuf.numel() / (t0.elapsed_time(t1) / 1e3) / 1e9
+    del hbuf, dbuf
     port = O.Port()
     band = np.ascontiguousarray(c2_img[:256])
     res = {"workload": "texture_set_512", "texels": total_px, "blocks": blocks,
-           "l2": "inputs 462 MB > L2, no flush"}
+           "l2": "inputs 462 MB > L2, no flush",
+           "host_link": dict(link, note="cudaMemcpyAsync of one 256 MB page-locked buffer")}
     for fmt in (CompressionFormat.DXT1, CompressionFormat.DXT5):
         bsz = 8 if fmt == CompressionFormat.DXT1 else 16
         outs = [torch.zeros(im.shape[0] * im.shape[1] * bsz // 16, dtype=torch.uint8, device="cuda")
@@ -655,7 +675,11 @@ def dxt_bench(imgs, din, hin, c2_img, reps: int = 5, clocks=None):
                          "algorithmic_bytes_per_block": 64 + bsz},
             "e2e": {"value": total_px / e2e_dt / 1e6, "unit": "MPix/s", "h2d_bytes_per_step": total_px * 4,
                     "d2h_bytes_per_step": blocks * bsz, "entry": "fastc_dxt_compress_batch, pinned buffers",
-                    "copy_gb_s": (total_px * 4 + blocks * bsz) / e2e_dt / 1e9},
+                    "copy_gb_s": (total_px * 4 + blocks * bsz) / e2e_dt / 1e9,
+                    # the time the link alone needs (texels up and blocks
+                    # down, the two directions concurrent) over the measured
+                    "frac_of_link_bound": max(total_px * 4 / (link["h2d_gb_s"] * 1e9),
+                                              blocks * bsz / (link["d2h_gb_s"] * 1e9)) / e2e_dt},
             "host_equals_device": bool(same),
             "cpu_port_1core_mpix_s": band.shape[0] * band.shape[1] / cpu_dt / 1e6,
             "band_equals_oracle": bool(np.array_equal(got, want)),
