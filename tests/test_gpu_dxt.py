@@ -260,3 +260,34 @@ def test_psnr_and_block_sse_match_oracle(gpu, port, manifest, name):
     ddb, dsse = dxt.psnr(torch.from_numpy(blocks).to(gpu), torch.from_numpy(img).to(gpu), w, h, fmt,
                          block_sse=True)
     assert ddb == db and np.array_equal(dsse, sse)
+
+
+@pytest.mark.parametrize("code", [1, 5])
+def test_threads_encode_disjoint_sub_jobs(gpu, port, code):
+    """FasTC's ThreadGroup path: several host threads call the encoder at
+    once, each on its own band of one image's blocks (disjoint sub-jobs
+    into one shared output buffer), as Core does through
+    DXTC::CompressImageDXT1 / DXT5; the blocks equal the whole image's."""
+    import threading
+
+    from fastc_gb300 import CompressionJob, dxt
+
+    img = np.ascontiguousarray(make_image("tile_mix(75, 128, 96)"))
+    out = np.zeros(128 * 96 * bsz(code) // 16, np.uint8)
+    bands = [(0, y, 128, y + 20) for y in range(0, 96, 24)]  # rows y .. y + 20 (FasTC's inclusive end)
+    errors = []
+
+    def work(rect):
+        try:
+            for _ in range(5):
+                dxt.compress_dxt_jobs([CompressionJob(img, out, 128, 96, *rect, format=fmt_of(code))])
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    ts = [threading.Thread(target=work, args=(r,)) for r in bands]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors
+    assert np.array_equal(out, port.dxt_compress(img, code == 5))

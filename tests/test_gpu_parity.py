@@ -268,3 +268,35 @@ def test_gpu_decoder_spec_mode_differs_only_on_mode4_index_mode1(gpu, port):
     mode4_im1 &= ((b[:, 0] >> 7) & 1) == 1
     diff = (ref != spec).reshape(32, 4, 32, 4, 4).any(axis=(1, 3, 4)).reshape(-1)
     assert not np.any(diff & ~mode4_im1)
+
+
+def test_threads_encode_disjoint_sub_jobs(gpu, port):
+    """FasTC's `tc -t N` path: N host threads call Compress at once, each on
+    its own band of one image (disjoint sub-jobs into one output buffer).
+    The image has no single-colour block, so FasTC's shared watermark
+    counter plays no part; the blocks equal the whole image's."""
+    import threading
+
+    from fastc_gb300 import CompressionJob, CompressionSettings, compress, synth
+
+    img = np.ascontiguousarray(make_image("gradient_noise_alpha_ramp(4, 96, 64)"))
+    assert not any((b == b[0]).all() for b in synth.blocks_of(img))
+    out = np.zeros(96 * 64, np.uint8)
+    s = CompressionSettings(num_simulated_annealing_steps=8, seed=11)
+    bands = [(0, y, 96, y + 12) for y in range(0, 64, 16)]
+    errors = []
+
+    def work(rect):
+        try:
+            for _ in range(3):
+                compress(CompressionJob(img, out, 96, 64, *rect), s)
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    ts = [threading.Thread(target=work, args=(r,)) for r in bands]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors
+    assert np.array_equal(out, port.compress(img, steps=8, seed=11))
