@@ -1936,6 +1936,8 @@ cudaError_t class_streams_create(ClassStreams *cs) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&cs->bound[b], cudaEventDisableTiming);
     for (int c = 0; c < kClasses && e == cudaSuccess; c++)
       e = cudaEventCreateWithFlags(&cs->join[b][c], cudaEventDisableTiming);
+    for (int c = 0; c < kClasses && e == cudaSuccess; c++)
+      e = cudaEventCreateWithFlags(&cs->setup[b][c], cudaEventDisableTiming);
   }
   for (int b = 0; b < 2 && e == cudaSuccess; b++)
     for (int c = 0; c < kClasses && e == cudaSuccess; c++)
@@ -1951,8 +1953,10 @@ void class_streams_destroy(ClassStreams *cs) {
   for (int b = 0; b < 2; b++) {
     if (cs->fork[b]) cudaEventDestroy(cs->fork[b]);
     if (cs->bound[b]) cudaEventDestroy(cs->bound[b]);
-    for (int c = 0; c < kClasses; c++)
+    for (int c = 0; c < kClasses; c++) {
       if (cs->join[b][c]) cudaEventDestroy(cs->join[b][c]);
+      if (cs->setup[b][c]) cudaEventDestroy(cs->setup[b][c]);
+    }
   }
   *cs = ClassStreams{};
 }
@@ -2158,13 +2162,16 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
       for (int c = 0; c < kClasses && ce == cudaSuccess; c++)
         ce = cudaStreamWaitEvent(side[c], cls->fork[par], 0);
       if (ce != cudaSuccess) return (int)ce;
-      // every class's setup one after another, then the bound stage, on
-      // the first class's stream (setups of different classes running at
-      // once compete for the SMs' instruction cache, as their code is
-      // large, which costs more than the tails between them); every
-      // class's annealing waits for the bound stage
+      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], false, args, side[kClassOrder[k]]);
+      // the bound stage runs on the first class's stream once every
+      // class's setup is done; every class's annealing waits for it
       const int lead = kClassOrder[0];
-      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], false, args, side[lead]);
+      for (int c = 0; c < kClasses && ce == cudaSuccess; c++) {
+        if (c == lead) continue;
+        ce = cudaEventRecord(cls->setup[par][c], side[c]);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(side[lead], cls->setup[par][c], 0);
+      }
+      if (ce != cudaSuccess) return (int)ce;
       launch_bound(args, side[lead]);
       ce = cudaEventRecord(cls->bound[par], side[lead]);
       for (int c = 0; c < kClasses && ce == cudaSuccess; c++)

@@ -109,18 +109,19 @@ struct PipelineCounters {
 constexpr size_t kCountersSlot = 1024;
 static_assert(sizeof(PipelineCounters) <= kCountersSlot, "PipelineCounters fits its slot");
 
-// Side streams that run the classes' annealing concurrently, forked from
-// and joined back into the caller's stream with events (both are recorded
-// into a CUDA graph when the caller's stream is being captured). Before it,
-// the first class's stream runs every class's setup and the per-block bound
-// stage, and the annealing of every class waits for that.
+// Side streams that run the classes' setup + annealing concurrently, forked
+// from and joined back into the caller's stream with events (both are
+// recorded into a CUDA graph when the caller's stream is being captured).
+// Between the two, the per-block bound stage waits for every class's setup
+// and the annealing of every class waits for it.
 // One set must not be enqueued on by two threads at once.
 // Chunks alternate between two sets, so that a class of chunk i + 1 starts
 // while the same class of chunk i drains.
 struct ClassStreams {
   cudaStream_t side[2][kClasses];
   cudaEvent_t fork[2];
-  cudaEvent_t bound[2];  // every class's setup and the block bounds are done
+  cudaEvent_t setup[2][kClasses];  // a class's setup stage is done
+  cudaEvent_t bound[2];            // the block bounds are done
   cudaEvent_t join[2][kClasses];
 };
 cudaError_t class_streams_create(ClassStreams *cs);
