@@ -2123,6 +2123,12 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
     }
     return (int)cudaPeekAtLastError();
   };
+  // One launch of a single large chunk runs its classes' setup kernels one
+  // after another: setups of different classes running at once compete for
+  // the SMs' instruction cache (their code is large). With several chunks,
+  // or a small one, the concurrent setups fill each other's tails instead.
+  const bool serial_setup =
+      tune.serial_setup > 0 || (tune.serial_setup < 0 && total <= cap && total >= kSerialSetupBlocks);
   uint32_t prev_nb = 0;
   int i = 0;
   for (uint64_t c0 = 0; c0 < total; c0 += cap, i++) {
@@ -2162,11 +2168,13 @@ int launch_pipeline(const JobDev *jobs, int njobs, uint64_t total, const EncodeS
       for (int c = 0; c < kClasses && ce == cudaSuccess; c++)
         ce = cudaStreamWaitEvent(side[c], cls->fork[par], 0);
       if (ce != cudaSuccess) return (int)ce;
-      for (int k = 0; k < kClasses; k++) launch_class_any(kClassOrder[k], false, args, side[kClassOrder[k]]);
       // the bound stage runs on the first class's stream once every
-      // class's setup is done; every class's annealing waits for it
+      // class's setup is done (there, or on their own streams); every
+      // class's annealing waits for it
       const int lead = kClassOrder[0];
-      for (int c = 0; c < kClasses && ce == cudaSuccess; c++) {
+      for (int k = 0; k < kClasses; k++)
+        launch_class_any(kClassOrder[k], false, args, side[serial_setup ? lead : kClassOrder[k]]);
+      for (int c = 0; c < kClasses && ce == cudaSuccess && !serial_setup; c++) {
         if (c == lead) continue;
         ce = cudaEventRecord(cls->setup[par][c], side[c]);
         if (ce == cudaSuccess) ce = cudaStreamWaitEvent(side[lead], cls->setup[par][c], 0);

@@ -145,7 +145,12 @@ struct PipelineTuning {
   int select_ctas_per_sm = 16; // grid of the select stage (grid-stride over the chunk's blocks)
   int setup_ctas_per_sm = 128; // grid cap of the setup stage (one thread per fit up to it)
   uint64_t chunk_blocks = 0;   // blocks per chunk, 0: pipeline_chunk(task bound); never more
+  // the classes' setup kernels one after another on one stream (1) or
+  // concurrently on the side streams (0); -1: one stream for a launch that
+  // is a single chunk of at least kSerialSetupBlocks blocks
+  int serial_setup = -1;
 };
+constexpr uint64_t kSerialSetupBlocks = 1ull << 18;
 // Blocks per chunk a launch uses for this task bound and tuning.
 uint64_t pipeline_chunk_blocks(int task_bound, const PipelineTuning &tune);
 

@@ -200,8 +200,12 @@ void fastc_bc7_server_s::launch(Slot &s) {
         std::lock_guard<std::mutex> lk(g_mu);
         shape = pick_shape(bc7_total);
       }
+      // batches share the GPU with other batches' stages, which fill the
+      // tails of concurrent setups: never the one-stream setup
+      fastc::PipelineTuning tune;
+      tune.serial_setup = 0;
       e = (cudaError_t)launch_engine(dtab, (int)dj.size(), bc7_total, scratch, engine, shape, tb,
-                                     s.cls, s.stream);
+                                     s.cls, tune, s.stream, nullptr, nullptr);
     }
     for (int a = 0; a < 2 && e == cudaSuccess; a++)
       if (!dxt[a].empty())
