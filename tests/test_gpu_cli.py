@@ -1,6 +1,7 @@
 """The tc-compatible command line on the GPU: PNG in, KTX out, the blocks
 those of the library call, PSNR printed as FasTC's tc prints it."""
 import hashlib
+import re
 
 import numpy as np
 import pytest
@@ -43,8 +44,10 @@ def test_tc_writes_fasTC_file_and_psnr_line(gpu, manifest, tmp_path, capsys, fmt
     assert tc.main(["-q", "0", "-f", fmt, "-d", str(out), str(src)]) == 0
     raw = out.read_bytes()
     assert len(raw) == e["bytes"] and hashlib.sha256(raw).hexdigest() == e["sha256"]
-    line = [l for l in capsys.readouterr().out.splitlines() if l.startswith("PSNR: ")]
-    assert line == [f"PSNR: {src_case['tc_psnr']:.3f}"]
+    # FasTC's stdout: the compression time (CompressImageData), then the PSNR
+    lines = capsys.readouterr().out.splitlines()
+    assert re.fullmatch(r"Compression time: \d+\.\d{3} ms", lines[0])
+    assert lines[1:] == [f"PSNR: {src_case['tc_psnr']:.3f}"]
 
 
 def test_tc_pads_odd_sizes_and_writes_decoded_png(gpu, tmp_path, capsys):
