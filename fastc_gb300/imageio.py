@@ -1,7 +1,7 @@
 """Image files for the command-line tool: PNG (8-bit RGB/RGBA/grey, no
-interlace) read and written with zlib, TGA read as FasTC's loader reads it,
-raw RGBA8, numpy arrays, and the KTX container FasTC writes for compressed
-images (BPTC, DXT1, DXT5).
+interlace) read and written with zlib, TGA and uncompressed KTX read as
+FasTC's loaders read them, raw RGBA8, numpy arrays, and the KTX container
+FasTC writes for compressed images (BPTC, DXT1, DXT5).
 
 The KTX layout follows FasTC's ImageWriterKTX (IO/src/ImageWriterKTX.cpp:
 the 12-byte identifier, thirteen little-endian words, one key/value pair
@@ -145,6 +145,43 @@ def png_bytes(rgba: np.ndarray) -> bytes:
             chunk(b"IDAT", zlib.compress(rows.tobytes(), 6)) + chunk(b"IEND", b""))
 
 
+GL_BYTE = 0x1400
+GL_RGBA8 = 0x8058
+
+
+def read_ktx_image(raw: bytes) -> np.ndarray:
+    """RGBA8 (h, w, 4) from an uncompressed KTX file, read as FasTC's loader
+    reads it (ImageLoaderKTX::ReadData, IO/src/ImageLoaderKTX.cpp:128-346):
+    the identifier, the byte order from the endianness word (big-endian
+    integers when its first byte is 4), the key/value data skipped; one
+    mipmap level, one face, no array, depth 0 and a nonzero size; glType
+    GL_BYTE (0x1400, the type FasTC's writer records for RGBA8) and
+    glInternalFormat GL_RGBA8; then the image size word and the texels in
+    file order, which must end the file. Compressed files (glType and
+    glFormat 0) are refused: they hold blocks, not texels to encode."""
+    if len(raw) < 68 or raw[:12] != KTX_IDENTIFIER:
+        raise ValueError("KTX: not a KTX file")
+    order = ">" if raw[12] == 0x04 else "<"
+    (gl_type, _type_size, gl_format, internal, _base, w, h, depth, arrays, faces, mips,
+     kv) = struct.unpack(order + "12I", raw[16:64])
+    pos = 64 + kv
+    if mips != 1:
+        raise ValueError(f"KTX: unsupported mipmap levels: {mips}")
+    if pos + 4 > len(raw):
+        raise ValueError("KTX: truncated")
+    if arrays > 1 or faces != 1 or depth != 0 or h == 0 or w == 0:
+        raise ValueError("KTX: only single 2-D images are supported")
+    if gl_type == 0 and gl_format == 0:
+        raise ValueError("KTX: a compressed file holds blocks; decode it before compressing")
+    if gl_type != GL_BYTE or internal != GL_RGBA8:
+        raise ValueError(f"KTX: unsupported type 0x{gl_type:x} / internal format 0x{internal:x}")
+    pos += 4  # the image size word
+    n = w * h * 4
+    if pos + n != len(raw):
+        raise ValueError("KTX: the texels do not end the file")
+    return np.frombuffer(raw, dtype=np.uint8, count=n, offset=pos).reshape(h, w, 4).copy()
+
+
 def read_tga(raw: bytes) -> np.ndarray:
     """RGBA8 (h, w, 4) from a TGA file, read as FasTC's loader reads it
     (ImageLoaderTGA::ReadData, IO/src/ImageLoaderTGA.cpp:35-48, over
@@ -226,8 +263,8 @@ def read_tga(raw: bytes) -> np.ndarray:
 
 
 def load_image(path: str, width: int = 0, height: int = 0) -> np.ndarray:
-    """RGBA8 (h, w, 4) from .png, .tga, .npy or raw RGBA (.rgba, needs
-    width/height)."""
+    """RGBA8 (h, w, 4) from .png, .tga, uncompressed .ktx, .npy or raw RGBA
+    (.rgba, needs width/height)."""
     if path.endswith(".npy"):
         img = np.load(path)
     elif path.endswith(".rgba") or path.endswith(".raw"):
@@ -237,6 +274,9 @@ def load_image(path: str, width: int = 0, height: int = 0) -> np.ndarray:
     elif path.endswith(".tga"):
         with open(path, "rb") as f:
             img = read_tga(f.read())
+    elif path.endswith(".ktx"):
+        with open(path, "rb") as f:
+            img = read_ktx_image(f.read())
     else:
         with open(path, "rb") as f:
             img = read_png(f.read())

@@ -423,6 +423,24 @@ class Reference:
         lib.ref_load_tga(raw, len(raw), _ptr(out), out.size, C.byref(w), C.byref(h))
         return out
 
+    def load_ktx(self, raw: bytes):
+        """The RGBA8 (h, w, 4) texels FasTC's KTX loader reads from an
+        uncompressed file; "compressed" for a file it loads as a
+        CompressedImage; None when it refuses the file."""
+        lib = self.lib
+        lib.ref_load_ktx.argtypes = [C.c_char_p, C.c_int32, _u8p, C.c_uint64,
+                                     C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        lib.ref_load_ktx.restype = C.c_int64
+        w, h = C.c_uint32(0), C.c_uint32(0)
+        n = lib.ref_load_ktx(raw, len(raw), None, 0, C.byref(w), C.byref(h))
+        if n == 0:
+            return None
+        if n < 0:
+            return "compressed"
+        out = np.zeros((h.value, w.value, 4), dtype=np.uint8)
+        lib.ref_load_ktx(raw, len(raw), _ptr(out), out.size, C.byref(w), C.byref(h))
+        return out
+
     def box_selection(self, px: np.ndarray, metric=0):
         px = np.ascontiguousarray(px, dtype=np.uint32)
         out = np.zeros(4, dtype=np.uint32)

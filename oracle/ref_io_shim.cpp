@@ -12,6 +12,9 @@
 //   * ref_ktx     -> the KTX file tc writes for `-d out.ktx`
 //                    (CLTool/src/tc.cpp:336-337 -> IO/src/ImageFile.cpp:132-160
 //                    -> ImageWriterKTX::WriteImage, IO/src/ImageWriterKTX.cpp:69-161)
+//   * ref_load_ktx -> the texels tc compresses for an uncompressed .ktx input
+//                    (ImageLoaderKTX::LoadImage / ReadData,
+//                    IO/src/ImageLoaderKTX.cpp:108-346)
 //   * ref_load_tga -> the texels tc compresses for a .tga input
 //                    (ImageLoaderTGA::ReadData, IO/src/ImageLoaderTGA.cpp:35-48,
 //                    over IO/third_party/tga/targa.c, then ImageLoader::LoadImage,
@@ -37,6 +40,7 @@
 #include "FasTC/ASTCCompressor.h"
 #include "FasTC/ETCCompressor.h"
 #include "FasTC/PVRTCCompressor.h"
+#include "ImageLoaderKTX.h"
 #include "ImageLoaderTGA.h"
 #include "ImageWriterKTX.h"
 
@@ -89,6 +93,31 @@ int64_t ref_load_tga(const uint8_t *data, int32_t n, uint8_t *out, uint64_t cap,
   ImageLoaderTGA loader(data, n);
   FasTC::Image<> *img = loader.LoadImage();
   if (!img) return 0;
+  *w = img->GetWidth();
+  *h = img->GetHeight();
+  const uint64_t texels = (uint64_t)*w * *h;
+  if (4 * texels <= cap)
+    for (uint64_t i = 0; i < texels; i++) {
+      const uint32 p = img->GetPixels()[i].Pack();
+      memcpy(out + 4 * i, &p, 4);
+    }
+  delete img;
+  return static_cast<int64_t>(texels);
+}
+
+// Loads a KTX file with FasTC's loader: returns the texel count with *w, *h
+// set (RGBA8 texels written to out when cap holds them) for an uncompressed
+// file, -1 for a compressed one (a CompressedImage), 0 when the loader
+// refuses the file.
+int64_t ref_load_ktx(const uint8_t *data, int32_t n, uint8_t *out, uint64_t cap, uint32_t *w,
+                     uint32_t *h) {
+  ImageLoaderKTX loader(data, n);
+  FasTC::Image<> *img = loader.LoadImage();
+  if (!img) return 0;
+  if (dynamic_cast<CompressedImage *>(img)) {
+    delete img;
+    return -1;
+  }
   *w = img->GetWidth();
   *h = img->GetHeight();
   const uint64_t texels = (uint64_t)*w * *h;

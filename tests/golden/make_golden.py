@@ -192,6 +192,56 @@ def make_tga(ref, manifest):
         print(name, "refused")
 
 
+# Uncompressed KTX inputs as FasTC's tc loads them (ImageLoaderKTX): name ->
+# (image, integer byte order, key/value block, mipmap levels, glType,
+# trailing bytes). FasTC reads the first two and refuses the next three;
+# the last is a compressed (BPTC) file, which it loads as blocks.
+KTX_IN = {
+    "ktxin_le": ("tile_mix(14, 20, 12)", "<", True, 1, 0x1400, b""),
+    "ktxin_be": ("tile_mix_radial_alpha(15, 16, 8, 7, 7)", ">", False, 1, 0x1400, b""),
+    "ktxin_mips2": ("tile_mix(16, 8, 8)", "<", True, 2, 0x1400, b""),
+    "ktxin_trailing": ("tile_mix(17, 8, 8)", "<", True, 1, 0x1400, b"\0\0\0\0"),
+    "ktxin_ubyte": ("tile_mix(18, 8, 8)", "<", True, 1, 0x1401, b""),
+}
+
+
+def ktx_rgba_file(img: np.ndarray, order: str, kv: bool, mips: int, gl_type: int, tail: bytes) -> bytes:
+    """An uncompressed RGBA8 KTX file laid out as FasTC's ImageWriterKTX
+    writes one (IO/src/ImageWriterKTX.cpp:116-123, 127-160), with the given
+    integer byte order, mipmap count, glType and trailing bytes."""
+    h, w = img.shape[:2]
+    kvb = b""
+    if kv:
+        body = b"KTXorientation\0S=r,T=d\0"
+        kvb = struct.pack(order + "I", len(body)) + body
+        kvb += b"K" * (-len(kvb) % 4)
+    words = (0x04030201, gl_type, 1, 0x1908, 0x8058, 0x1908, w, h, 0, 0, 1, mips, len(kvb))
+    ident = bytes([0xAB, 0x4B, 0x54, 0x58, 0x20, 0x31, 0x31, 0xBB, 0x0D, 0x0A, 0x1A, 0x0A])
+    return (ident + struct.pack(order + "13I", *words) + kvb + struct.pack(order + "I", w * h * 4) +
+            np.ascontiguousarray(img).tobytes() + tail)
+
+
+def make_ktx_in(ref, manifest):
+    manifest["ktx_in"] = {}
+    files = {name: ktx_rgba_file(make(expr), *rest) for name, (expr, *rest) in KTX_IN.items()}
+    bptc = np.fromfile(os.path.join(HERE, "tile_q0.bin"), np.uint8)
+    from fastc_gb300 import imageio
+    files["ktxin_compressed"] = imageio.ktx_bytes(bptc, 128, 128)
+    for name, raw in files.items():
+        with open(os.path.join(HERE, name + ".ktx"), "wb") as f:
+            f.write(raw)
+        got = ref.load_ktx(raw)
+        e = {"file_sha256": hashlib.sha256(raw).hexdigest()}
+        if got is None:
+            e["refused"] = True
+        elif isinstance(got, str):
+            e["compressed"] = True
+        else:
+            e.update(width=int(got.shape[1]), height=int(got.shape[0]), decoded_sha256=sha(got))
+        manifest["ktx_in"][name] = e
+        print(name, e)
+
+
 def dxt_random_blocks(w: int, h: int, fmt: int, seed: int) -> np.ndarray:
     n = ((w + 3) // 4) * ((h + 3) // 4) * (8 if fmt == 1 else 16)
     return np.random.default_rng(seed).integers(0, 256, n, dtype=np.uint8)
@@ -346,7 +396,7 @@ def main():
     ap.add_argument("--dxt-only", action="store_true",
                     help="only (re)write the DXT1 / DXT5 fixtures")
     ap.add_argument("--tc-only", action="store_true",
-                    help="only (re)write tc's PSNR values, the KTX and the TGA fixtures")
+                    help="only (re)write tc's PSNR values and the KTX and TGA fixtures")
     ap.add_argument("--workers", type=int, default=6)
     args = ap.parse_args()
     if not O.build_ref(args.reference):
@@ -363,6 +413,7 @@ def main():
         elif args.tc_only:
             make_tc(ref, manifest)
             make_tga(ref, manifest)
+            make_ktx_in(ref, manifest)
         else:
             make_full_size(manifest, args.workers)
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
@@ -402,6 +453,7 @@ def main():
     make_dxt(ref, manifest)
     make_tc(ref, manifest)
     make_tga(ref, manifest)
+    make_ktx_in(ref, manifest)
     make_full_size(manifest, args.workers)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)

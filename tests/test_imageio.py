@@ -136,3 +136,37 @@ def test_tga_reads_as_fasTC_loader(manifest, name):
     assert img.shape == (e["height"], e["width"], 4) and img.dtype == np.uint8
     assert hashlib.sha256(img.tobytes()).hexdigest() == e["decoded_sha256"]
     assert np.array_equal(imageio.load_image(path), img)
+
+
+def _ktx_in_names():
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(__file__), "golden", "manifest.json")) as f:
+        return sorted(json.load(f)["ktx_in"])
+
+
+@pytest.mark.parametrize("name", _ktx_in_names())
+def test_uncompressed_ktx_reads_as_fasTC_loader(manifest, name):
+    """Uncompressed KTX inputs give the texels FasTC's tc loads from them
+    (ImageLoaderKTX: either byte order, key/value data skipped, texels in
+    file order), the files it refuses are refused, and a compressed file
+    (which FasTC loads as blocks) is refused as an input to compress."""
+    import hashlib
+    import os
+
+    from fastc_gb300 import imageio
+
+    e = manifest["ktx_in"][name]
+    path = os.path.join(os.path.dirname(__file__), "golden", name + ".ktx")
+    with open(path, "rb") as f:
+        raw = f.read()
+    assert hashlib.sha256(raw).hexdigest() == e["file_sha256"]
+    if e.get("refused") or e.get("compressed"):
+        with pytest.raises(ValueError):
+            imageio.read_ktx_image(raw)
+        return
+    img = imageio.read_ktx_image(raw)
+    assert img.shape == (e["height"], e["width"], 4)
+    assert hashlib.sha256(img.tobytes()).hexdigest() == e["decoded_sha256"]
+    assert np.array_equal(imageio.load_image(path), img)
