@@ -16,8 +16,8 @@ compression; "Compression time: %.3f ms" (the mean) is printed before the PSNR, 
 the GPU. -l runs CompressWithStats with a log stream and writes FasTC's
 per-block log to <basename>.log (for DXT the log stays empty, as FasTC's
 does: it has no logging DXT encoder); ETC1 and PVRTC are refused.
-Inputs: PNG (8-bit), TGA (as FasTC's loader reads it), .npy RGBA8 arrays, raw
-RGBA (.rgba/.raw with -s WxH).
+Inputs: PNG (8-bit), TGA and uncompressed KTX (as FasTC's loaders read them),
+.npy RGBA8 arrays, raw RGBA (.rgba/.raw with -s WxH).
 """
 from __future__ import annotations
 
