@@ -238,6 +238,8 @@ def make_ktx_in(ref, manifest):
             e["compressed"] = True
         else:
             e.update(width=int(got.shape[1]), height=int(got.shape[0]), decoded_sha256=sha(got))
+            blocks = ref.compress(got, steps=0)  # what `tc -q 0` makes of the file
+            e.update(q0_blocks_sha256=sha(blocks), q0_tc_psnr=ref.tc_psnr(got, blocks, 7))
         manifest["ktx_in"][name] = e
         print(name, e)
 

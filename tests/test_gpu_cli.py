@@ -113,18 +113,20 @@ def test_tc_dxt_to_ktx_and_png(gpu, port, tmp_path, capsys, monkeypatch, fmt):
     assert (tmp_path / "dxt_in.log").read_text() == ""
 
 
-@pytest.mark.parametrize("name", ["tga24_raw", "tga32_rle", "tga16_raw"])
-def test_tc_tga_input_gives_fasTC_output(gpu, manifest, tmp_path, capsys, name):
-    """`tc -q 0 -d out.ktx file.tga`: the blocks FasTC's tc writes for the
-    texels its loader reads, and its PSNR line."""
+@pytest.mark.parametrize("group,name,ext", [("tga", "tga24_raw", ".tga"), ("tga", "tga32_rle", ".tga"),
+                                            ("tga", "tga16_raw", ".tga"), ("ktx_in", "ktxin_le", ".ktx"),
+                                            ("ktx_in", "ktxin_be", ".ktx")])
+def test_tc_tga_and_ktx_input_gives_fasTC_output(gpu, manifest, tmp_path, capsys, group, name, ext):
+    """`tc -q 0 -d out.ktx file.tga|file.ktx`: the blocks FasTC's tc writes
+    for the texels its loader reads, and its PSNR line."""
     import os
     import shutil
 
     from fastc_gb300 import imageio, tc
 
-    e = manifest["tga"][name]
-    src = tmp_path / (name + ".tga")
-    shutil.copy(os.path.join(os.path.dirname(__file__), "golden", name + ".tga"), src)
+    e = manifest[group][name]
+    src = tmp_path / ("in_" + name + ext)
+    shutil.copy(os.path.join(os.path.dirname(__file__), "golden", name + ext), src)
     out = tmp_path / "out.ktx"
     assert tc.main(["-q", "0", "-d", str(out), str(src)]) == 0
     blocks, w, h = imageio.read_ktx(out.read_bytes())
